@@ -1,0 +1,372 @@
+#!/usr/bin/env python3
+"""Benchmark of the MESSI likelihood hot path on GB300.
+
+One step = one structure-integrated likelihood evaluation (what every NLopt
+objective and every MCMC proposal of the reference runs,
+src/FARCE.jl:2322-2345): unpaired column likelihoods, 16-state pair pruning
+over every column pair within the span limit for all 45 categories, gap
+masking and the banded KH99 inside pass to Z.  Workload: seeded synthetic
+alignment of 64 sequences x 1,000 nt, max pair span 500 (374,750 pairs).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``value`` is site-pair likelihoods/s with the alignment
+resident in HBM (CUDA events on the library's stream, L2 flushed between
+steps); ``e2e`` runs the reference-facing call chain (felsensteincuda ->
+maskgapped -> computeinsideKH99, src/MESSI.jl:305-311) with host buffers.
+``--impl reference`` times the FP64 CPU restatement of the reference's CPU
+path (oracle/) on this host's cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "site-pair likelihoods/s"
+UNIT = "pairs/s"
+WORKLOAD = "c2"
+BYTES_PER_UPDATE = 212  # algorithmic bytes of one node update (2 child rows + exps + indices in, 1 row out)
+# DRAM bytes per node update of prune_level_kernel from an ncu capture
+# (profiles/prune_level_kernel_c2.md); None until captured.
+TRAFFIC_BYTES_PER_UPDATE = None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms",
+                                          "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_params(s, count, seed):
+    """`count` parameter vectors around the workload's generating vector (the
+    moves an MCMC chain makes); discretised on the host like getparams."""
+    import numpy as np
+
+    from messi_gb300 import model as M
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        p = s.params15.copy()
+        p[0:3] = np.clip(p[0:3] * np.exp(rng.normal(0, 0.02, 3)), 1.0, 50.0)
+        p[3:9] = p[3:9] * np.exp(rng.normal(0, 0.02, 6))
+        out.append(M.getparams(p, s.dataset.branchlengths))
+    return out
+
+
+def cpu_oracle_rate(s, rows, nthreads):
+    """FP64 CPU restatement timed on a bounded sample: pair pruning for a block
+    of rows, plus the full unpaired and inside passes pro-rated to the sample."""
+    import numpy as np
+
+    from oracle import c_oracle as co
+    from oracle import model_ref as mr
+    ds = s.dataset
+    rp = mr.getparams(s.params15, ds.branchlengths)
+    P, pi16, logw, *_ = mr.pair_categories(rp)
+    t0 = time.perf_counter()
+    u, _ = mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
+    t_unp = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p, _ = co.pair_matrix(ds.children, ds.seqindex, ds.masks, P, pi16, logw, s.W, rows=rows, nthreads=nthreads)
+    t_pairs = time.perf_counter() - t0
+    sample = int(np.isfinite(p[np.triu_indices(ds.numcols, 1)]).sum())
+    return u, t_unp, t_pairs, sample
+
+
+def cpu_inside_time(u, W, L, nthreads):
+    import numpy as np
+
+    from oracle import c_oracle as co
+    rng = np.random.default_rng(0)
+    p = np.full((L, L), -np.inf)
+    for i in range(L):
+        j = np.arange(i + 1, min(L, i + W + 1))
+        p[i, j] = u[i] + u[j] + rng.normal(-3, 4, len(j))
+    p = np.triu(p, 1)
+    p = p + p.T
+    p[np.tril_indices(L)] = -np.inf
+    p = np.maximum(p, p.T)
+    t0 = time.perf_counter()
+    co.inside(u, p, 1.0, nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+def total_pairs(L, W):
+    return sum(min(W, L - 1 - x) for x in range(L))
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from messi_gb300 import synth
+    s = synth.make_workload(WORKLOAD, seed=1)
+    L, W = s.dataset.numcols, s.W
+    npairs = total_pairs(L, W)
+    nthreads = os.cpu_count() or 1
+    rows_per_step = 16
+    u, t_unp, _, _ = cpu_oracle_rate(s, (0, 1), nthreads)
+    t_in = cpu_inside_time(u, W, L, nthreads)
+    times, samples = [], []
+    for k in range(args.warmup + args.steps):
+        x0 = (k * rows_per_step) % (L - rows_per_step)
+        _, _, t_pairs, sample = cpu_oracle_rate(s, (x0, x0 + rows_per_step), nthreads)
+        frac = sample / npairs
+        if k >= args.warmup:
+            times.append(t_pairs + (t_unp + t_in) * frac)
+            samples.append(sample)
+    value = sum(samples) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD}: 64 seqs x 1,000 nt, max pair span 500, 45 categories",
+                   "pairs_per_full_step": npairs},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{rows_per_step} alignment rows of pairs per step (~{int(statistics.mean(samples))} "
+                                   f"pairs) with the unpaired and inside passes pro-rated by pair fraction"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from messi_gb300 import api, synth
+
+    s = synth.make_workload(WORKLOAD, seed=1 + rank)
+    ds = s.dataset
+    L, W = ds.numcols, s.W
+    npairs = total_pairs(L, W)
+    params = make_params(s, args.warmup + args.steps, seed=rank)
+    ctx = api.get_context(local)
+    h = ctx.dataset(ds, W)
+    stats = h.stats()
+    margs = [api.ModelArgs(p) for p in params]
+    gf = np.ascontiguousarray(ds.gapfrequency, np.float64)
+
+    import ctypes
+    Zc = ctypes.c_double()
+
+    def step(m):
+        ctx.check(ctx.lib.messi_likelihood(ctx.handle, h.handle, ctypes.byref(m.struct),
+                                           gf.ctypes.data_as(ctypes.c_void_p), 1.0, ctypes.byref(Zc), None),
+                  "messi_likelihood")
+        return ctx.last_launches()
+
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for k in range(args.warmup):
+        step(margs[k])
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- timed region: K steps, L2 flushed between steps (outside the events)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches = 0
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t_wall = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev[k][0].record(stream)
+            launches += step(margs[args.warmup + k])
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier()
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = ws * npairs * args.steps / (ms / 1e3)
+
+    # ---- kernel-level timing pass (event pairs around each pruning launch)
+    ctx.profile(True)
+    nprof = min(args.steps, 5)
+    for k in range(nprof):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step(margs[args.warmup + k])
+    p_ms, p_n, p_units = ctx.profile_read(0)
+    i_ms, i_n, i_cells = ctx.profile_read(1)
+    s_ms, s_n, s_cells = ctx.profile_read(2)
+    ctx.profile(False)
+    peak, peak_kind = measured_peaks()
+    achieved = (p_units * BYTES_PER_UPDATE / 1e9) / (p_ms / 1e3) if p_ms > 0 else None
+    units_per_launch = p_units / p_n if p_n else None
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": (achieved / peak) if achieved else None,
+        "traffic": (TRAFFIC_BYTES_PER_UPDATE * units_per_launch) if (TRAFFIC_BYTES_PER_UPDATE and units_per_launch)
+        else None,
+        "kernel": "prune_level_kernel", "peak_source": f"{peak_kind} hbm_gbs",
+        "bytes_per_unit": BYTES_PER_UPDATE, "unit_name": "node update (pair x category x internal node)",
+        "units_per_launch": units_per_launch, "launches": p_n, "avg_launch_ms": p_ms / p_n if p_n else None,
+        "kernel_ms_per_step": p_ms / nprof,
+    }
+    inside_ms = (i_ms + s_ms) / nprof
+    band_cells = sum(L - d for d in range(W + 1)) + max(0, L - 1 - W)
+
+    # ---- e2e: the reference-facing call chain with host buffers
+    ne2e = min(args.steps, 5)
+    t_e2e = []
+    for k in range(ne2e):
+        prm = params[args.warmup + k]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u = api.computeunpairedlikelihoods(ds, prm, ctx=ctx)
+        mat, _ = api.felsensteincuda(ds, prm, None, W, ctx=ctx)
+        api.maskgapped(mat, ds.gapfrequency, 1.0, -np.inf)
+        api.computeinsideKH99(u, mat, ctx=ctx)
+        t_e2e.append(time.perf_counter() - t0)
+    model_bytes = (45 * (16 + 256 + 16) + 3 * (4 + 16 + 4) + 45 * 3 + 3 + 4 + ds.numnodes) * 8 + 45 * 16 * 4
+    h2d = 2 * model_bytes + L * L * 8 + L * 8
+    d2h = L * 8 + L * L * 8 + 8
+    e2e_value = ws * npairs / statistics.mean(t_e2e)
+
+    # ---- CPU baseline (rank 0, single process)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        rows = 24
+        u_c, t_unp, t_pairs, sample = cpu_oracle_rate(s, (0, rows), nthreads)
+        t_in = cpu_inside_time(u_c, W, L, nthreads)
+        t_full = t_pairs * npairs / sample + t_unp + t_in
+        cpu = {"value": npairs / t_full, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"pairs of the first {rows} alignment rows ({sample} pairs, {t_pairs:.1f} s) extrapolated "
+                         f"to {npairs} pairs, plus full unpaired ({t_unp:.2f} s) and inside ({t_in:.1f} s) passes"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD}: 64 seqs x 1,000 nt, max pair span 500, 45 categories "
+                               "(3 x 3 site rates x 5 lambda), 30% paired, 5% gaps",
+                   "pairs_per_step": npairs, "step": "unpaired + pair pruning + gap mask + banded inside -> Z",
+                   "l2": "flushed between steps (256 MB write outside the timed events)",
+                   "parallelism": f"replicas x{ws}", "plan": stats},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "chain": "computeunpairedlikelihoods + felsensteincuda + maskgapped + computeinsideKH99"},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "inside": {"cells_per_s": band_cells / (inside_ms / 1e3) if inside_ms > 0 else None,
+                   "band_cells": band_cells, "full_triangle_cells": L * (L + 1) // 2,
+                   "ms_per_pass": inside_ms, "launches_per_pass": (i_n + s_n) / nprof},
+        "wall_ms_per_step": 1e3 * t_wall / args.steps,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,166 @@
+/*
+ * messi_gb300.h -- C ABI of the GB300 (sm_103a) implementation of MESSI's
+ * likelihood hot path: 16-state site-pair pruning (HP1) and the KH99 SCFG
+ * inside/outside passes with base-pairing posteriors (HP2).
+ *
+ * Every entry point returns MESSI_OK (0) or a negative status; there is no
+ * CPU fallback.  Host buffers are caller-owned and copied in/out inside the
+ * call.  Calls on one context are serialised on the context's CUDA stream and
+ * are not re-entrant across threads.
+ *
+ * Conventions (those of the reference's Julia arrays):
+ *   - matrices are column-major: element (i, j) of an L x L matrix is at
+ *     i + j*L; element (X, i, j) of a 3 x L x L table is at X + 3*(i + L*j),
+ *     X: 0 = S, 1 = F, 2 = L (src/InsideOutsideAlgorithm.jl:40-53);
+ *   - impossible events are -Inf on input and output;
+ *   - the tree is rooted and binary, nodes numbered in pre-order with the
+ *     root = 0 (src/Tree.jl:190-208); branch length n is the branch above
+ *     node n;
+ *   - nucleotide masks: bit 0 = A, 1 = C, 2 = G, 3 = U/T; 15 = gap
+ *     (src/Dataset.jl:13-96); the 16-state pair index is 4*first + second.
+ */
+#ifndef MESSI_GB300_H
+#define MESSI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MESSI_OK 0
+#define MESSI_EINVAL -1   /* invalid argument */
+#define MESSI_ENOMEM -2   /* device or host allocation failed */
+#define MESSI_ECUDA -3    /* a CUDA call failed */
+#define MESSI_ETIMEOUT -4 /* a bounded device-side wait gave up */
+#define MESSI_ESTATE -5   /* object used in the wrong state */
+
+typedef struct messi_ctx messi_ctx;
+typedef struct messi_dataset messi_dataset;
+
+/* Alignment and rooted binary tree: the inputs of src/Dataset.jl:121-198. */
+typedef struct {
+    int32_t numseqs;
+    int32_t numcols;
+    int32_t numnodes;          /* 2*numseqs - 1 */
+    const uint8_t* masks;      /* [numseqs][numcols] nucleotide masks, row-major */
+    const int32_t* children;   /* [numnodes][2], -1 for leaves */
+    const int32_t* seqindex;   /* [numnodes], row of `masks` for leaves, -1 otherwise */
+} messi_alignment;
+
+/* Substitution-model parameters after discretisation (the fields of
+ * ModelParameters / MuseSpecificParameters, src/FARCE.jl:461-503, 699-727). */
+typedef struct {
+    double freqs[4];             /* nucleotide frequencies A, C, G, U */
+    double q[6];                 /* GTR exchangeabilities q1..q6 */
+    const double* branchlengths; /* [numnodes] */
+    int32_t nsite;               /* site-rate categories */
+    const double* siteRates;     /* [nsite] */
+    const double* siteWeights;   /* [nsite] */
+    int32_t nlambda;             /* coevolution categories */
+    const double* lambdaGC;      /* [nlambda] multipliers (1 + lambdarate) */
+    const double* lambdaAT;
+    const double* lambdaGT;
+    const double* lambdaWeights; /* [nlambda] */
+} messi_model;
+
+/* Human-readable text of a status code. */
+const char* messi_strerror(int status);
+
+/* Library version: major*10000 + minor*100 + patch. */
+int messi_version(void);
+
+/* Context: one CUDA device and one stream.  Replaces the per-call
+ * CuContext(CuDevice(0)) / destroy! pairs of src/FelsensteinCUDA.jl:240-241,506
+ * and src/InsideCUDA.jl:96-97,133. */
+int messi_ctx_create(int device, messi_ctx** ctx);
+int messi_ctx_destroy(messi_ctx* ctx);
+/* The context's cudaStream_t (as void*), for event timing by callers. */
+int messi_ctx_stream(messi_ctx* ctx, void** stream);
+/* Number of kernel launches issued by the last call on this context. */
+int messi_ctx_last_launches(messi_ctx* ctx, int64_t* launches);
+/* Text of the last error recorded on this context. */
+const char* messi_ctx_last_error(messi_ctx* ctx);
+
+/* Per-kernel timing (instrumentation; no counterpart in the reference).
+ * enable != 0 records a CUDA event pair around each launch of the timed
+ * kernel families on the context's stream and resets the counters.
+ * kernel: 0 = pair node update (every tree level), 1 = inside span diagonals,
+ * 2 = inside suffix column, 3 = outside span diagonals.  units = node updates
+ * (kernel 0) or cells (kernels 1-3) processed by the timed launches. */
+int messi_ctx_profile(messi_ctx* ctx, int enable);
+int messi_ctx_profile_read(messi_ctx* ctx, int kernel, double* total_ms, int64_t* launches, double* units);
+
+/* Dataset handle: uploads the alignment and builds the per-node pair plan
+ * (column-pattern compression and unique pair lists).  Replaces
+ * getindexdict + its process-global cache, src/FelsensteinCUDA.jl:77-142,
+ * 210-238, and Dataset.subcolumnrefs, src/Dataset.jl:180-196.
+ *   maxbasepairdistance: pairs with y - x > W are not evaluated (-Inf).
+ *   pairmask: optional L x L bytes, non-zero = evaluate (the
+ *             dataset.maxbasepairprobs[x,y] > 0 test, src/FelsensteinCUDA.jl:91). */
+int messi_dataset_create(messi_ctx* ctx, const messi_alignment* aln, int32_t maxbasepairdistance,
+                         const uint8_t* pairmask, messi_dataset** ds);
+int messi_dataset_destroy(messi_dataset* ds);
+/* Plan statistics: out[0] pairs in band, [1] unique root pairs, [2] node
+ * updates per category executed (sum over internal nodes of unique pairs),
+ * [3] naive node updates per category (pairs x internal nodes), [4] tree
+ * levels, [5] partial-buffer rows per category, [6] categories per pass.
+ * n = number of entries wanted (<= 7). */
+int messi_dataset_stats(messi_dataset* ds, int64_t* out, int32_t n);
+
+/* felsensteincuda (src/FelsensteinCUDA.jl:214-516): pair log-likelihoods
+ * mixed over all nsite*nsite*nlambda categories.
+ *   pairedlogprobs: [L x L] output, symmetric, -Inf outside band/mask and on
+ *                   the diagonal.
+ *   museconditionals: optional [nlambda][L x L] per-lambda-category mixtures
+ *                   (keepmuseconditionals, src/FelsensteinCUDA.jl:387-398). */
+int messi_felsenstein_pairs(messi_ctx* ctx, messi_dataset* ds, const messi_model* model,
+                            double* pairedlogprobs, double* museconditionals);
+
+/* computeunpairedlikelihoods(dataset, params) (src/FARCE.jl:1198-1220):
+ * per-column log-likelihood mixed over site-rate categories.  [L] output. */
+int messi_unpaired(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, double* unpairedlogprobs);
+
+/* computeinsideKH99 (src/InsideCUDA.jl:23-53): KH99 inside pass.
+ *   maxspan: largest pair span to consider; < 0 infers it from `paired`
+ *            (the largest j - i with a finite entry).  The result equals the
+ *            unbanded pass whenever every pair beyond maxspan is -Inf.
+ *   B:       exponent on rule and emission terms (1.0 in every caller).
+ *   Z:       log marginal likelihood (scalar output).
+ *   inside:  optional [3 x L x L] table.  Cells with span > maxspan are
+ *            -Inf except S on the last column (the only ones Z uses). */
+int messi_inside(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,
+                 double B, double* Z, double* inside);
+
+/* computeoutsideKH99 (src/InsideCUDA.jl:55-61): outside pass from a host
+ * inside table.  [3 x L x L] output (same band convention as messi_inside). */
+int messi_outside(messi_ctx* ctx, int32_t L, const double* inside, const double* unpaired,
+                  const double* paired, int32_t maxspan, double* outside);
+
+/* computebasepairprobs (src/InsideOutsideAlgorithm.jl:486-533) from host
+ * inside/outside tables: row-normalised unpaired [L] and pair [L x L]
+ * posteriors. */
+int messi_basepairprobs(messi_ctx* ctx, int32_t L, const double* inside, const double* outside,
+                        const double* unpaired, const double* paired, int32_t maxspan, double* single,
+                        double* pairprobs);
+
+/* Inside -> outside -> posteriors in one device-resident call (the
+ * computeinsideKH99(zonly=false) / computeoutsideKH99 / computebasepairprobs
+ * chain of src/MESSI.jl:1101-1103).  Z optional. */
+int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,
+                     double* Z, double* single, double* pairprobs);
+
+/* computestructureintegratedlikelihood without the prior
+ * (src/FARCE.jl:2322-2345, with maskgapped! as at src/MESSI.jl:310): unpaired
+ * likelihoods, pair pruning, gap masking and the inside pass, all on the
+ * device.  gapfrequency: [L]; columns with gapfrequency >= gapcutoff cannot
+ * pair.  Z: log marginal likelihood.  unpaired: optional [L] output. */
+int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const double* gapfrequency,
+                     double gapcutoff, double* Z, double* unpaired);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESSI_GB300_H */

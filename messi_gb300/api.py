@@ -1,0 +1,302 @@
+"""Reference-named host API over the C ABI.
+
+Each function keeps the name, argument meaning and return value of the Julia
+function it replaces (see the citations); the work runs in libmessi_gb300.so
+on the GPU.  There is no CPU fallback: ``usecuda=False`` raises.
+
+Matrices come back as Fortran-ordered numpy arrays (Julia's layout), so
+``inside[X, i, j]`` and ``pairedlogprobs[x, y]`` index them like the
+reference's arrays (0-based).
+"""
+import ctypes
+import hashlib
+import threading
+
+import numpy as np
+
+from . import _lib
+from .model import computeprior, getmusespecificparamsarray
+
+_tls = threading.local()
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """One CUDA device and stream (replaces CuContext(CuDevice(0)) per call,
+    src/FelsensteinCUDA.jl:240-241, src/InsideCUDA.jl:96-97)."""
+
+    def __init__(self, device=0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.messi_ctx_create(int(device), ctypes.byref(h)), "messi_ctx_create")
+        self.handle = h
+        self.device = device
+        self._datasets = {}
+
+    def close(self):
+        for ds in list(self._datasets.values()):
+            ds.close()
+        self._datasets.clear()
+        if self.handle:
+            self.lib.messi_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _lib.check(self.lib.messi_ctx_stream(self.handle, ctypes.byref(s)), "messi_ctx_stream")
+        return s.value
+
+    def last_launches(self):
+        n = ctypes.c_int64()
+        _lib.check(self.lib.messi_ctx_last_launches(self.handle, ctypes.byref(n)), "messi_ctx_last_launches")
+        return n.value
+
+    def profile(self, enable=True):
+        """Enable (and reset) per-kernel CUDA-event timing."""
+        self.check(self.lib.messi_ctx_profile(self.handle, 1 if enable else 0), "messi_ctx_profile")
+
+    def profile_read(self, kernel):
+        """(total_ms, launches, units) for kernel family 0 = pair node update,
+        1 = inside diagonals, 2 = inside suffix, 3 = outside diagonals."""
+        ms, n, units = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        self.check(self.lib.messi_ctx_profile_read(self.handle, int(kernel), ctypes.byref(ms), ctypes.byref(n),
+                                                   ctypes.byref(units)), "messi_ctx_profile_read")
+        return ms.value, n.value, units.value
+
+    def check(self, status, what):
+        _lib.check(status, what, self.handle)
+
+    def dataset(self, dataset, maxbasepairdistance=1000000, pairmask=None):
+        """Cached dataset handle (the reference caches its pair index in
+        process globals, src/FelsensteinCUDA.jl:206-238; here the cache key is
+        the dataset, the band and the pair mask)."""
+        W = int(min(max(1, maxbasepairdistance), max(1, dataset.numcols - 1)))
+        mkey = None if pairmask is None else hashlib.sha1(np.ascontiguousarray(pairmask, np.uint8)).hexdigest()
+        key = (id(dataset), W, mkey)
+        h = self._datasets.get(key)
+        if h is None or h.dataset is not dataset:
+            h = DatasetHandle(self, dataset, W, pairmask)
+            self._datasets[key] = h
+        return h
+
+
+def get_context(device=0):
+    ctxs = getattr(_tls, "ctxs", None)
+    if ctxs is None:
+        ctxs = _tls.ctxs = {}
+    c = ctxs.get(device)
+    if c is None:
+        c = ctxs[device] = Context(device)
+    return c
+
+
+class DatasetHandle:
+    def __init__(self, ctx, dataset, W, pairmask=None):
+        self.ctx = ctx
+        self.dataset = dataset
+        self.W = W
+        self._masks = np.ascontiguousarray(dataset.masks, np.uint8)
+        self._children = np.ascontiguousarray(dataset.children, np.int32)
+        self._seqindex = np.ascontiguousarray(dataset.seqindex, np.int32)
+        aln = _lib.Alignment(dataset.numseqs, dataset.numcols, dataset.numnodes, _p(self._masks), _p(self._children),
+                             _p(self._seqindex))
+        pm = None if pairmask is None else np.asfortranarray(pairmask, np.uint8)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.messi_dataset_create(ctx.handle, ctypes.byref(aln), int(W), _p(pm), ctypes.byref(h)),
+                  "messi_dataset_create")
+        self.handle = h
+
+    def stats(self):
+        out = np.zeros(7, np.int64)
+        self.ctx.check(self.ctx.lib.messi_dataset_stats(self.handle, _p(out), 7), "messi_dataset_stats")
+        keys = ("band_pairs", "unique_root_pairs", "executed_updates_per_category", "naive_updates_per_category",
+                "levels", "arena_rows", "categories_per_pass")
+        return dict(zip(keys, (int(x) for x in out)))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.messi_dataset_destroy(self.handle)
+            self.handle = None
+
+
+class ModelArgs:
+    """messi_model built from ModelParameters (+ museparams), arrays kept alive."""
+
+    def __init__(self, params, museparams=None, branchlengths=None):
+        if museparams is None:
+            museparams = getmusespecificparamsarray(params)
+        k = np.array([mp.lambdacat - 1 for mp in museparams], dtype=np.int64)
+        self.lGC = np.ascontiguousarray(np.asarray(params.lambdaratesGC, np.float64)[k] + 1.0)
+        self.lAT = np.ascontiguousarray(np.asarray(params.lambdaratesAT, np.float64)[k] + 1.0)
+        self.lGT = np.ascontiguousarray(np.asarray(params.lambdaratesGT, np.float64)[k] + 1.0)
+        self.lw = np.ascontiguousarray([mp.prob for mp in museparams], np.float64)
+        self.sr = np.ascontiguousarray(params.siteRates, np.float64)
+        self.sw = np.ascontiguousarray(params.siteWeights, np.float64)
+        bl = params.branchlengths if branchlengths is None else branchlengths
+        self.bl = np.ascontiguousarray(bl, np.float64)
+        m = _lib.Model()
+        for a in range(4):
+            m.freqs[a] = float(params.freqs[a])
+        for a, qv in enumerate(params.q):
+            m.q[a] = float(qv)
+        m.branchlengths = _p(self.bl)
+        m.nsite = len(self.sr)
+        m.siteRates = _p(self.sr)
+        m.siteWeights = _p(self.sw)
+        m.nlambda = len(self.lw)
+        m.lambdaGC, m.lambdaAT, m.lambdaGT = _p(self.lGC), _p(self.lAT), _p(self.lGT)
+        m.lambdaWeights = _p(self.lw)
+        self.struct = m
+
+
+def _need_cuda(flag):
+    if not flag:
+        raise NotImplementedError("messi_gb300 runs on the GPU only; there is no CPU path")
+
+
+# ---------------------------------------------------------------------------
+# HP1: pair pruning
+# ---------------------------------------------------------------------------
+def felsensteincuda(dataset, params, museparams=None, maxbasepairdistance=1000000, keepmuseconditionals=False,
+                    pairmask=None, ctx=None):
+    """src/FelsensteinCUDA.jl:214-516.  Returns (mat, ret): mat is the L x L
+    mixed pair log-likelihood matrix (-Inf outside the band and mask), ret the
+    per-lambda-category matrices when keepmuseconditionals."""
+    ctx = ctx or get_context()
+    h = ctx.dataset(dataset, maxbasepairdistance, pairmask)
+    m = ModelArgs(params, museparams)
+    L = dataset.numcols
+    mat = np.empty((L, L), order="F")
+    per = np.empty(len(m.lw) * L * L) if keepmuseconditionals else None
+    ctx.check(ctx.lib.messi_felsenstein_pairs(ctx.handle, h.handle, ctypes.byref(m.struct), _p(mat), _p(per)),
+              "messi_felsenstein_pairs")
+    ret = []
+    if keepmuseconditionals:
+        ret = [per[k * L * L:(k + 1) * L * L].reshape((L, L), order="F") for k in range(len(m.lw))]
+    return mat, ret
+
+
+def coevolutionall(dataset, params, parallel=True, keepmatrices=False, integratesiterates=True,
+                   maxbasepairdistance=1000000, usecuda=True):
+    """src/FARCE.jl:1736-1741 (the GPU branch)."""
+    _need_cuda(usecuda and integratesiterates)
+    return felsensteincuda(dataset, params, getmusespecificparamsarray(params), maxbasepairdistance, keepmatrices)
+
+
+def computeunpairedlikelihoods(dataset, params, ctx=None):
+    """src/FARCE.jl:1198-1220 (site-rate categories integrated)."""
+    ctx = ctx or get_context()
+    h = ctx.dataset(dataset)
+    m = ModelArgs(params)
+    u = np.empty(dataset.numcols)
+    ctx.check(ctx.lib.messi_unpaired(ctx.handle, h.handle, ctypes.byref(m.struct), _p(u)), "messi_unpaired")
+    return u
+
+
+def maskgapped(probs, gapfrequency, cutoff, v=0.0):
+    """src/RNATools.jl:441-451 (in place, host matrix)."""
+    g = np.asarray(gapfrequency) >= cutoff
+    probs[g, :] = v
+    probs[:, g] = v
+    return probs
+
+
+# ---------------------------------------------------------------------------
+# HP2: inside / outside / posteriors
+# ---------------------------------------------------------------------------
+def _f64c(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+def _f64f(a):
+    return np.asfortranarray(a, np.float64)
+
+
+def computeinsideKH99(unpairedlogprobs, pairedlogprobs, B=1.0, zonly=True, usecudain=True, maxspan=-1, ctx=None):
+    """src/InsideCUDA.jl:23-53.  Z when zonly, else the 3 x L x L table."""
+    _need_cuda(usecudain)
+    ctx = ctx or get_context()
+    u = _f64c(unpairedlogprobs)
+    p = _f64f(pairedlogprobs)
+    L = len(u)
+    Z = ctypes.c_double()
+    ins = None if zonly else np.empty((3, L, L), order="F")
+    ctx.check(ctx.lib.messi_inside(ctx.handle, L, _p(u), _p(p), int(maxspan), float(B), ctypes.byref(Z), _p(ins)),
+              "messi_inside")
+    return Z.value if zonly else ins
+
+
+def computeoutsideKH99(inside, unpairedlogprobs, pairedlogprobs, usecuda=True, maxspan=-1, ctx=None):
+    """src/InsideCUDA.jl:55-61."""
+    _need_cuda(usecuda)
+    ctx = ctx or get_context()
+    u = _f64c(unpairedlogprobs)
+    L = len(u)
+    out = np.empty((3, L, L), order="F")
+    ctx.check(ctx.lib.messi_outside(ctx.handle, L, _p(_f64f(inside)), _p(u), _p(_f64f(pairedlogprobs)),
+                                    int(maxspan), _p(out)), "messi_outside")
+    return out
+
+
+def computebasepairprobs(inside, outside, unpairedlogprobs, pairedlogprobs, grammar=None, maxspan=-1, ctx=None):
+    """src/InsideOutsideAlgorithm.jl:486-533: row-normalised posteriors."""
+    ctx = ctx or get_context()
+    u = _f64c(unpairedlogprobs)
+    L = len(u)
+    single = np.empty(L)
+    pair = np.empty((L, L), order="F")
+    ctx.check(ctx.lib.messi_basepairprobs(ctx.handle, L, _p(_f64f(inside)), _p(_f64f(outside)), _p(u),
+                                          _p(_f64f(pairedlogprobs)), int(maxspan), _p(single), _p(pair)),
+              "messi_basepairprobs")
+    return single, pair
+
+
+def computeposteriors(unpairedlogprobs, pairedlogprobs, maxspan=-1, ctx=None):
+    """inside -> outside -> computebasepairprobs on the device
+    (src/MESSI.jl:1101-1103).  Returns (Z, single, pair)."""
+    ctx = ctx or get_context()
+    u = _f64c(unpairedlogprobs)
+    L = len(u)
+    single = np.empty(L)
+    pair = np.empty((L, L), order="F")
+    Z = ctypes.c_double()
+    ctx.check(ctx.lib.messi_posteriors(ctx.handle, L, _p(u), _p(_f64f(pairedlogprobs)), int(maxspan),
+                                       ctypes.byref(Z), _p(single), _p(pair)), "messi_posteriors")
+    return Z.value, single, pair
+
+
+# ---------------------------------------------------------------------------
+# the likelihood evaluation of every NLopt / MCMC step
+# ---------------------------------------------------------------------------
+def computestructureintegratedlikelihood(dataset, params, maxbasepairdistance=1000000, samplebranchlengths=False,
+                                         fixLambdaGT=False, integratesiterates=True, usecuda=True, gapcutoff=1.0,
+                                         ctx=None, return_unpaired=False):
+    """src/FARCE.jl:2322-2345 (+ maskgapped!, src/MESSI.jl:310): logprior + Z,
+    with unpaired, pair and inside passes resident on the device."""
+    _need_cuda(usecuda and integratesiterates)
+    ctx = ctx or get_context()
+    saved = params.lambdaGT
+    if fixLambdaGT:
+        params.lambdaGT = 1.0
+    try:
+        h = ctx.dataset(dataset, maxbasepairdistance)
+        m = ModelArgs(params)
+        Z = ctypes.c_double()
+        gf = _f64c(dataset.gapfrequency)
+        u = np.empty(dataset.numcols) if return_unpaired else None
+        ctx.check(ctx.lib.messi_likelihood(ctx.handle, h.handle, ctypes.byref(m.struct), _p(gf), float(gapcutoff),
+                                           ctypes.byref(Z), _p(u)), "messi_likelihood")
+        params.logprior = computeprior(params, samplebranchlengths, fixLambdaGT)
+    finally:
+        params.lambdaGT = saved
+    total = params.logprior + Z.value
+    return (total, Z.value, u) if return_unpaired else total

@@ -1,0 +1,547 @@
+// api.cu -- C ABI entry points (include/messi_gb300.h): contexts, dataset
+// handles and the orchestration of each call on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "internal.h"
+
+namespace messi {
+
+int fail(messi_ctx* ctx, int code, const std::string& msg)
+{
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+int cuda_fail(messi_ctx* ctx, cudaError_t e, const char* what)
+{
+    return fail(ctx, (e == cudaErrorMemoryAllocation) ? MESSI_ENOMEM : MESSI_ECUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int ensure(messi_ctx* ctx, int slot, size_t bytes, void** p)
+{
+    DevBuf& b = ctx->scratch[slot];
+    if (bytes == 0) bytes = 16;
+    if (b.bytes < bytes) {
+        if (b.p) cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+        cudaError_t e = cudaMalloc(&b.p, bytes);
+        if (e != cudaSuccess) {
+            b.p = nullptr;
+            return cuda_fail(ctx, e, "scratch allocation");
+        }
+        b.bytes = bytes;
+    }
+    *p = b.p;
+    return MESSI_OK;
+}
+
+int ensure_pinned(messi_ctx* ctx, size_t bytes, void** p)
+{
+    if (ctx->pinned_bytes < bytes) {
+        if (ctx->pinned) cudaFreeHost(ctx->pinned);
+        ctx->pinned = nullptr;
+        ctx->pinned_bytes = 0;
+        cudaError_t e = cudaMallocHost(&ctx->pinned, bytes);
+        if (e != cudaSuccess) {
+            ctx->pinned = nullptr;
+            return cuda_fail(ctx, e, "pinned staging allocation");
+        }
+        ctx->pinned_bytes = bytes;
+    }
+    *p = ctx->pinned;
+    return MESSI_OK;
+}
+
+static cudaEvent_t prof_event(messi_ctx* ctx)
+{
+    if (!ctx->prof_pool.empty()) {
+        cudaEvent_t e = ctx->prof_pool.back();
+        ctx->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+int prof_begin(messi_ctx* ctx, int kernel, double units)
+{
+    if (!ctx->profiling) return -1;
+    ProfRec r{kernel, prof_event(ctx), prof_event(ctx), units};
+    cudaEventRecord(r.a, ctx->stream);
+    ctx->prof_pending.push_back(r);
+    return (int)ctx->prof_pending.size() - 1;
+}
+
+void prof_end(messi_ctx* ctx)
+{
+    if (!ctx->profiling || ctx->prof_pending.empty()) return;
+    cudaEventRecord(ctx->prof_pending.back().b, ctx->stream);
+}
+
+static void prof_collect(messi_ctx* ctx)
+{
+    for (ProfRec& r : ctx->prof_pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess && r.kernel >= 0 && r.kernel < kProfKernels) {
+            ctx->prof_ms[r.kernel] += ms;
+            ctx->prof_count[r.kernel] += 1;
+            ctx->prof_units[r.kernel] += r.units;
+        }
+        ctx->prof_pool.push_back(r.a);
+        ctx->prof_pool.push_back(r.b);
+    }
+    ctx->prof_pending.clear();
+}
+
+namespace {
+
+// Scratch slots (grow-only, per context).  0..14 belong to the band tables.
+enum Slot { kSlotStage = 15, kSlotP16 = 16, kSlotDense = 17, kSlotVec = 18, kSlotTable = 19, kSlotP4 = 21 };
+
+struct Staged {
+    size_t off = 0;
+    std::vector<char> host;
+    template <typename T>
+    size_t add(const T* src, size_t n)
+    {
+        off = (off + 15) & ~size_t(15);
+        size_t at = off;
+        host.resize(off + n * sizeof(T));
+        std::memcpy(host.data() + at, src, n * sizeof(T));
+        off += n * sizeof(T);
+        return at;
+    }
+};
+
+struct ModelDev {
+    Categories cat;
+    float* P16 = nullptr;
+    double* P4 = nullptr;
+    float* pi16 = nullptr;
+    double* logw = nullptr;
+    int* lam = nullptr;
+    double* pi4 = nullptr;
+    double* logw_site = nullptr;
+    uint8_t* gapmask = nullptr;
+};
+
+// Builds categories on the host, uploads them in one copy and assembles the
+// transition matrices on the device.
+int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool pairs, bool unpaired,
+                 const uint8_t* gapmask, ModelDev* md)
+{
+    std::string err;
+    int rc = build_categories(m, ds->numnodes, &md->cat, &err);
+    if (rc) return fail(ctx, rc, err);
+    Categories& c = md->cat;
+    Staged st;
+    size_t o_eig = st.add(c.eig.data(), c.eig.size());
+    size_t o_bl = st.add(m->branchlengths, (size_t)ds->numnodes);
+    size_t o_pi16 = st.add(c.pi16.data(), c.pi16.size());
+    size_t o_logw = st.add(c.logw.data(), c.logw.size());
+    size_t o_lam = st.add(c.lam.data(), c.lam.size());
+    size_t o_eig4 = st.add(c.eig4.data(), c.eig4.size());
+    size_t o_pi4 = st.add(c.pi4, 4);
+    size_t o_lws = st.add(c.logw_site.data(), c.logw_site.size());
+    size_t o_gap = gapmask ? st.add(gapmask, (size_t)ds->L) : 0;
+    void *pin, *dev;
+    if ((rc = ensure_pinned(ctx, st.host.size(), &pin))) return rc;
+    if ((rc = ensure(ctx, kSlotStage, st.host.size(), &dev))) return rc;
+    std::memcpy(pin, st.host.data(), st.host.size());
+    cudaError_t e = cudaMemcpyAsync(dev, pin, st.host.size(), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "model upload");
+    char* base = (char*)dev;
+    md->pi16 = (float*)(base + o_pi16);
+    md->logw = (double*)(base + o_logw);
+    md->lam = (int*)(base + o_lam);
+    md->pi4 = (double*)(base + o_pi4);
+    md->logw_site = (double*)(base + o_lws);
+    md->gapmask = gapmask ? (uint8_t*)(base + o_gap) : nullptr;
+    const double* d_bl = (const double*)(base + o_bl);
+    if (pairs) {
+        void* p;
+        if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * sizeof(float), &p))) return rc;
+        md->P16 = (float*)p;
+        if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, ds->numnodes, c.C, md->P16))) return rc;
+    }
+    if (unpaired) {
+        void* p;
+        if ((rc = ensure(ctx, kSlotP4, (size_t)c.nsite * ds->numnodes * 16 * sizeof(double), &p))) return rc;
+        md->P4 = (double*)p;
+        if ((rc = launch_build_P4(ctx, (const double*)(base + o_eig4), d_bl, ds->numnodes, c.nsite, md->P4)))
+            return rc;
+    }
+    return MESSI_OK;
+}
+
+int prepare_arena(messi_ctx* ctx, messi_dataset* ds, int C)
+{
+    std::string err;
+    if (ds->chunk == 0 || ds->arena_C != C) {
+        int rc = allocate_arena(ds, C, &err);
+        if (rc) return fail(ctx, rc, err);
+        ds->arena_C = C;
+    }
+    return MESSI_OK;
+}
+
+int finish(messi_ctx* ctx)
+{
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream synchronize");
+    if (!ctx->prof_pending.empty()) prof_collect(ctx);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel execution");
+    return MESSI_OK;
+}
+
+int begin(messi_ctx* ctx)
+{
+    if (!ctx) return MESSI_EINVAL;
+    ctx->launches = 0;
+    ctx->last_error.clear();
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+    return MESSI_OK;
+}
+
+int h2d(messi_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "host to device copy");
+}
+
+int d2h(messi_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "device to host copy");
+}
+
+// Upload a dense L x L pair matrix, pick the band width, prepare the band.
+int dense_pairs_to_band(messi_ctx* ctx, int L, const double* unpaired, const double* paired, int maxspan,
+                        double B, bool outside, Band* t)
+{
+    int rc;
+    void* p;
+    if ((rc = ensure(ctx, kSlotDense, (size_t)L * L * sizeof(double), &p))) return rc;
+    double* d_dense = (double*)p;
+    if ((rc = h2d(ctx, d_dense, paired, (size_t)L * L * sizeof(double)))) return rc;
+    int Wb = maxspan;
+    if (maxspan < 0) {
+        void* q;
+        if ((rc = ensure(ctx, kSlotVec, 64, &q))) return rc;
+        if ((rc = launch_maxspan(ctx, L, d_dense, (int*)q))) return rc;
+        int host = 0;
+        if ((rc = d2h(ctx, &host, q, sizeof(int)))) return rc;
+        if ((rc = finish(ctx))) return rc;
+        Wb = host;
+    }
+    Wb = std::max(0, std::min(Wb, L - 1));
+    if ((rc = band_alloc(ctx, L, Wb, outside, t))) return rc;
+    if ((rc = h2d(ctx, t->u, unpaired, (size_t)L * sizeof(double)))) return rc;
+    if ((rc = launch_baseline(ctx, *t, B))) return rc;
+    return launch_bandprep_from_dense(ctx, *t, d_dense, B);
+}
+
+}  // namespace
+}  // namespace messi
+
+using namespace messi;
+
+extern "C" {
+
+const char* messi_strerror(int status)
+{
+    switch (status) {
+        case MESSI_OK: return "ok";
+        case MESSI_EINVAL: return "invalid argument";
+        case MESSI_ENOMEM: return "out of memory";
+        case MESSI_ECUDA: return "CUDA error";
+        case MESSI_ETIMEOUT: return "bounded device wait timed out";
+        case MESSI_ESTATE: return "object used in the wrong state";
+        default: return "unknown status";
+    }
+}
+
+int messi_version(void) { return 100; }
+
+int messi_ctx_create(int device, messi_ctx** out)
+{
+    if (!out) return MESSI_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MESSI_ECUDA;
+    if (device < 0 || device >= n) return MESSI_EINVAL;
+    messi_ctx* ctx = new (std::nothrow) messi_ctx();
+    if (!ctx) return MESSI_ENOMEM;
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) !=
+                                                    cudaSuccess) {
+        delete ctx;
+        return MESSI_ECUDA;
+    }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    *out = ctx;
+    return MESSI_OK;
+}
+
+int messi_ctx_profile(messi_ctx* ctx, int enable)
+{
+    if (!ctx) return MESSI_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    prof_collect(ctx);
+    ctx->profiling = enable != 0;
+    for (int k = 0; k < kProfKernels; k++) {
+        ctx->prof_ms[k] = 0.0;
+        ctx->prof_count[k] = 0;
+        ctx->prof_units[k] = 0.0;
+    }
+    return MESSI_OK;
+}
+
+int messi_ctx_profile_read(messi_ctx* ctx, int kernel, double* total_ms, int64_t* launches, double* units)
+{
+    if (!ctx || kernel < 0 || kernel >= kProfKernels) return MESSI_EINVAL;
+    if (total_ms) *total_ms = ctx->prof_ms[kernel];
+    if (launches) *launches = ctx->prof_count[kernel];
+    if (units) *units = ctx->prof_units[kernel];
+    return MESSI_OK;
+}
+
+int messi_ctx_destroy(messi_ctx* ctx)
+{
+    if (!ctx) return MESSI_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    prof_collect(ctx);
+    for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
+    for (auto& b : ctx->scratch)
+        if (b.p) cudaFree(b.p);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MESSI_OK;
+}
+
+int messi_ctx_stream(messi_ctx* ctx, void** stream)
+{
+    if (!ctx || !stream) return MESSI_EINVAL;
+    *stream = (void*)ctx->stream;
+    return MESSI_OK;
+}
+
+int messi_ctx_last_launches(messi_ctx* ctx, int64_t* launches)
+{
+    if (!ctx || !launches) return MESSI_EINVAL;
+    *launches = ctx->launches;
+    return MESSI_OK;
+}
+
+const char* messi_ctx_last_error(messi_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+int messi_dataset_create(messi_ctx* ctx, const messi_alignment* aln, int32_t maxbasepairdistance,
+                         const uint8_t* pairmask, messi_dataset** out)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!aln || !out) return fail(ctx, MESSI_EINVAL, "dataset: null argument");
+    *out = nullptr;
+    messi_dataset* ds = new (std::nothrow) messi_dataset();
+    if (!ds) return fail(ctx, MESSI_ENOMEM, "dataset: host allocation");
+    ds->ctx = ctx;
+    std::string err;
+    rc = build_plan(ds, aln, maxbasepairdistance, pairmask, &err);
+    if (rc) {
+        messi_dataset_destroy(ds);
+        return fail(ctx, rc, err);
+    }
+    *out = ds;
+    return MESSI_OK;
+}
+
+int messi_dataset_destroy(messi_dataset* ds)
+{
+    if (!ds) return MESSI_EINVAL;
+    if (ds->ctx) {
+        cudaSetDevice(ds->ctx->device);
+        cudaStreamSynchronize(ds->ctx->stream);
+    }
+    void* bufs[] = {ds->d_bandidx, ds->d_lr, ds->d_leaf, ds->d_nodes, ds->d_tiles, ds->d_masks, ds->d_tree,
+                    ds->d_post, ds->d_arena_f, ds->d_arena_e, ds->d_mix, ds->d_mixlam};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    delete ds;
+    return MESSI_OK;
+}
+
+int messi_dataset_stats(messi_dataset* ds, int64_t* out, int32_t n)
+{
+    if (!ds || !out || n < 0) return MESSI_EINVAL;
+    const int64_t v[7] = {ds->band_pairs, ds->nroot, ds->executed, ds->naive, ds->H, ds->arena_rows, ds->chunk};
+    for (int k = 0; k < n && k < 7; k++) out[k] = v[k];
+    return MESSI_OK;
+}
+
+int messi_felsenstein_pairs(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, double* pairedlogprobs,
+                            double* museconditionals)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ds || !model || !pairedlogprobs) return fail(ctx, MESSI_EINVAL, "felsenstein_pairs: null argument");
+    ModelDev md;
+    if ((rc = upload_model(ctx, ds, model, true, false, nullptr, &md))) return rc;
+    if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
+    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, museconditionals != nullptr)))
+        return rc;
+    void* p;
+    const size_t LL = (size_t)ds->L * ds->L;
+    if ((rc = ensure(ctx, kSlotDense, LL * sizeof(double), &p))) return rc;
+    double* d_dense = (double*)p;
+    if ((rc = launch_scatter_dense(ctx, ds, ds->d_mix, d_dense))) return rc;
+    if ((rc = d2h(ctx, pairedlogprobs, d_dense, LL * sizeof(double)))) return rc;
+    if (museconditionals) {
+        // one L x L matrix per lambda category; the copy of the previous one
+        // must finish before the buffer is reused (same stream: ordered)
+        for (int l = 0; l < md.cat.nlam; l++) {
+            if ((rc = launch_scatter_dense(ctx, ds, ds->d_mixlam + (size_t)l * ds->nroot, d_dense))) return rc;
+            if ((rc = d2h(ctx, museconditionals + (size_t)l * LL, d_dense, LL * sizeof(double)))) return rc;
+        }
+    }
+    return finish(ctx);
+}
+
+int messi_unpaired(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, double* unpairedlogprobs)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ds || !model || !unpairedlogprobs) return fail(ctx, MESSI_EINVAL, "unpaired: null argument");
+    ModelDev md;
+    if ((rc = upload_model(ctx, ds, model, false, true, nullptr, &md))) return rc;
+    void* p;
+    if ((rc = ensure(ctx, kSlotVec, (size_t)ds->L * sizeof(double), &p))) return rc;
+    if ((rc = launch_unpaired(ctx, ds, md.P4, md.pi4, md.logw_site, md.cat.nsite, (double*)p))) return rc;
+    if ((rc = d2h(ctx, unpairedlogprobs, p, (size_t)ds->L * sizeof(double)))) return rc;
+    return finish(ctx);
+}
+
+int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const double* gapfrequency,
+                     double gapcutoff, double* Z, double* unpaired)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ds || !model || !Z) return fail(ctx, MESSI_EINVAL, "likelihood: null argument");
+    std::vector<uint8_t> gm;
+    if (gapfrequency) {
+        gm.resize(ds->L);
+        for (int i = 0; i < ds->L; i++) gm[i] = (gapfrequency[i] >= gapcutoff) ? 1 : 0;
+    }
+    ModelDev md;
+    if ((rc = upload_model(ctx, ds, model, true, true, gapfrequency ? gm.data() : nullptr, &md))) return rc;
+    if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
+    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
+    Band t;
+    const int Wb = std::max(0, std::min(ds->W, ds->L - 1));
+    if ((rc = band_alloc(ctx, ds->L, Wb, false, &t))) return rc;
+    if ((rc = launch_unpaired(ctx, ds, md.P4, md.pi4, md.logw_site, md.cat.nsite, t.u))) return rc;
+    if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
+    if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0))) return rc;
+    if ((rc = run_inside(ctx, t, 1.0))) return rc;
+    if ((rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;
+    if (unpaired && (rc = d2h(ctx, unpaired, t.u, (size_t)ds->L * sizeof(double)))) return rc;
+    return finish(ctx);
+}
+
+int messi_inside(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan, double B,
+                 double* Z, double* inside)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !unpaired || !paired || !Z) return fail(ctx, MESSI_EINVAL, "inside: bad arguments");
+    Band t;
+    if ((rc = dense_pairs_to_band(ctx, L, unpaired, paired, maxspan, B, false, &t))) return rc;
+    if ((rc = run_inside(ctx, t, B))) return rc;
+    if ((rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;
+    if (inside) {
+        void* p;
+        const size_t bytes = (size_t)3 * L * L * sizeof(double);
+        if ((rc = ensure(ctx, kSlotTable, bytes, &p))) return rc;
+        if ((rc = launch_dense_inside(ctx, t, (double*)p))) return rc;
+        if ((rc = d2h(ctx, inside, p, bytes))) return rc;
+    }
+    return finish(ctx);
+}
+
+int messi_outside(messi_ctx* ctx, int32_t L, const double* inside, const double* unpaired, const double* paired,
+                  int32_t maxspan, double* outside)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !inside || !unpaired || !paired || !outside) return fail(ctx, MESSI_EINVAL, "outside: bad arguments");
+    Band t;
+    if ((rc = dense_pairs_to_band(ctx, L, unpaired, paired, maxspan, 1.0, true, &t))) return rc;
+    void* p;
+    const size_t bytes = (size_t)3 * L * L * sizeof(double);
+    if ((rc = ensure(ctx, kSlotTable, bytes, &p))) return rc;
+    if ((rc = h2d(ctx, p, inside, bytes))) return rc;
+    if ((rc = launch_band_from_dense_inside(ctx, t, (const double*)p))) return rc;
+    if ((rc = run_outside(ctx, t, 1.0))) return rc;
+    if ((rc = launch_dense_outside(ctx, t, (double*)p))) return rc;
+    if ((rc = d2h(ctx, outside, p, bytes))) return rc;
+    return finish(ctx);
+}
+
+int messi_basepairprobs(messi_ctx* ctx, int32_t L, const double* inside, const double* outside,
+                        const double* unpaired, const double* paired, int32_t maxspan, double* single,
+                        double* pairprobs)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !inside || !outside || !unpaired || !paired || !single || !pairprobs)
+        return fail(ctx, MESSI_EINVAL, "basepairprobs: bad arguments");
+    Band t;
+    if ((rc = dense_pairs_to_band(ctx, L, unpaired, paired, maxspan, 1.0, true, &t))) return rc;
+    void* p;
+    const size_t bytes = (size_t)3 * L * L * sizeof(double);
+    if ((rc = ensure(ctx, kSlotTable, bytes, &p))) return rc;
+    if ((rc = h2d(ctx, p, inside, bytes))) return rc;
+    if ((rc = launch_band_from_dense_inside(ctx, t, (const double*)p))) return rc;
+    if ((rc = h2d(ctx, p, outside, bytes))) return rc;
+    if ((rc = launch_band_from_dense_outside(ctx, t, (const double*)p))) return rc;
+    void *ds_single, *ds_pair;
+    if ((rc = ensure(ctx, kSlotVec, (size_t)L * sizeof(double), &ds_single))) return rc;
+    if ((rc = ensure(ctx, kSlotDense, (size_t)L * L * sizeof(double), &ds_pair))) return rc;
+    if ((rc = run_posteriors(ctx, t, 1.0, (double*)ds_single, (double*)ds_pair))) return rc;
+    if ((rc = d2h(ctx, single, ds_single, (size_t)L * sizeof(double)))) return rc;
+    if ((rc = d2h(ctx, pairprobs, ds_pair, (size_t)L * L * sizeof(double)))) return rc;
+    return finish(ctx);
+}
+
+int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,
+                     double* Z, double* single, double* pairprobs)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !unpaired || !paired || !single || !pairprobs)
+        return fail(ctx, MESSI_EINVAL, "posteriors: bad arguments");
+    Band t;
+    if ((rc = dense_pairs_to_band(ctx, L, unpaired, paired, maxspan, 1.0, true, &t))) return rc;
+    if ((rc = run_inside(ctx, t, 1.0))) return rc;
+    if ((rc = run_outside(ctx, t, 1.0))) return rc;
+    void *ds_single, *ds_pair;
+    if ((rc = ensure(ctx, kSlotVec, (size_t)L * sizeof(double), &ds_single))) return rc;
+    if ((rc = ensure(ctx, kSlotDense, (size_t)L * L * sizeof(double), &ds_pair))) return rc;
+    if ((rc = run_posteriors(ctx, t, 1.0, (double*)ds_single, (double*)ds_pair))) return rc;
+    if (Z && (rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;
+    if ((rc = d2h(ctx, single, ds_single, (size_t)L * sizeof(double)))) return rc;
+    if ((rc = d2h(ctx, pairprobs, ds_pair, (size_t)L * L * sizeof(double)))) return rc;
+    return finish(ctx);
+}
+
+}  // extern "C"

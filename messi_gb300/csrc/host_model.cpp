@@ -1,0 +1,214 @@
+// host_model.cpp -- FP64 substitution models and their eigensystems (host side).
+//
+// Rate matrices restate src/RateMatrices.jl (gtr :2-37, calculatemusefreqs
+// :40-67, muse :69-148).  exp(Qt) in the reference comes from a general
+// eigendecomposition (src/FARCE.jl:410-433); every Q here is reversible with
+// respect to its stationary frequencies, so the library diagonalises the
+// symmetric matrix D^1/2 Q D^-1/2 (D = diag(pi)) by cyclic Jacobi and the
+// device assembles P = D^-1/2 U exp(W t) U^T D^1/2 per branch in FP64.
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace messi {
+
+static const int kPairClass[16] = {0, 0, 0, 2, 0, 0, 1, 0, 0, 1, 0, 3, 2, 0, 3, 0};
+
+void host_gtr(const double* q, const double* piv, double* Q)
+{
+    static const int ij[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    double S[16] = {0};
+    for (int k = 0; k < 6; k++) {
+        S[ij[k][0] * 4 + ij[k][1]] = q[k];
+        S[ij[k][1] * 4 + ij[k][0]] = q[k];
+    }
+    for (int i = 0; i < 4; i++) {
+        double d = 0.0;
+        for (int j = 0; j < 4; j++) {
+            Q[i * 4 + j] = S[i * 4 + j] * piv[j];
+            if (i != j) d -= Q[i * 4 + j];
+        }
+        Q[i * 4 + i] = d;
+    }
+}
+
+void host_musefreqs(const double* pi4, double lGC, double lAT, double lGT, double* out16)
+{
+    const double lam[4] = {1.0, lGC, lAT, lGT};
+    const double piGC = pi4[1] * pi4[2], piAT = pi4[0] * pi4[3], piGT = pi4[2] * pi4[3];
+    const double kappa = 1.0 / (1.0 + 2.0 * (piAT * (lAT * lAT - 1.0)) + 2.0 * (piGC * (lGC * lGC - 1.0)) +
+                                2.0 * (piGT * (lGT * lGT - 1.0)));
+    for (int a = 0; a < 16; a++) {
+        double l = lam[kPairClass[a]];
+        out16[a] = kappa * l * l * pi4[a / 4] * pi4[a % 4];
+    }
+}
+
+void host_muse(double lGC, double lAT, double lGT, const double* q, const double* pi4, double sr1, double sr2,
+               double* Q)
+{
+    const double ones[4] = {1.0, 1.0, 1.0, 1.0};
+    const double lam[4] = {1.0, lGC, lAT, lGT};
+    double g[16];
+    host_gtr(q, ones, g);
+    for (int h = 0; h < 16; h++) {
+        double d = 0.0;
+        for (int v = 0; v < 16; v++) {
+            double rate = 0.0;
+            if (v != h) {
+                int from = -1, to = -1;
+                double sr = 1.0;
+                if (h / 4 == v / 4) { from = h % 4; to = v % 4; sr = sr2; }
+                else if (h % 4 == v % 4) { from = h / 4; to = v / 4; sr = sr1; }
+                if (from >= 0) rate = g[from * 4 + to] * sr * pi4[to] * lam[kPairClass[v]] / lam[kPairClass[h]];
+            }
+            Q[h * 16 + v] = rate;
+            d -= rate;
+        }
+        Q[h * 16 + h] = d;
+    }
+}
+
+static void jacobi(int n, double* A, double* w, double* V)
+{
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) V[i * n + j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 64; sweep++) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n * n; i++) tot += A[i] * A[i];
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++)
+                if (i != j) off += A[i * n + j] * A[i * n + j];
+        if (off <= 1e-30 * tot) break;
+        for (int p = 0; p < n; p++)
+            for (int r = p + 1; r < n; r++) {
+                double apr = A[p * n + r];
+                if (std::fabs(apr) < 1e-300) continue;
+                double theta = (A[r * n + r] - A[p * n + p]) / (2.0 * apr);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; k++) {
+                    double akp = A[k * n + p], akr = A[k * n + r];
+                    A[k * n + p] = c * akp - s * akr;
+                    A[k * n + r] = s * akp + c * akr;
+                }
+                for (int k = 0; k < n; k++) {
+                    double apk = A[p * n + k], ark = A[r * n + k];
+                    A[p * n + k] = c * apk - s * ark;
+                    A[r * n + k] = s * apk + c * ark;
+                }
+                for (int k = 0; k < n; k++) {
+                    double vkp = V[k * n + p], vkr = V[k * n + r];
+                    V[k * n + p] = c * vkp - s * vkr;
+                    V[k * n + r] = s * vkp + c * vkr;
+                }
+            }
+    }
+    for (int i = 0; i < n; i++) w[i] = A[i * n + i];
+}
+
+int host_reversible_eig(int n, const double* Q, const double* pi, double* w, double* U)
+{
+    double A[256];
+    if (n > 16) return MESSI_EINVAL;
+    for (int i = 0; i < n; i++)
+        if (!(pi[i] > 0.0) || !std::isfinite(pi[i])) return MESSI_EINVAL;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) A[i * n + j] = std::sqrt(pi[i]) * Q[i * n + j] / std::sqrt(pi[j]);
+    for (int i = 0; i < n; i++)
+        for (int j = i + 1; j < n; j++) {
+            double s = 0.5 * (A[i * n + j] + A[j * n + i]);
+            A[i * n + j] = A[j * n + i] = s;
+        }
+    for (int i = 0; i < n * n; i++)
+        if (!std::isfinite(A[i])) return MESSI_EINVAL;
+    jacobi(n, A, w, U);
+    return MESSI_OK;
+}
+
+static double safe_log(double x) { return x > 0.0 ? std::log(x) : -INFINITY; }
+
+// Categories in the reference order: siteCat1 outer, siteCat2, lambda inner
+// (src/FelsensteinCUDA.jl:277-279), weight log(w1) + log(w2) + log(w_lambda)
+// (src/FelsensteinCUDA.jl:403-418).
+int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err)
+{
+    if (!m || m->nsite < 1 || m->nlambda < 1 || !m->siteRates || !m->siteWeights || !m->lambdaGC ||
+        !m->lambdaAT || !m->lambdaGT || !m->lambdaWeights || !m->branchlengths) {
+        *err = "model: missing arrays or empty category sets";
+        return MESSI_EINVAL;
+    }
+    if (m->nlambda > kMaxLambda) {
+        *err = "model: at most 8 lambda categories are supported";
+        return MESSI_EINVAL;
+    }
+    for (int a = 0; a < 4; a++)
+        if (!(m->freqs[a] > 0.0)) { *err = "model: nucleotide frequencies must be positive"; return MESSI_EINVAL; }
+    for (int k = 0; k < 6; k++)
+        if (!(m->q[k] >= 0.0) || !std::isfinite(m->q[k])) { *err = "model: invalid exchangeability"; return MESSI_EINVAL; }
+    for (int s = 0; s < m->nsite; s++)
+        if (!(m->siteRates[s] >= 0.0) || !std::isfinite(m->siteRates[s]) || !(m->siteWeights[s] >= 0.0)) {
+            *err = "model: invalid site rate or weight";
+            return MESSI_EINVAL;
+        }
+    for (int l = 0; l < m->nlambda; l++)
+        if (!(m->lambdaGC[l] > 0.0) || !(m->lambdaAT[l] > 0.0) || !(m->lambdaGT[l] > 0.0) ||
+            !std::isfinite(m->lambdaGC[l] + m->lambdaAT[l] + m->lambdaGT[l]) || !(m->lambdaWeights[l] >= 0.0)) {
+            *err = "model: invalid lambda category";
+            return MESSI_EINVAL;
+        }
+    for (int v = 0; v < numnodes; v++)
+        if (!(m->branchlengths[v] >= 0.0) || !std::isfinite(m->branchlengths[v])) {
+            *err = "model: branch lengths must be finite and non-negative";
+            return MESSI_EINVAL;
+        }
+    Categories& c = *out;
+    c.nsite = m->nsite;
+    c.nlam = m->nlambda;
+    c.C = m->nsite * m->nsite * m->nlambda;
+    c.eig.assign((size_t)c.C * kEigStride, 0.0);
+    c.pi16.assign((size_t)c.C * 16, 0.f);
+    c.logw.assign(c.C, 0.0);
+    c.lam.assign(c.C, 0);
+    int k = 0;
+    for (int s1 = 0; s1 < m->nsite; s1++)
+        for (int s2 = 0; s2 < m->nsite; s2++)
+            for (int l = 0; l < m->nlambda; l++, k++) {
+                double Q[256], pi16[16];
+                host_muse(m->lambdaGC[l], m->lambdaAT[l], m->lambdaGT[l], m->q, m->freqs, m->siteRates[s1],
+                          m->siteRates[s2], Q);
+                host_musefreqs(m->freqs, m->lambdaGC[l], m->lambdaAT[l], m->lambdaGT[l], pi16);
+                double* e = &c.eig[(size_t)k * kEigStride];
+                if (host_reversible_eig(16, Q, pi16, e, e + 16)) {
+                    *err = "model: rate matrix is not diagonalisable";
+                    return MESSI_EINVAL;
+                }
+                for (int a = 0; a < 16; a++) {
+                    e[16 + 256 + a] = std::sqrt(pi16[a]);
+                    c.pi16[(size_t)k * 16 + a] = (float)pi16[a];
+                }
+                c.logw[k] = safe_log(m->siteWeights[s1]) + safe_log(m->siteWeights[s2]) + safe_log(m->lambdaWeights[l]);
+                c.lam[k] = l;
+            }
+    // unpaired 4-state model per site rate: gtr(q, freqs) * rate (src/FARCE.jl:742-750)
+    c.eig4.assign((size_t)m->nsite * kEig4Stride, 0.0);
+    c.logw_site.assign(m->nsite, 0.0);
+    double Q4[16];
+    host_gtr(m->q, m->freqs, Q4);
+    for (int s = 0; s < m->nsite; s++) {
+        double Qr[16];
+        for (int i = 0; i < 16; i++) Qr[i] = Q4[i] * m->siteRates[s];
+        double* e = &c.eig4[(size_t)s * kEig4Stride];
+        if (host_reversible_eig(4, Qr, m->freqs, e, e + 4)) {
+            *err = "model: GTR matrix is not diagonalisable";
+            return MESSI_EINVAL;
+        }
+        for (int a = 0; a < 4; a++) e[4 + 16 + a] = std::sqrt(m->freqs[a]);
+        c.logw_site[s] = safe_log(m->siteWeights[s]);
+    }
+    for (int a = 0; a < 4; a++) c.pi4[a] = m->freqs[a];
+    return MESSI_OK;
+}
+
+}  // namespace messi

@@ -1,0 +1,401 @@
+// prune.cu -- site-pair pruning (HP1) and unpaired column likelihoods on the GPU.
+//
+// Replaces the kernels of src/cuda/felsenstein.cu used by
+// src/FelsensteinCUDA.jl:214-516 (felsensteinleaves16 :117-133,
+// felsensteinhelper16 :153-200, sumfinal :428-442, storearr/logsumexparr
+// :135-151) with:
+//   * build_P16_kernel: P = exp(Qt) per (category, branch) in FP64 from the
+//     host eigensystem, stored as FP32 rows (row = parent state);
+//   * prune_level_kernel: one launch per tree level and category pass; a CTA
+//     owns a tile of unique pairs of one node, stages that node's 2 x C
+//     transition matrices in shared memory, gathers the child rows with
+//     16-byte loads and writes the rescaled node rows.  Rows are rescaled by
+//     an exact power of two (exponent kept as an int), which computes the
+//     same likelihood as the reference's divide-by-max (felsenstein.cu:193-198);
+//   * the root variant folds sumfinal and the category log-sum-exp into the
+//     same pass (FP64 log-likelihood reduction).
+// unpaired_kernel restates computeunpairedlikelihoodscat (src/FARCE.jl:742-773)
+// in FP64 with the CPU rescaling rule.
+#include <algorithm>
+#include <cmath>
+
+#include "internal.h"
+
+namespace messi {
+
+__global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl, int numnodes,
+                                 float* __restrict__ P)
+{
+    const int v = blockIdx.x, c = blockIdx.y, t = threadIdx.x;
+    const double* e = eig + (size_t)c * kEigStride;
+    __shared__ double ex[16], U[256], sp[16];
+    const double tl = bl[v];
+    U[t] = e[16 + t];
+    if (t < 16) {
+        ex[t] = exp(e[t] * tl);
+        sp[t] = e[16 + 256 + t];
+    }
+    __syncthreads();
+    const int a = t >> 4, d = t & 15;
+    float out;
+    if (v == 0) {
+        out = 0.f;  // the root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
+    } else if (tl == 0.0) {
+        out = (a == d) ? 1.f : 0.f;
+    } else {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 16; k++) s += U[a * 16 + k] * ex[k] * U[d * 16 + k];
+        s *= sp[d] / sp[a];
+        out = (s <= 0.0) ? 0.f : (float)s;  // absmat clamp (1e-50 rounds to 0 in FP32)
+    }
+    P[((size_t)c * numnodes + v) * 256 + t] = out;
+}
+
+__global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl, int numnodes,
+                                double* __restrict__ P4)
+{
+    const int v = blockIdx.x, s = blockIdx.y, t = threadIdx.x;  // 16 threads
+    const double* e = eig4 + (size_t)s * kEig4Stride;
+    const double tl = bl[v];
+    const int a = t >> 2, d = t & 3;
+    double out;
+    if (v == 0) {
+        out = 0.0;
+    } else if (tl == 0.0) {
+        out = (a == d) ? 1.0 : 0.0;
+    } else {
+        double acc = 0.0;
+        for (int k = 0; k < 4; k++) acc += e[4 + a * 4 + k] * exp(e[k] * tl) * e[4 + d * 4 + k];
+        acc *= e[20 + d] / e[20 + a];
+        out = (acc <= 0.0) ? 1e-50 : acc;
+    }
+    P4[((size_t)s * numnodes + v) * 16 + t] = out;
+}
+
+int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, int numnodes, int C, float* d_P)
+{
+    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, numnodes, d_P);
+    LAUNCH_CHECK(ctx, "build_P16_kernel");
+    return MESSI_OK;
+}
+
+int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, int numnodes, int nsite, double* d_P4)
+{
+    build_P4_kernel<<<dim3(numnodes, nsite), 16, 0, ctx->stream>>>(d_eig4, d_bl, numnodes, d_P4);
+    LAUNCH_CHECK(ctx, "build_P4_kernel");
+    return MESSI_OK;
+}
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+__device__ __forceinline__ double lse_d(double a, double b)
+{
+    if (b == -INFINITY) return a;
+    if (a == -INFINITY) return b;
+    return (a < b) ? b + log1p(exp(a - b)) : a + log1p(exp(b - a));
+}
+
+// One tree level, one pass over categories [c0, c0 + nc).
+template <bool ROOT>
+__global__ void __launch_bounds__(kTile) prune_level_kernel(
+    const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ P, int numnodes,
+    int c0, int nc, const float* __restrict__ pi16, const double* __restrict__ logw, const int* __restrict__ lam,
+    double* __restrict__ mix, double* __restrict__ mixlam, int nroot, int per_lambda)
+{
+    extern __shared__ float4 smem4[];
+    const float* sP = reinterpret_cast<const float*>(smem4);  // [nc][2][256]
+    const int2 tile = tiles[blockIdx.x];
+    const NodeDev& nd = nodes[tile.x];
+    const int left = nd.left, right = nd.right, n = nd.n;
+    for (int idx = threadIdx.x; idx < nc * 128; idx += blockDim.x) {
+        const int cc = idx >> 7, r = idx & 127;
+        const int node = (r >> 6) ? right : left;
+        smem4[idx] = __ldg(reinterpret_cast<const float4*>(P + ((size_t)(c0 + cc) * numnodes + node) * 256) + (r & 63));
+    }
+    float* sPi = reinterpret_cast<float*>(smem4 + nc * 128);  // [nc][16] (root only)
+    if (ROOT)
+        for (int idx = threadIdx.x; idx < nc * 16; idx += blockDim.x) sPi[idx] = pi16[(size_t)c0 * 16 + idx];
+    __syncthreads();
+    const int u = tile.y + threadIdx.x;
+    if (u >= n) return;
+    const int l = __ldg(nd.li + u), r = __ldg(nd.ri + u);
+    const float* lf = nd.lf;
+    const float* rf = nd.rf;
+    const int* le = nd.le;
+    const int* re = nd.re;
+    const long long lcs = nd.lcs, rcs = nd.rcs;
+
+    double mm = -INFINITY;  // root: running max of logw + loglik (FP64)
+    float ss = 0.f;         // root: running sum of exp(term - max)
+    double lm[kMaxLambda];
+    float ls[kMaxLambda];
+    if (ROOT) {
+#pragma unroll
+        for (int k = 0; k < kMaxLambda; k++) { lm[k] = -INFINITY; ls[k] = 0.f; }
+    }
+    for (int cc = 0; cc < nc; cc++) {
+        const float* lrow = lf + ((size_t)cc * lcs + l) * 16;
+        const float* rrow = rf + ((size_t)cc * rcs + r) * 16;
+        float4 Lv[4], Rv[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            Lv[q] = ldg4(lrow + 4 * q);
+            Rv[q] = ldg4(rrow + 4 * q);
+        }
+        int e = (le ? __ldg(le + (size_t)cc * lcs + l) : 0) + (re ? __ldg(re + (size_t)cc * rcs + r) : 0);
+        const float4* pl = reinterpret_cast<const float4*>(sP + cc * 512);
+        const float4* pr = pl + 64;
+        float v[16];
+#pragma unroll
+        for (int a = 0; a < 16; a++) {
+            float sl = 0.f, sr = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float4 x = pl[a * 4 + q];
+                const float4 y = pr[a * 4 + q];
+                sl = fmaf(x.x, Lv[q].x, sl);
+                sl = fmaf(x.y, Lv[q].y, sl);
+                sl = fmaf(x.z, Lv[q].z, sl);
+                sl = fmaf(x.w, Lv[q].w, sl);
+                sr = fmaf(y.x, Rv[q].x, sr);
+                sr = fmaf(y.y, Rv[q].y, sr);
+                sr = fmaf(y.z, Rv[q].z, sr);
+                sr = fmaf(y.w, Rv[q].w, sr);
+            }
+            v[a] = sl * sr;
+        }
+        if (ROOT) {
+            float dot = 0.f;
+#pragma unroll
+            for (int a = 0; a < 16; a++) dot = fmaf(sPi[cc * 16 + a], v[a], dot);
+            const double ll = (dot > 0.f) ? (double)logf(dot) + (double)e * 0.69314718055994530942 : -INFINITY;
+            const double t = __ldg(logw + c0 + cc) + ll;
+            if (t > mm) {
+                ss = ss * __expf((float)(mm - t)) + 1.f;
+                mm = t;
+            } else if (t != -INFINITY) {
+                ss += __expf((float)(t - mm));
+            }
+            if (per_lambda) {
+                const int k = __ldg(lam + c0 + cc);
+#pragma unroll
+                for (int q = 0; q < kMaxLambda; q++)
+                    if (q == k) {
+                        if (t > lm[q]) {
+                            ls[q] = ls[q] * __expf((float)(lm[q] - t)) + 1.f;
+                            lm[q] = t;
+                        } else if (t != -INFINITY) {
+                            ls[q] += __expf((float)(t - lm[q]));
+                        }
+                    }
+            }
+        } else {
+            float m = 0.f;
+#pragma unroll
+            for (int a = 0; a < 16; a++) m = fmaxf(m, v[a]);
+            int ex = 0;
+            if (m > 0.f) frexpf(m, &ex);
+            const float sc = ldexpf(1.f, -ex);
+            float4* o = reinterpret_cast<float4*>(nd.of + ((size_t)cc * nd.ocs + u) * 16);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                o[q] = make_float4(v[4 * q] * sc, v[4 * q + 1] * sc, v[4 * q + 2] * sc, v[4 * q + 3] * sc);
+            nd.oe[(size_t)cc * nd.ocs + u] = e + ex;
+        }
+    }
+    if (ROOT) {
+        const double res = (mm == -INFINITY) ? -INFINITY : mm + log((double)ss);
+        mix[u] = (c0 == 0) ? res : lse_d(mix[u], res);
+        if (per_lambda) {
+#pragma unroll
+            for (int q = 0; q < kMaxLambda; q++) {
+                const double rq = (lm[q] == -INFINITY) ? -INFINITY : lm[q] + log((double)ls[q]);
+                double* dst = mixlam + (size_t)q * nroot + u;
+                *dst = (c0 == 0) ? rq : lse_d(*dst, rq);
+            }
+        }
+    }
+}
+
+int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
+              const int* d_lam, int C, int nlam, bool per_lambda)
+{
+    (void)nlam;
+    const int chunk = ds->chunk;
+    const size_t smem_max = (size_t)chunk * (128 * sizeof(float4) + 16 * sizeof(float));
+    if (smem_max > 227 * 1024) return fail(ctx, MESSI_EINVAL, "category pass does not fit in shared memory");
+    if (smem_max > 48 * 1024) {
+        cudaFuncSetAttribute(prune_level_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        cudaFuncSetAttribute(prune_level_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    }
+    for (int c0 = 0; c0 < C; c0 += chunk) {
+        const int nc = std::min(chunk, C - c0);
+        for (int lv = 1; lv <= ds->H; lv++) {
+            const int nt = ds->tile_cnt[lv];
+            if (nt == 0) continue;
+            const int2* tiles = ds->d_tiles + ds->tile_off[lv];
+            if (ctx->profiling) {
+                double units = 0.0;
+                for (int v : ds->level_nodes[lv]) units += (double)ds->nunique[v] * nc;
+                prof_begin(ctx, 0, units);
+            }
+            if (lv < ds->H) {
+                const size_t smem = (size_t)nc * 128 * sizeof(float4);
+                prune_level_kernel<false><<<nt, kTile, smem, ctx->stream>>>(
+                    ds->d_nodes, tiles, d_P, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix, ds->d_mixlam,
+                    (int)ds->nroot, per_lambda ? 1 : 0);
+                LAUNCH_CHECK(ctx, "prune_level_kernel");
+            } else {
+                const size_t smem = (size_t)nc * (128 * sizeof(float4) + 16 * sizeof(float));
+                prune_level_kernel<true><<<nt, kTile, smem, ctx->stream>>>(
+                    ds->d_nodes, tiles, d_P, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix, ds->d_mixlam,
+                    (int)ds->nroot, per_lambda ? 1 : 0);
+                LAUNCH_CHECK(ctx, "prune_level_kernel<root>");
+            }
+            prof_end(ctx);
+        }
+    }
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Unpaired columns: one thread per column, nodes in post-order, partials of
+// every node kept in a [numnodes][L][4] scratch table (FP64).
+// ---------------------------------------------------------------------------
+__global__ void unpaired_kernel(const uint8_t* __restrict__ masks, const int* __restrict__ tree,
+                                const int* __restrict__ post, int nn, int L, const double* __restrict__ P4,
+                                const double* __restrict__ pi4, const double* __restrict__ logw_site, int nsite,
+                                double* __restrict__ part, double* __restrict__ lmv, double* __restrict__ u)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= L) return;
+    double acc = -INFINITY;
+    for (int s = 0; s < nsite; s++) {
+        const double* Ps = P4 + (size_t)s * nn * 16;
+        for (int t = 0; t < nn; t++) {
+            const int v = post[t];
+            const int c0 = tree[4 * v], c1 = tree[4 * v + 1];
+            double* pv = part + ((size_t)v * L + x) * 4;
+            if (c0 < 0) {
+                const int m = masks[(size_t)tree[4 * v + 2] * L + x];
+#pragma unroll
+                for (int a = 0; a < 4; a++) pv[a] = (double)((m >> a) & 1);
+                lmv[(size_t)v * L + x] = 0.0;
+                continue;
+            }
+            const double* p0 = part + ((size_t)c0 * L + x) * 4;
+            const double* p1 = part + ((size_t)c1 * L + x) * 4;
+            const double* P0 = Ps + (size_t)c0 * 16;
+            const double* P1 = Ps + (size_t)c1 * 16;
+            double l[4], r[4], o[4], m = -INFINITY;
+#pragma unroll
+            for (int a = 0; a < 4; a++) { l[a] = p0[a]; r[a] = p1[a]; }
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                double sl = 0.0, sr = 0.0;
+#pragma unroll
+                for (int d = 0; d < 4; d++) {
+                    sl += P0[a * 4 + d] * l[d];
+                    sr += P1[a * 4 + d] * r[d];
+                }
+                o[a] = sl * sr;
+                m = fmax(m, o[a]);
+            }
+            double lm = lmv[(size_t)c0 * L + x] + lmv[(size_t)c1 * L + x];
+            if (m < 1e-20) {  // src/FARCE.jl:2226-2238
+#pragma unroll
+                for (int a = 0; a < 4; a++) o[a] /= m;
+                lm += log(m);
+            }
+#pragma unroll
+            for (int a = 0; a < 4; a++) pv[a] = o[a];
+            lmv[(size_t)v * L + x] = lm;
+        }
+        const double* pr = part + (size_t)x * 4;  // root = node 0
+        double tot = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; a++) tot += pi4[a] * pr[a];
+        const double ll = log(tot) + lmv[x] + logw_site[s];
+        acc = (s == 0) ? ll : lse_d(acc, ll);
+    }
+    u[x] = acc;
+}
+
+int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, const double* d_pi4,
+                    const double* d_logw_site, int nsite, double* d_u)
+{
+    void* scratch;
+    const size_t n = (size_t)ds->numnodes * ds->L;
+    int rc = ensure(ctx, 20, n * 5 * sizeof(double), &scratch);
+    if (rc) return rc;
+    double* part = (double*)scratch;
+    double* lmv = part + n * 4;
+    const int bs = 128;
+    unpaired_kernel<<<(ds->L + bs - 1) / bs, bs, 0, ctx->stream>>>(ds->d_masks, ds->d_tree, ds->d_post,
+                                                                   ds->numnodes, ds->L, d_P4, d_pi4, d_logw_site,
+                                                                   nsite, part, lmv, d_u);
+    LAUNCH_CHECK(ctx, "unpaired_kernel");
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Output layouts
+// ---------------------------------------------------------------------------
+__global__ void scatter_dense_kernel(const int* __restrict__ bandidx, const double* __restrict__ vals, int L, int W,
+                                     double* __restrict__ out)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)L * L) return;
+    const int x = (int)(idx % L), y = (int)(idx / L);
+    const int k = (x > y) ? x - y : y - x;
+    const int i = (x < y) ? x : y;
+    double val = -INFINITY;
+    if (k >= 1 && k <= W) {
+        const int b = bandidx[(size_t)i * (W + 1) + k];
+        if (b >= 0) val = vals[b];
+    }
+    out[idx] = val;
+}
+
+int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, double* d_out)
+{
+    const long long n = (long long)ds->L * ds->L;
+    const int bs = 256;
+    scatter_dense_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, ctx->stream>>>(ds->d_bandidx, d_vals, ds->L, ds->W,
+                                                                                d_out);
+    LAUNCH_CHECK(ctx, "scatter_dense_kernel");
+    return MESSI_OK;
+}
+
+// Banded log-odds pair scores from the root mixtures (device-resident path),
+// with maskgapped! (src/RNATools.jl:441-451) folded in.
+__global__ void bandprep_from_mix_kernel(const int* __restrict__ bandidx, const double* __restrict__ mix, int L, int W,
+                                         int Wb, int RS, const uint8_t* __restrict__ gapmask,
+                                         const double* __restrict__ b, double B, float* __restrict__ pb)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)L * RS) return;
+    const int i = (int)(idx / RS), k = (int)(idx % RS);
+    float out = -INFINITY;
+    if (k >= 1 && k <= Wb && i + k < L && k <= W) {
+        const int bi = bandidx[(size_t)i * (W + 1) + k];
+        if (bi >= 0 && !(gapmask && (gapmask[i] || gapmask[i + k]))) {
+            const double p = mix[bi];
+            if (p != -INFINITY) out = (float)(B * p - b[i] - b[i + k]);
+        }
+    }
+    pb[idx] = out;
+}
+
+int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask, double B)
+{
+    const long long n = (long long)t.L * t.RS;
+    const int bs = 256;
+    bandprep_from_mix_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, ctx->stream>>>(
+        ds->d_bandidx, ds->d_mix, ds->L, ds->W, t.Wb, t.RS, d_gapmask, t.b, B, t.pb);
+    LAUNCH_CHECK(ctx, "bandprep_from_mix_kernel");
+    return MESSI_OK;
+}
+
+}  // namespace messi

@@ -1,0 +1,722 @@
+// scfg.cu -- KH99 SCFG inside/outside passes and base-pairing posteriors (HP2).
+//
+// Replaces initialiseinside / insidealgorithm / insidez / outsidealgorithm of
+// src/cuda/inside.cu (driven by src/InsideCUDA.jl:87-181, 301-389) and the
+// CPU computebasepairprobs (src/InsideOutsideAlgorithm.jl:486-533).
+//
+// Representation.  Cells are stored as FP32 log-odds against a per-column
+// baseline b_k = B*(u_k + log r1 + log r6) (u_k: unpaired log-likelihood):
+//     Xbar(i,j) = X(i,j) - sum_{k=i..j} b_k.
+// The baseline is additive over the split point, so the recurrences keep
+// their form with pair scores pbar_ij = B*p_ij - b_i - b_j; an all-unpaired
+// span keeps Sbar constant, which keeps FP32 magnitudes small.  The prefix
+// sums of b and Z = Sbar(0, L-1) + sum_k b_k are FP64.
+//
+// Banding.  With every pair of span > Wb forbidden, only cells of span <= Wb
+// and the S cells of the last column (the "suffix") reach Z
+// (S->LS chains end at j = L-1; F and L need an enclosing or own pair), so
+// the pass keeps a band of Wb+1 diagonals plus one suffix column.
+//
+// Layouts (row stride RS floats, RS >= Wb+1, multiple of 32):
+//   Lrow[i][k] = Lbar(i, i+k)     Lcol[j][k] = Lbar(j-k, j)
+//   Srow[i][k] = Sbar(i, i+k)     Scol[j][k] = Sbar(j-k, j)
+//   Frow[i][k] = Fbar(i, i+k)     pb[i][k]   = pbar(i, i+k)
+//   Ssuf[i]    = Sbar(i, L-1)
+// so the split sum of cell (i, j) reads row i of L and column j of S with
+// unit stride.  Outside tables mirror them (OSrow/OScol/OFrow/OFcol/OLrow/Osuf).
+//
+// Schedule.  One launch per span diagonal; a cell is reduced by a group of G
+// lanes (G grows with the number of split points) with shuffle log-sum-exp.
+// The suffix recurrences run in one CTA in blocks of 32 cells: the terms that
+// reach outside the block are summed by 32 warps in parallel, the in-block
+// triangle by one warp.
+#include <algorithm>
+#include <cmath>
+
+#include "internal.h"
+
+namespace messi {
+
+namespace {
+
+__device__ __forceinline__ void lse_add(float& m, float& s, float x)
+{
+    if (x > m) {
+        s = s * __expf(m - x) + 1.f;
+        m = x;
+    } else if (x != -INFINITY) {
+        s += __expf(x - m);
+    }
+}
+
+__device__ __forceinline__ void lse_merge(float& m, float& s, float m2, float s2)
+{
+    if (m2 > m) {
+        s = s * __expf(m - m2) + s2;
+        m = m2;
+    } else if (m2 != -INFINITY) {
+        s += s2 * __expf(m2 - m);
+    }
+}
+
+__device__ __forceinline__ float lse_val(float m, float s) { return (m == -INFINITY) ? -INFINITY : m + __logf(s); }
+
+__device__ __forceinline__ float lse2f(float a, float b)
+{
+    const float m = fmaxf(a, b);
+    if (m == -INFINITY) return -INFINITY;
+    return m + __logf(__expf(a - m) + __expf(b - m));
+}
+
+template <int G>
+__device__ __forceinline__ void group_reduce(float& m, float& s)
+{
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+        const float m2 = __shfl_xor_sync(0xffffffffu, m, off);
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+        lse_merge(m, s, m2, s2);
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------
+int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
+{
+    t->L = L;
+    t->Wb = Wb;
+    t->RS = ((Wb + 1 + 31) / 32) * 32;
+    const size_t tab = (size_t)L * t->RS * sizeof(float);
+    void* p;
+    int rc;
+    float** in_tabs[6] = {&t->Lrow, &t->Lcol, &t->Srow, &t->Scol, &t->Frow, &t->pb};
+    for (int k = 0; k < 6; k++) {
+        if ((rc = ensure(ctx, k, tab, &p))) return rc;
+        *in_tabs[k] = (float*)p;
+    }
+    if ((rc = ensure(ctx, 6, (size_t)(L + 1) * sizeof(float) * 2, &p))) return rc;
+    t->Ssuf = (float*)p;
+    t->Osuf = t->Ssuf + (L + 1);
+    if ((rc = ensure(ctx, 7, (size_t)(3 * L + 8) * sizeof(double), &p))) return rc;
+    t->b = (double*)p;
+    t->cb = t->b + L;
+    t->u = t->cb + (L + 1);
+    t->Zd = t->u + L;
+    t->maxspan = (int*)(t->Zd + 2);
+    if (outside) {
+        float** out_tabs[6] = {&t->OSrow, &t->OScol, &t->OFrow, &t->OFcol, &t->OLrow, &t->PP};
+        for (int k = 0; k < 6; k++) {
+            if ((rc = ensure(ctx, 8 + k, tab, &p))) return rc;
+            *out_tabs[k] = (float*)p;
+        }
+        if ((rc = ensure(ctx, 14, (size_t)2 * L * sizeof(float), &p))) return rc;
+        t->SL = (float*)p;
+        t->nrm = t->SL + L;
+    } else {
+        t->OSrow = t->OScol = t->OFrow = t->OFcol = t->OLrow = t->PP = t->SL = t->nrm = nullptr;
+    }
+    return MESSI_OK;
+}
+
+static Rules make_rules(double B)
+{
+    static const double p[7] = {0.868534, 0.117609877998, 0.013856122002, 0.787640, 0.21236, 0.894603, 0.105397};
+    Rules r;
+    for (int k = 0; k < 7; k++) r.r[k] = (float)(B * std::log(p[k]));
+    return r;
+}
+
+static double baseline_c() { return std::log(0.868534) + std::log(0.894603); }
+
+// ---------------------------------------------------------------------------
+// baseline b_k and prefix sums cb (one block, deterministic FP64 scan)
+// ---------------------------------------------------------------------------
+__global__ void baseline_kernel(const double* __restrict__ u, int L, double B, double c, double* __restrict__ b,
+                                double* __restrict__ cb)
+{
+    __shared__ double part[1024];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int per = (L + nt - 1) / nt;
+    const int lo = min(L, t * per), hi = min(L, lo + per);
+    double s = 0.0;
+    for (int k = lo; k < hi; k++) {
+        const double uk = u[k];
+        const double bk = B * ((isfinite(uk) ? uk : 0.0) + c);
+        b[k] = bk;
+        s += bk;
+    }
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < nt; off <<= 1) {
+        const double v = (t >= off) ? part[t - off] : 0.0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    double run = (t == 0) ? 0.0 : part[t - 1];
+    for (int k = lo; k < hi; k++) {
+        cb[k] = run;
+        run += b[k];
+    }
+    if (t == nt - 1) cb[L] = part[nt - 1];
+}
+
+int launch_baseline(messi_ctx* ctx, const Band& t, double B)
+{
+    baseline_kernel<<<1, 1024, 0, ctx->stream>>>(t.u, t.L, B, baseline_c(), t.b, t.cb);
+    LAUNCH_CHECK(ctx, "baseline_kernel");
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pair-score preparation from a dense host matrix
+// ---------------------------------------------------------------------------
+__global__ void maxspan_kernel(const double* __restrict__ p, int L, int* __restrict__ out)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int best = 0;
+    if (idx < (long long)L * L) {
+        const int i = (int)(idx % L), j = (int)(idx / L);
+        if (i < j && isfinite(p[idx])) best = j - i;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, off));
+    if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(out, best);
+}
+
+int launch_maxspan(messi_ctx* ctx, int L, const double* d_dense, int* d_out)
+{
+    cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(int), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset maxspan");
+    const long long n = (long long)L * L;
+    maxspan_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(d_dense, L, d_out);
+    LAUNCH_CHECK(ctx, "maxspan_kernel");
+    return MESSI_OK;
+}
+
+// pb[i][k] from the upper triangle p(i, i+k) of a dense column-major matrix.
+// Threads walk i fastest for a fixed column j so the dense reads coalesce.
+__global__ void bandprep_from_dense_kernel(const double* __restrict__ p, int L, int Wb, int RS,
+                                           const double* __restrict__ b, double B, float* __restrict__ pb)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)L * RS) return;
+    const int j = (int)(idx / RS), r = (int)(idx % RS);
+    // r enumerates rows i = j - RS + 1 + r .. j; k = j - i
+    const int k = RS - 1 - r;
+    const int i = j - k;
+    if (i < 0) return;
+    float out = -INFINITY;
+    if (k >= 1 && k <= Wb) {
+        const double v = p[(size_t)i + (size_t)j * L];
+        if (v != -INFINITY && !isnan(v)) out = (float)(B * v - b[i] - b[j]);
+    }
+    pb[(size_t)i * RS + k] = out;
+}
+
+__global__ void fill_kernel(float* __restrict__ a, long long n, float v)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < n) a[idx] = v;
+}
+
+static int fill(messi_ctx* ctx, float* a, long long n, float v)
+{
+    fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(a, n, v);
+    LAUNCH_CHECK(ctx, "fill_kernel");
+    return MESSI_OK;
+}
+
+int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_dense, double B)
+{
+    int rc = fill(ctx, t.pb, (long long)t.L * t.RS, -INFINITY);
+    if (rc) return rc;
+    const long long n = (long long)t.L * t.RS;
+    bandprep_from_dense_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(d_dense, t.L, t.Wb, t.RS, t.b,
+                                                                                      B, t.pb);
+    LAUNCH_CHECK(ctx, "bandprep_from_dense_kernel");
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// inside
+// ---------------------------------------------------------------------------
+__global__ void inside_init_kernel(Band t, Rules R, double B)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.L) return;
+    const double ui = t.u[i];
+    const float S = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[1] - t.b[i]);
+    const float Lv = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[5] - t.b[i]);
+    const size_t o = (size_t)i * t.RS;
+    t.Srow[o] = S;
+    t.Scol[o] = S;
+    t.Lrow[o] = Lv;
+    t.Lcol[o] = Lv;
+    t.Frow[o] = -INFINITY;
+    if (i == t.L - 1) t.Ssuf[i] = S;
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) inside_diag_kernel(Band t, Rules R, int d)
+{
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x & (G - 1);
+    const int i = gid;
+    const bool valid = i < t.L - d;
+    float m = -INFINITY, s = 0.f;
+    if (valid) {
+        const int j = i + d;
+        const float* lrow = t.Lrow + (size_t)i * t.RS;
+        const float* scol = t.Scol + (size_t)j * t.RS + (d - 1);
+        for (int k = lane; k < d; k += G) lse_add(m, s, lrow[k] + scol[-k]);
+    }
+    group_reduce<G>(m, s);
+    if (!valid || lane != 0) return;
+    const int j = i + d;
+    const float tmp = lse_val(m, s);
+    const float v = (d >= 2) ? t.pb[(size_t)i * t.RS + d] + t.Frow[(size_t)(i + 1) * t.RS + (d - 2)] : -INFINITY;
+    const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
+    const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
+    const float Lv = R.r[6] + v;
+    t.Lrow[(size_t)i * t.RS + d] = Lv;
+    t.Lcol[(size_t)j * t.RS + d] = Lv;
+    t.Srow[(size_t)i * t.RS + d] = S;
+    t.Scol[(size_t)j * t.RS + d] = S;
+    t.Frow[(size_t)i * t.RS + d] = F;
+    if (j == t.L - 1) t.Ssuf[i] = S;
+}
+
+// Ssuf[i] for spans beyond the band (i < T = L-1-Wb), descending i:
+// Ssuf[i] = r1 + LSE_{k=0..Wb} (Lrow[i][k] + Ssuf[i+k+1]).
+__global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R)
+{
+    const int T = t.L - 1 - t.Wb;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ float known[32];
+    for (int i0 = T - 1; i0 >= 0; i0 -= 32) {
+        const int lo = max(0, i0 - 31);
+        const int i = i0 - w;
+        if (i >= lo) {
+            float m = -INFINITY, s = 0.f;
+            const float* lrow = t.Lrow + (size_t)i * t.RS;
+            for (int k = (i0 - i) + lane; k <= t.Wb; k += 32) lse_add(m, s, lrow[k] + t.Ssuf[i + k + 1]);
+            group_reduce<32>(m, s);
+            if (lane == 0) known[w] = lse_val(m, s);
+        }
+        __syncthreads();
+        if (w == 0) {
+            const int nb = i0 - lo + 1;
+            float mine = -INFINITY;  // lane l holds Ssuf[i0 - l] once computed
+            for (int l = 0; l < nb; l++) {
+                const int ic = i0 - l;
+                const int k = l - lane - 1;
+                float x = -INFINITY;
+                if (lane < l && k <= t.Wb) x = t.Lrow[(size_t)ic * t.RS + k] + mine;
+                float m = x, s = (x == -INFINITY) ? 0.f : 1.f;
+                group_reduce<32>(m, s);
+                const float sv = R.r[0] + lse2f(known[l], lse_val(m, s));
+                if (lane == l) mine = sv;
+                if (lane == 0) t.Ssuf[ic] = sv;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void finish_Z_kernel(Band t)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) t.Zd[0] = (double)t.Ssuf[0] + t.cb[t.L];
+}
+
+int launch_finish_Z(messi_ctx* ctx, const Band& t)
+{
+    finish_Z_kernel<<<1, 32, 0, ctx->stream>>>(t);
+    LAUNCH_CHECK(ctx, "finish_Z_kernel");
+    return MESSI_OK;
+}
+
+template <int G>
+static int launch_inside_diag(messi_ctx* ctx, const Band& t, const Rules& R, int d)
+{
+    const long long threads = (long long)(t.L - d) * G;
+    inside_diag_kernel<G><<<(unsigned)((threads + 255) / 256), 256, 0, ctx->stream>>>(t, R, d);
+    LAUNCH_CHECK(ctx, "inside_diag_kernel");
+    return MESSI_OK;
+}
+
+static int inside_diag(messi_ctx* ctx, const Band& t, const Rules& R, int d, int nterms)
+{
+    if (nterms <= 8) return launch_inside_diag<1>(ctx, t, R, d);
+    if (nterms <= 32) return launch_inside_diag<4>(ctx, t, R, d);
+    if (nterms <= 96) return launch_inside_diag<8>(ctx, t, R, d);
+    if (nterms <= 256) return launch_inside_diag<16>(ctx, t, R, d);
+    return launch_inside_diag<32>(ctx, t, R, d);
+}
+
+int run_inside(messi_ctx* ctx, const Band& t, double B)
+{
+    const Rules R = make_rules(B);
+    inside_init_kernel<<<(t.L + 255) / 256, 256, 0, ctx->stream>>>(t, R, B);
+    LAUNCH_CHECK(ctx, "inside_init_kernel");
+    int rc;
+    for (int d = 1; d <= t.Wb; d++) {
+        prof_begin(ctx, 1, (double)(t.L - d));
+        if ((rc = inside_diag(ctx, t, R, d, d))) return rc;
+        prof_end(ctx);
+    }
+    if (t.L - 1 > t.Wb) {
+        prof_begin(ctx, 2, (double)(t.L - 1 - t.Wb));
+        inside_suffix_kernel<<<1, 1024, 0, ctx->stream>>>(t, R);
+        LAUNCH_CHECK(ctx, "inside_suffix_kernel");
+        prof_end(ctx);
+    }
+    return launch_finish_Z(ctx, t);
+}
+
+// ---------------------------------------------------------------------------
+// outside
+// ---------------------------------------------------------------------------
+// Osuf[i] for spans beyond the band on the last column, ascending i:
+// Osuf[0] = 0;  Osuf[i] = r1 + LSE_{k=0..Wb, i-k-1>=0} (Osuf[i-k-1] + Lcol[i-1][k]).
+__global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
+{
+    const int T = t.L - 1 - t.Wb;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ float known[32];
+    for (int i0 = 0; i0 < T; i0 += 32) {
+        const int hi = min(T - 1, i0 + 31);
+        const int i = i0 + w;
+        if (i <= hi) {
+            float m = -INFINITY, s = 0.f;
+            if (i >= 1) {
+                const float* lcol = t.Lcol + (size_t)(i - 1) * t.RS;
+                const int kmax = min(t.Wb, i - 1);
+                for (int k = (i - i0) + lane; k <= kmax; k += 32) lse_add(m, s, t.Osuf[i - k - 1] + lcol[k]);
+            }
+            group_reduce<32>(m, s);
+            if (lane == 0) known[w] = lse_val(m, s);
+        }
+        __syncthreads();
+        if (w == 0) {
+            const int nb = hi - i0 + 1;
+            float mine = -INFINITY;  // lane l holds Osuf[i0 + l]
+            for (int l = 0; l < nb; l++) {
+                const int ic = i0 + l;
+                const int k = l - lane - 1;
+                float x = -INFINITY;
+                if (lane < l && k <= t.Wb && ic >= 1) x = t.Lcol[(size_t)(ic - 1) * t.RS + k] + mine;
+                float m = x, s = (x == -INFINITY) ? 0.f : 1.f;
+                group_reduce<32>(m, s);
+                const float sv = (ic == 0) ? 0.f : R.r[0] + lse2f(known[l], lse_val(m, s));
+                if (lane == l) mine = sv;
+                if (lane == 0) t.Osuf[ic] = sv;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) outside_diag_kernel(Band t, Rules R, int d)
+{
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x & (G - 1);
+    const int i = gid;
+    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    const bool valid = i < L - d;
+    const int j = i + d;
+    float mL = -INFINITY, sL = 0.f, mS = -INFINITY, sS = 0.f;
+    if (valid) {
+        // L(i,j) as left child of S->LS / F->LS at parents (i, jp), jp in (j, min(i+Wb, L-1)]
+        const int nL = min(i + Wb, L - 1) - j;
+        const float* osr = t.OSrow + (size_t)i * RS + d + 1;
+        const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
+        if (j + 1 <= L - 1) {
+            const float* srw = t.Srow + (size_t)(j + 1) * RS;
+            for (int q = lane; q < nL; q += G) {
+                const float sib = srw[q];
+                lse_add(mL, sL, R.r[0] + osr[q] + sib);
+                lse_add(mL, sL, R.r[4] + ofr[q] + sib);
+            }
+            if (lane == 0 && L - 1 > i + Wb) lse_add(mL, sL, R.r[0] + t.Osuf[i] + t.Ssuf[j + 1]);
+        }
+        // S(i,j) as right child at parents (ip, j), ip in [max(0, j-Wb), i)
+        if (i >= 1) {
+            const int ip0 = max(0, j - Wb);
+            const int nS = i - ip0;
+            const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
+            const float* osc = t.OScol + (size_t)j * RS + d + 1;
+            const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
+            for (int q = lane; q < nS; q += G) {
+                const float lft = lcol[q];
+                lse_add(mS, sS, R.r[0] + osc[q] + lft);
+                lse_add(mS, sS, R.r[4] + ofc[q] + lft);
+            }
+            if (j == L - 1) {
+                const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
+                for (int ip = a + lane; ip <= bnd; ip += G) lse_add(mS, sS, R.r[0] + t.Osuf[ip] + lcol[i - 1 - ip]);
+            }
+        }
+    }
+    group_reduce<G>(mL, sL);
+    group_reduce<G>(mS, sS);
+    if (!valid || lane != 0) return;
+    const float oL = lse_val(mL, sL);
+    float oS = lse_val(mS, sS);
+    if (i == 0 && j == L - 1) oS = 0.f;
+    float oF = -INFINITY;
+    if (i >= 1 && j <= L - 2 && d + 2 <= Wb) {
+        const size_t pr = (size_t)(i - 1) * RS + d + 2;
+        const float pp = t.pb[pr];
+        if (pp != -INFINITY) {
+            float m = -INFINITY, s = 0.f;
+            lse_add(m, s, R.r[2] + pp + t.OSrow[pr]);
+            lse_add(m, s, R.r[3] + pp + t.OFrow[pr]);
+            lse_add(m, s, R.r[6] + pp + t.OLrow[pr]);
+            oF = lse_val(m, s);
+        }
+    }
+    t.OSrow[(size_t)i * RS + d] = oS;
+    t.OScol[(size_t)j * RS + d] = oS;
+    t.OFrow[(size_t)i * RS + d] = oF;
+    t.OFcol[(size_t)j * RS + d] = oF;
+    t.OLrow[(size_t)i * RS + d] = oL;
+    if (j == L - 1) t.Osuf[i] = oS;
+}
+
+template <int G>
+static int launch_outside_diag(messi_ctx* ctx, const Band& t, const Rules& R, int d)
+{
+    const long long threads = (long long)(t.L - d) * G;
+    outside_diag_kernel<G><<<(unsigned)((threads + 255) / 256), 256, 0, ctx->stream>>>(t, R, d);
+    LAUNCH_CHECK(ctx, "outside_diag_kernel");
+    return MESSI_OK;
+}
+
+int run_outside(messi_ctx* ctx, const Band& t, double B)
+{
+    const Rules R = make_rules(B);
+    int rc;
+    if (t.L - 1 > t.Wb) {
+        outside_suffix_kernel<<<1, 1024, 0, ctx->stream>>>(t, R);
+        LAUNCH_CHECK(ctx, "outside_suffix_kernel");
+    }
+    for (int d = t.Wb; d >= 0; d--) {
+        const int nterms = 2 * (t.Wb - d) + 2;
+        prof_begin(ctx, 3, (double)(t.L - d));
+        if (nterms <= 8) rc = launch_outside_diag<1>(ctx, t, R, d);
+        else if (nterms <= 32) rc = launch_outside_diag<4>(ctx, t, R, d);
+        else if (nterms <= 96) rc = launch_outside_diag<8>(ctx, t, R, d);
+        else if (nterms <= 256) rc = launch_outside_diag<16>(ctx, t, R, d);
+        else rc = launch_outside_diag<32>(ctx, t, R, d);
+        if (rc) return rc;
+        prof_end(ctx);
+    }
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// posteriors (computebasepairprobs, row-normalised)
+// ---------------------------------------------------------------------------
+__global__ void post_cells_kernel(Band t, Rules R, double B)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)t.L * t.RS) return;
+    const int j = (int)(idx / t.RS), d = (int)(idx % t.RS);
+    const float Zbar = t.Ssuf[0];
+    if (d == 0) {
+        float m = -INFINITY, s = 0.f;
+        lse_add(m, s, t.OSrow[(size_t)j * t.RS] + R.r[1]);
+        lse_add(m, s, t.OLrow[(size_t)j * t.RS] + R.r[5]);
+        const double uj = t.u[j];
+        t.SL[j] = (uj == -INFINITY) ? -INFINITY : (float)((double)lse_val(m, s) + B * uj - t.b[j]) - Zbar;
+        t.PP[idx] = -INFINITY;
+        return;
+    }
+    float out = -INFINITY;
+    if (d <= t.Wb && j + d < t.L) {
+        const float pp = t.pb[idx];
+        const float fin = (d >= 2) ? t.Frow[(size_t)(j + 1) * t.RS + (d - 2)] : -INFINITY;
+        if (pp != -INFINITY && fin != -INFINITY) {
+            float m = -INFINITY, s = 0.f;
+            lse_add(m, s, t.OSrow[idx] + R.r[2]);
+            lse_add(m, s, t.OFrow[idx] + R.r[3]);
+            lse_add(m, s, t.OLrow[idx] + R.r[6]);
+            out = lse_val(m, s) + fin + pp - Zbar;
+        }
+    }
+    t.PP[idx] = out;
+}
+
+// one warp per row x: log normaliser over the unpaired term and every partner
+__global__ void post_norm_kernel(Band t)
+{
+    const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (x >= t.L) return;
+    float m = -INFINITY, s = 0.f;
+    if (lane == 0) lse_add(m, s, t.SL[x]);
+    for (int d = 1 + lane; d <= t.Wb; d += 32) {
+        if (x + d < t.L) lse_add(m, s, t.PP[(size_t)x * t.RS + d]);
+        if (x - d >= 0) lse_add(m, s, t.PP[(size_t)(x - d) * t.RS + d]);
+    }
+    group_reduce<32>(m, s);
+    if (lane == 0) t.nrm[x] = lse_val(m, s);
+}
+
+__global__ void post_dense_kernel(Band t, double* __restrict__ single, double* __restrict__ pair)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = t.L;
+    if (idx >= (long long)L * L) return;
+    const int x = (int)(idx % L), y = (int)(idx / L);
+    const int k = (x > y) ? x - y : y - x;
+    double v = 0.0;
+    if (k >= 1 && k <= t.Wb) {
+        const int i = (x < y) ? x : y;
+        const float pp = t.PP[(size_t)i * t.RS + k];
+        if (pp != -INFINITY) v = exp((double)pp - (double)t.nrm[x]);
+    }
+    pair[idx] = v;
+    if (y == 0) single[x] = exp((double)t.SL[x] - (double)t.nrm[x]);
+}
+
+int run_posteriors(messi_ctx* ctx, const Band& t, double B, double* d_single, double* d_pair)
+{
+    const Rules R = make_rules(B);
+    const long long n = (long long)t.L * t.RS;
+    post_cells_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(t, R, B);
+    LAUNCH_CHECK(ctx, "post_cells_kernel");
+    post_norm_kernel<<<(unsigned)(((long long)t.L * 32 + 255) / 256), 256, 0, ctx->stream>>>(t);
+    LAUNCH_CHECK(ctx, "post_norm_kernel");
+    const long long nn = (long long)t.L * t.L;
+    post_dense_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx->stream>>>(t, d_single, d_pair);
+    LAUNCH_CHECK(ctx, "post_dense_kernel");
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dense (Julia-layout) tables <-> band tables
+// ---------------------------------------------------------------------------
+__global__ void dense_inside_kernel(Band t, double* __restrict__ out)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = t.L;
+    if (idx >= (long long)L * L) return;
+    const int i = (int)(idx % L), j = (int)(idx / L);
+    double S = -INFINITY, F = -INFINITY, Lv = -INFINITY;
+    if (j >= i) {
+        const int d = j - i;
+        const double base = t.cb[j + 1] - t.cb[i];
+        if (d <= t.Wb) {
+            const size_t o = (size_t)i * t.RS + d;
+            S = (double)t.Srow[o] + base;
+            F = (double)t.Frow[o] + base;
+            Lv = (double)t.Lrow[o] + base;
+        } else if (j == L - 1) {
+            S = (double)t.Ssuf[i] + base;
+        }
+    }
+    out[3 * idx] = S;
+    out[3 * idx + 1] = F;
+    out[3 * idx + 2] = Lv;
+}
+
+__global__ void dense_outside_kernel(Band t, double* __restrict__ out)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = t.L;
+    if (idx >= (long long)L * L) return;
+    const int i = (int)(idx % L), j = (int)(idx / L);
+    double S = -INFINITY, F = -INFINITY, Lv = -INFINITY;
+    if (j >= i) {
+        const int d = j - i;
+        const double base = t.cb[L] - (t.cb[j + 1] - t.cb[i]);
+        if (d <= t.Wb) {
+            const size_t o = (size_t)i * t.RS + d;
+            S = (double)t.OSrow[o] + base;
+            F = (double)t.OFrow[o] + base;
+            Lv = (double)t.OLrow[o] + base;
+        } else if (j == L - 1) {
+            S = (double)t.Osuf[i] + base;
+        }
+    }
+    out[3 * idx] = S;
+    out[3 * idx + 1] = F;
+    out[3 * idx + 2] = Lv;
+}
+
+int launch_dense_inside(messi_ctx* ctx, const Band& t, double* d_out)
+{
+    const long long n = (long long)t.L * t.L;
+    dense_inside_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(t, d_out);
+    LAUNCH_CHECK(ctx, "dense_inside_kernel");
+    return MESSI_OK;
+}
+
+int launch_dense_outside(messi_ctx* ctx, const Band& t, double* d_out)
+{
+    const long long n = (long long)t.L * t.L;
+    dense_outside_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(t, d_out);
+    LAUNCH_CHECK(ctx, "dense_outside_kernel");
+    return MESSI_OK;
+}
+
+__global__ void band_from_dense_inside_kernel(Band t, const double* __restrict__ in)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = t.L;
+    if (idx >= (long long)L * L) return;
+    const int i = (int)(idx % L), j = (int)(idx / L);
+    if (j < i) return;
+    const int d = j - i;
+    const double base = t.cb[j + 1] - t.cb[i];
+    const double S = in[3 * idx], F = in[3 * idx + 1], Lv = in[3 * idx + 2];
+    if (d <= t.Wb) {
+        const float s = (float)(S - base), f = (float)(F - base), l = (float)(Lv - base);
+        t.Srow[(size_t)i * t.RS + d] = s;
+        t.Scol[(size_t)j * t.RS + d] = s;
+        t.Frow[(size_t)i * t.RS + d] = f;
+        t.Lrow[(size_t)i * t.RS + d] = l;
+        t.Lcol[(size_t)j * t.RS + d] = l;
+    }
+    if (j == L - 1) t.Ssuf[i] = (float)(S - base);
+}
+
+__global__ void band_from_dense_outside_kernel(Band t, const double* __restrict__ in)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = t.L;
+    if (idx >= (long long)L * L) return;
+    const int i = (int)(idx % L), j = (int)(idx / L);
+    if (j < i) return;
+    const int d = j - i;
+    if (d > t.Wb) return;
+    const double base = t.cb[L] - (t.cb[j + 1] - t.cb[i]);
+    const size_t o = (size_t)i * t.RS + d;
+    t.OSrow[o] = (float)(in[3 * idx] - base);
+    t.OFrow[o] = (float)(in[3 * idx + 1] - base);
+    t.OLrow[o] = (float)(in[3 * idx + 2] - base);
+}
+
+int launch_band_from_dense_inside(messi_ctx* ctx, const Band& t, const double* d_in)
+{
+    const long long n = (long long)t.L * t.L;
+    band_from_dense_inside_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(t, d_in);
+    LAUNCH_CHECK(ctx, "band_from_dense_inside_kernel");
+    return MESSI_OK;
+}
+
+int launch_band_from_dense_outside(messi_ctx* ctx, const Band& t, const double* d_out)
+{
+    const long long n = (long long)t.L * t.L;
+    band_from_dense_outside_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(t, d_out);
+    LAUNCH_CHECK(ctx, "band_from_dense_outside_kernel");
+    return MESSI_OK;
+}
+
+}  // namespace messi
