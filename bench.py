@@ -32,6 +32,10 @@ sys.path.insert(0, ROOT)
 METRIC = "site-pair likelihoods/s"
 UNIT = "pairs/s"
 WORKLOAD = "c2"
+WORKLOAD_TEXT = {"c2": "c2: 64 seqs x 1,000 nt, max pair span 500",
+                 "c2p": "c2p: 64 seqs x 600 nt, max pair span 300",
+                 "c4": "c4: 30 seqs x 9,000 nt, max pair span 800",
+                 "c1": "c1: 16 seqs x 120 nt, all pairs"}
 BYTES_PER_UPDATE = 212  # algorithmic bytes of one node update (2 child rows + exps + indices in, 1 row out)
 # DRAM bytes per node update of prune_level_kernel from an ncu capture
 # (profiles/prune_level_kernel_c2.md); None until captured.
@@ -172,7 +176,7 @@ def run_reference(args):
     if rank != 0:
         return
     from messi_gb300 import synth
-    s = synth.make_workload(WORKLOAD, seed=1)
+    s = synth.make_workload(args.workload, seed=1)
     L, W = s.dataset.numcols, s.W
     npairs = total_pairs(L, W)
     nthreads = os.cpu_count() or 1
@@ -192,7 +196,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-        "config": {"workload": f"{WORKLOAD}: 64 seqs x 1,000 nt, max pair span 500, 45 categories",
+        "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories",
                    "pairs_per_full_step": npairs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": f"{rows_per_step} alignment rows of pairs per step (~{int(statistics.mean(samples))} "
@@ -213,7 +217,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from messi_gb300 import api, synth
 
-    s = synth.make_workload(WORKLOAD, seed=1 + rank)
+    s = synth.make_workload(args.workload, seed=1 + rank)
     ds = s.dataset
     L, W = ds.numcols, s.W
     npairs = total_pairs(L, W)
@@ -237,6 +241,13 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     for k in range(args.warmup):
         step(margs[k])
+    if args.profile_only:
+        # minimal launch sequence for profilers: the timed steps only
+        for k in range(args.steps):
+            step(margs[args.warmup + k])
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_only": args.workload, "steps": args.steps, "Z": Zc.value}), flush=True)
+        return
 
     def barrier():
         if ws > 1:
@@ -329,8 +340,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": f"{WORKLOAD}: 64 seqs x 1,000 nt, max pair span 500, 45 categories "
-                               "(3 x 3 site rates x 5 lambda), 30% paired, 5% gaps",
+        "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories "
+                               "(3 x 3 site rates x 5 lambda), synthetic from seed, 5% gaps",
                    "pairs_per_step": npairs, "step": "unpaired + pair pruning + gap mask + banded inside -> Z",
                    "l2": "flushed between steps (256 MB write outside the timed events)",
                    "parallelism": f"replicas x{ws}", "plan": stats},
@@ -359,6 +370,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT))
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warm-up + timed steps only (for ncu), print a short line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -12,6 +12,7 @@ Named workloads (seeded ``numpy.random.Generator(PCG64(seed))``):
   "c1": 16 seqs x 120 nt, every pair (W = 119), 30% paired, mean branch 0.1
   "c2": 64 seqs x 1,000 nt, max pair span 500, 30% paired, mean branch 0.1
   "c4": 30 seqs x 9,000 nt, max pair span 800, 20% paired, mean branch 0.05
+  "c2p": 64 seqs x 600 nt, max pair span 300 (profiling-sized c2)
 Every workload: pi ~ Dirichlet(5,5,5,5), lambda_GC/AT/GT ~ U(1,5), exchange
 rates and site-rate shape at the reference's starting vector
 (src/MESSI.jl:1479), 5% i.i.d. gaps.
@@ -28,6 +29,8 @@ WORKLOADS = {
     "c1": dict(numseqs=16, numcols=120, W=119, paired=0.30, mean_bl=0.10),
     "c2": dict(numseqs=64, numcols=1000, W=500, paired=0.30, mean_bl=0.10),
     "c4": dict(numseqs=30, numcols=9000, W=800, paired=0.20, mean_bl=0.05),
+    # profiling-sized case of the c2 shape (about 2 GB of partials)
+    "c2p": dict(numseqs=64, numcols=600, W=300, paired=0.30, mean_bl=0.10),
 }
 
 
