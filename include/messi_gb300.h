@@ -35,6 +35,7 @@ extern "C" {
 #define MESSI_ECUDA -3    /* a CUDA call failed */
 #define MESSI_ETIMEOUT -4 /* a bounded device-side wait gave up */
 #define MESSI_ESTATE -5   /* object used in the wrong state */
+#define MESSI_ETOOBIG -6  /* problem larger than a fixed-size buffer allows */
 
 typedef struct messi_ctx messi_ctx;
 typedef struct messi_dataset messi_dataset;
@@ -158,6 +159,25 @@ int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const do
  * pair.  Z: log marginal likelihood.  unpaired: optional [L] output. */
 int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const double* gapfrequency,
                      double gapcutoff, double* Z, double* unpaired);
+
+/* KH99 inside pass that allocates nothing (no counterpart in the reference;
+ * computeinsideKH99 always allocates its tables).  For callers that must not
+ * call cudaMalloc -- code running under CUDA stream capture, inside a
+ * framework that owns the device allocator, or in a loop that must not enter
+ * the driver's allocator.  Inputs and output are DEVICE pointers; the work is
+ * queued on `stream` (a cudaStream_t) of the current device:
+ *   d_unpaired [L] doubles, d_paired [L x L] column-major doubles, d_Z one
+ *   double.  maxspan as in messi_inside (< 0 infers it, which synchronises
+ *   `stream` once to read the span back).
+ * Scratch lives in one fixed file-scope device array (about 25 MB per GPU
+ * that loads the library, held until exit): each of its six band tables
+ * holds L * RS <= 2^20 floats, RS = 32 * ceil((maxspan + 1) / 32), and
+ * L <= 16384; larger problems return MESSI_ETOOBIG.  Every call shares that
+ * array, so calls that overlap on the GPU race; serialise them.  The first
+ * call on a device resolves the array's address (set-up) and should come
+ * before any stream capture. */
+int messi_inside_noalloc(void* stream, int32_t L, const double* d_unpaired, const double* d_paired, int32_t maxspan,
+                         double B, double* d_Z);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,7 @@ MESSI_ENOMEM = -2
 MESSI_ECUDA = -3
 MESSI_ETIMEOUT = -4
 MESSI_ESTATE = -5
+MESSI_ETOOBIG = -6
 
 
 class MessiError(RuntimeError):
@@ -69,6 +70,8 @@ _SIGS = {
                                         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "messi_likelihood": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Model), ctypes.c_void_p,
                                         ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "messi_inside_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int32, ctypes.c_double, ctypes.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -265,6 +265,7 @@ const char* messi_strerror(int status)
         case MESSI_ECUDA: return "CUDA error";
         case MESSI_ETIMEOUT: return "bounded device wait timed out";
         case MESSI_ESTATE: return "object used in the wrong state";
+        case MESSI_ETOOBIG: return "problem exceeds the fixed scratch size of this entry point";
         default: return "unknown status";
     }
 }

@@ -1,0 +1,115 @@
+// noalloc.cu -- messi_inside_noalloc: the KH99 inside pass with no allocation.
+//
+// Some callers cannot call cudaMalloc on the path where they need Z: code
+// running while a stream is being captured into a CUDA graph, code inside a
+// framework that owns the device allocator (and forbids side allocations), or
+// real-time loops that must not trigger the driver's allocator.  This entry
+// point takes device pointers for its inputs and output, launches on the
+// caller's stream and keeps its band tables in one fixed file-scope device
+// array, so it calls no cudaMalloc/cudaFree and no allocating library routine.
+//
+// Limits.  Each of the six band tables holds at most kNoAllocCells floats,
+// i.e. L * RS <= 2^20 where RS = 32 * ceil((maxspan + 1) / 32), and
+// L <= kNoAllocMaxL: e.g. L = 2,048 with maxspan <= 511, or L = 1,000 with
+// maxspan <= 991.  The array (about 25 MB) is reserved on every GPU that
+// loads the library until the process exits.
+//
+// Sharing.  All calls on a device use the same array and it keeps the last
+// call's contents; every cell a call reads is written by that call first (the
+// band tables are filled before use and the span counter is cleared).  Calls
+// that overlap on the GPU (two streams, or two host threads) race on the
+// array, so callers serialise them.
+//
+// Set-up.  The first call on a device resolves the array's device address
+// with cudaGetSymbolAddress while that device is current and caches it; make
+// that first call before any stream capture begins.
+#include <mutex>
+
+#include "internal.h"
+
+namespace messi {
+
+constexpr size_t kNoAllocCells = size_t(1) << 20;
+constexpr int kNoAllocMaxL = 16384;
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocScratch {
+    float tabs[6][kNoAllocCells];           // Lrow, Lcol, Srow, Scol, Frow, pb
+    float suf[2 * (kNoAllocMaxL + 1)];      // Ssuf (+ unused outside half)
+    double vec[2 * kNoAllocMaxL + 8];       // b, cb
+    int maxspan[64];
+};
+
+// Host code must not use this name as a device address: it is a host-side
+// stand-in.  Host code reads the address with cudaGetSymbolAddress.
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+static std::mutex g_noalloc_mu;
+static NoAllocScratch* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+static int noalloc_scratch(int device, NoAllocScratch** out)
+{
+    if (device < 0 || device >= kNoAllocMaxDevices) return MESSI_EINVAL;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return MESSI_ECUDA;
+        g_noalloc_ptr[device] = static_cast<NoAllocScratch*>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return MESSI_OK;
+}
+
+}  // namespace messi
+
+using namespace messi;
+
+extern "C" int messi_inside_noalloc(void* stream, int32_t L, const double* d_unpaired, const double* d_paired,
+                                    int32_t maxspan, double B, double* d_Z)
+{
+    if (L < 1 || !d_unpaired || !d_paired || !d_Z) return MESSI_EINVAL;
+    if (L > kNoAllocMaxL) return MESSI_ETOOBIG;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return MESSI_ECUDA;
+    NoAllocScratch* s = nullptr;
+    int rc = noalloc_scratch(device, &s);
+    if (rc) return rc;
+    messi_ctx local;  // launch bookkeeping only; owns no device memory
+    local.device = device;
+    local.stream = static_cast<cudaStream_t>(stream);
+    int Wb = maxspan;
+    if (maxspan < 0) {
+        if ((rc = launch_maxspan(&local, L, d_paired, s->maxspan))) return rc;
+        int host = 0;
+        if (cudaMemcpyAsync(&host, s->maxspan, sizeof(int), cudaMemcpyDeviceToHost, local.stream) != cudaSuccess ||
+            cudaStreamSynchronize(local.stream) != cudaSuccess)
+            return MESSI_ECUDA;
+        Wb = host;
+    }
+    if (Wb > L - 1) Wb = L - 1;
+    if (Wb < 0) Wb = 0;
+    Band t;
+    t.L = L;
+    t.Wb = Wb;
+    t.RS = ((Wb + 1 + 31) / 32) * 32;
+    if ((size_t)L * (size_t)t.RS > kNoAllocCells) return MESSI_ETOOBIG;
+    t.Lrow = s->tabs[0];
+    t.Lcol = s->tabs[1];
+    t.Srow = s->tabs[2];
+    t.Scol = s->tabs[3];
+    t.Frow = s->tabs[4];
+    t.pb = s->tabs[5];
+    t.Ssuf = s->suf;
+    t.Osuf = s->suf + (L + 1);
+    t.b = s->vec;
+    t.cb = s->vec + L;
+    t.u = const_cast<double*>(d_unpaired);  // read only
+    t.Zd = d_Z;
+    t.maxspan = s->maxspan;
+    t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = nullptr;
+    if ((rc = launch_baseline(&local, t, B))) return rc;
+    if ((rc = launch_bandprep_from_dense(&local, t, d_paired, B))) return rc;
+    if ((rc = run_inside(&local, t, B))) return rc;
+    return MESSI_OK;
+}
