@@ -37,9 +37,10 @@ WORKLOAD_TEXT = {"c2": "c2: 64 seqs x 1,000 nt, max pair span 500",
                  "c4": "c4: 30 seqs x 9,000 nt, max pair span 800",
                  "c1": "c1: 16 seqs x 120 nt, all pairs"}
 BYTES_PER_UPDATE = 212  # algorithmic bytes of one node update (2 child rows + exps + indices in, 1 row out)
-# DRAM bytes per node update of prune_level_kernel from an ncu capture
-# (profiles/prune_level_kernel_c2.md); None until captured.
-TRAFFIC_BYTES_PER_UPDATE = None
+# DRAM bytes (read + write) per node update of the pruning kernel from one ncu
+# capture of the c2-shaped profiling case, weighted over its interior-level
+# launches (profiles/prune_level_kernel_c2p.md); scaled by updates per launch.
+TRAFFIC_BYTES_PER_UPDATE = 150.0
 
 
 def measured_peaks():
@@ -165,6 +166,33 @@ def cpu_inside_time(u, W, L, nthreads):
     t0 = time.perf_counter()
     co.inside(u, p, 1.0, nthreads=nthreads)
     return time.perf_counter() - t0
+
+
+def reference_gpu_rate(s, npairs):
+    """Pairs/s of the reference's kernels (src/cuda/felsenstein.cu, inside.cu,
+    compiled unmodified for sm_103a) replaying its launch sequence on the same
+    workload: pair pruning for all 45 categories + the inside pass."""
+    try:
+        from oracle import c_oracle as co
+        from oracle import model_ref as mr
+        from oracle import ref_kernels as rk
+        if not rk.available():
+            return {"unavailable": "reference cubins not built (make -C oracle ref)"}
+        ds = s.dataset
+        rp = mr.getparams(s.params15, ds.branchlengths)
+        P, pi16, logw, *_ = mr.pair_categories(rp)
+        plan = rk.index_plan(ds.children, ds.seqindex, ds.masks, s.W)
+        u, _ = mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
+        tp, ti = {}, {}
+        p = rk.pair_matrix(ds.children, ds.seqindex, ds.masks, P, pi16, logw, s.W, plan=plan, timing=tp)
+        p = co.maskgapped(p, ds.gapfrequency, 1.0)
+        Zr, _ = rk.inside(u, p, timing=ti)
+        return {"value": npairs / ((tp["ms"] + ti["ms"]) / 1e3), "unit": UNIT, "pairs_ms": tp["ms"],
+                "inside_ms": ti["ms"], "Z": Zr,
+                "kind": "reference CUDA kernels compiled unmodified for sm_103a, Julia launch sequence replayed "
+                        "(oracle/ref_kernels.py); unpaired pass on the host excluded"}
+    except Exception as exc:  # the reference path is a reported baseline only
+        return {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
 
 
 def total_pairs(L, W):
@@ -336,6 +364,11 @@ def run_ours(args):
                "sample": f"pairs of the first {rows} alignment rows ({sample} pairs, {t_pairs:.1f} s) extrapolated "
                          f"to {npairs} pairs, plus full unpaired ({t_unp:.2f} s) and inside ({t_in:.1f} s) passes"}
 
+    # ---- the reference's own CUDA kernels on the same GPU (launch sequence replayed)
+    refgpu = None
+    if rank == 0 and ws == 1 and not args.no_reference_gpu:
+        refgpu = reference_gpu_rate(s, npairs)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -355,6 +388,7 @@ def run_ours(args):
         "wall_ms_per_step": 1e3 * t_wall / args.steps,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "reference_gpu": refgpu,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -370,6 +404,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT))
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up + timed steps only (for ncu), print a short line")
