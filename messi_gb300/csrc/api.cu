@@ -2,6 +2,7 @@
 // handles and the orchestration of each call on the context's stream.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -166,7 +167,8 @@ int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool p
     const double* d_bl = (const double*)(base + o_bl);
     if (pairs) {
         void* p;
-        if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * sizeof(float), &p))) return rc;
+        // FP32 matrices followed by their TF32 hi/lo split
+        if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * 3 * sizeof(float), &p))) return rc;
         md->P16 = (float*)p;
         if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, ds->numnodes, c.C, md->P16))) return rc;
     }
@@ -288,6 +290,10 @@ int messi_ctx_create(int device, messi_ctx** out)
         return MESSI_ECUDA;
     }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    {
+        const char* k = std::getenv("MESSI_PRUNE_KERNEL");
+        if (k && std::strcmp(k, "fma") == 0) ctx->prune_kernel = 1;
+    }
     *out = ctx;
     return MESSI_OK;
 }

@@ -82,6 +82,8 @@ constexpr int kProfKernels = 4;
 
 struct messi_ctx {
     int device = 0;
+    // pair node-update kernel: 0 = tensor cores (3xTF32 mma.sync), 1 = FP32 FMA
+    int prune_kernel = 0;
     // per-kernel event timing (messi_ctx_profile)
     bool profiling = false;
     std::vector<messi::ProfRec> prof_pending;

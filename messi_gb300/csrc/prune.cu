@@ -23,8 +23,17 @@
 
 namespace messi {
 
+__device__ __forceinline__ uint32_t f32_to_tf32(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+// P[c][v][a][d] in FP32 and, for the tensor-core pruning kernel, its 3xTF32
+// split PT[c][v][0|1][a][d] = hi, lo with P ~= hi + lo (both TF32 values).
 __global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl, int numnodes,
-                                 float* __restrict__ P)
+                                 float* __restrict__ P, float* __restrict__ PT)
 {
     const int v = blockIdx.x, c = blockIdx.y, t = threadIdx.x;
     const double* e = eig + (size_t)c * kEigStride;
@@ -50,6 +59,10 @@ __global__ void build_P16_kernel(const double* __restrict__ eig, const double* _
         out = (s <= 0.0) ? 0.f : (float)s;  // absmat clamp (1e-50 rounds to 0 in FP32)
     }
     P[((size_t)c * numnodes + v) * 256 + t] = out;
+    const uint32_t hi = f32_to_tf32(out);
+    const uint32_t lo = f32_to_tf32(out - __uint_as_float(hi));
+    PT[(((size_t)c * numnodes + v) * 2 + 0) * 256 + t] = __uint_as_float(hi);
+    PT[(((size_t)c * numnodes + v) * 2 + 1) * 256 + t] = __uint_as_float(lo);
 }
 
 __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl, int numnodes,
@@ -75,7 +88,9 @@ __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* _
 
 int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, int numnodes, int C, float* d_P)
 {
-    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, numnodes, d_P);
+    // d_P holds C*numnodes*256 FP32 values followed by the hi/lo split
+    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, numnodes, d_P,
+                                                                  d_P + (size_t)C * numnodes * 256);
     LAUNCH_CHECK(ctx, "build_P16_kernel");
     return MESSI_OK;
 }
@@ -218,11 +233,245 @@ __global__ void __launch_bounds__(kTile) prune_level_kernel(
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Tensor-core node update (3xTF32 mma.sync).  A warp owns 32 unique pairs of
+// one node; for each category the two child mat-vecs are the products
+// [32 pairs x 16] x [16 x 16]^T, done as m16n8k8 TF32 MMAs with both operands
+// split hi + lo (hi*hi + hi*lo + lo*hi: FP32-level accuracy; all operands are
+// non-negative, so no cancellation).  The contraction index d is permuted so
+// that lane (g, t) owns d = 4t..4t+3: its A fragment for pair row r is one
+// 16-byte load of child row r, and its B fragment is one 16-byte load of
+// P[8nt + g][4t..4t+3].  Lane (g, t) ends with states {2t, 2t+1, 8+2t, 9+2t}
+// of pairs g, g+8, g+16, g+24; lane t keeps the scalar bookkeeping (exponent,
+// mixture) of pair g + 8t.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float comp4(const float4& v, int k)
+{
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// D[mt][nt][4] += X (rows g + 8k, k = 0..3) x P^T for one child.
+__device__ __forceinline__ void child_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bl)[2],
+                                          float (&D)[2][2][4])
+{
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++) {
+#pragma unroll
+        for (int ks = 0; ks < 2; ks++) {
+            const float av[4] = {comp4(X[2 * mt], 2 * ks), comp4(X[2 * mt + 1], 2 * ks), comp4(X[2 * mt], 2 * ks + 1),
+                                 comp4(X[2 * mt + 1], 2 * ks + 1)};
+            uint32_t ah[4], al[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                ah[i] = f32_to_tf32(av[i]);
+                al[i] = f32_to_tf32(av[i] - __uint_as_float(ah[i]));
+            }
+#pragma unroll
+            for (int nt = 0; nt < 2; nt++) {
+                const uint32_t bh0 = __float_as_uint(comp4(Bh[nt], 2 * ks)), bh1 = __float_as_uint(comp4(Bh[nt], 2 * ks + 1));
+                const uint32_t bl0 = __float_as_uint(comp4(Bl[nt], 2 * ks)), bl1 = __float_as_uint(comp4(Bl[nt], 2 * ks + 1));
+                mma_tf32(D[mt][nt], al, bh0, bh1);
+                mma_tf32(D[mt][nt], ah, bl0, bl1);
+                mma_tf32(D[mt][nt], ah, bh0, bh1);
+            }
+        }
+    }
+}
+
+template <bool ROOT>
+__global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
+    const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ PT, int numnodes,
+    int c0, int nc, const float* __restrict__ pi16, const double* __restrict__ logw, const int* __restrict__ lam,
+    double* __restrict__ mix, double* __restrict__ mixlam, int nroot, int per_lambda)
+{
+    const int2 tile = tiles[blockIdx.x];
+    const NodeDev& nd = nodes[tile.x];
+    const int n = nd.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int base = tile.y + warp * 32;  // first pair of this warp
+    if (base >= n) return;                // whole warp idle (warp-uniform)
+    // child rows of pairs g + 8k (clamped to a valid row past the end)
+    int li[4], ri[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int u = base + g + 8 * k;
+        const int uc = (u < n) ? u : (n - 1);
+        li[k] = __ldg(nd.li + uc);
+        ri[k] = __ldg(nd.ri + uc);
+    }
+    const int myu = base + g + 8 * t;  // pair whose scalars this lane keeps
+    const bool myvalid = myu < n;
+    const int myl = li[0] * (t == 0) + li[1] * (t == 1) + li[2] * (t == 2) + li[3] * (t == 3);
+    const int myr = ri[0] * (t == 0) + ri[1] * (t == 1) + ri[2] * (t == 2) + ri[3] * (t == 3);
+    const float* lf = nd.lf;
+    const float* rf = nd.rf;
+    const long long lcs = nd.lcs, rcs = nd.rcs;
+    double mm = -INFINITY;
+    float ss = 0.f;
+    double lm[kMaxLambda];
+    float ls[kMaxLambda];
+    if (ROOT) {
+#pragma unroll
+        for (int q = 0; q < kMaxLambda; q++) { lm[q] = -INFINITY; ls[q] = 0.f; }
+    }
+    for (int cc = 0; cc < nc; cc++) {
+        float4 XL[4], XR[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            XL[k] = ldg4(lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
+            XR[k] = ldg4(rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
+        }
+        int e = 0;
+        if (myvalid) e = (nd.le ? __ldg(nd.le + (size_t)cc * lcs + myl) : 0) + (nd.re ? __ldg(nd.re + (size_t)cc * rcs + myr) : 0);
+        const float* ptl = PT + ((size_t)(c0 + cc) * numnodes + nd.left) * 512;
+        const float* ptr = PT + ((size_t)(c0 + cc) * numnodes + nd.right) * 512;
+        float4 Bh[2], Bl[2];
+        float DL[2][2][4], DR[2][2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) { DL[mt][nt][i] = 0.f; DR[mt][nt][i] = 0.f; }
+#pragma unroll
+        for (int nt = 0; nt < 2; nt++) {
+            Bh[nt] = ldg4(ptl + (8 * nt + g) * 16 + 4 * t);
+            Bl[nt] = ldg4(ptl + 256 + (8 * nt + g) * 16 + 4 * t);
+        }
+        child_mma(XL, Bh, Bl, DL);
+#pragma unroll
+        for (int nt = 0; nt < 2; nt++) {
+            Bh[nt] = ldg4(ptr + (8 * nt + g) * 16 + 4 * t);
+            Bl[nt] = ldg4(ptr + 256 + (8 * nt + g) * 16 + 4 * t);
+        }
+        child_mma(XR, Bh, Bl, DR);
+        // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}
+        float V[4][4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int mt = k >> 1, h = k & 1;
+            V[k][0] = DL[mt][0][2 * h] * DR[mt][0][2 * h];
+            V[k][1] = DL[mt][0][2 * h + 1] * DR[mt][0][2 * h + 1];
+            V[k][2] = DL[mt][1][2 * h] * DR[mt][1][2 * h];
+            V[k][3] = DL[mt][1][2 * h + 1] * DR[mt][1][2 * h + 1];
+        }
+        if (ROOT) {
+            const float* pc = pi16 + (size_t)(c0 + cc) * 16;
+            const float p0 = __ldg(pc + 2 * t), p1 = __ldg(pc + 2 * t + 1), p2 = __ldg(pc + 8 + 2 * t),
+                        p3 = __ldg(pc + 9 + 2 * t);
+            float dots[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                float dk = p0 * V[k][0] + p1 * V[k][1] + p2 * V[k][2] + p3 * V[k][3];
+                dk += __shfl_xor_sync(0xffffffffu, dk, 1);
+                dk += __shfl_xor_sync(0xffffffffu, dk, 2);
+                dots[k] = dk;
+            }
+            const float dot = dots[0] * (t == 0) + dots[1] * (t == 1) + dots[2] * (t == 2) + dots[3] * (t == 3);
+            const double ll = (dot > 0.f) ? (double)logf(dot) + (double)e * 0.69314718055994530942 : -INFINITY;
+            const double tt = __ldg(logw + c0 + cc) + ll;
+            if (tt > mm) {
+                ss = ss * __expf((float)(mm - tt)) + 1.f;
+                mm = tt;
+            } else if (tt != -INFINITY) {
+                ss += __expf((float)(tt - mm));
+            }
+            if (per_lambda) {
+                const int kq = __ldg(lam + c0 + cc);
+#pragma unroll
+                for (int q = 0; q < kMaxLambda; q++)
+                    if (q == kq) {
+                        if (tt > lm[q]) {
+                            ls[q] = ls[q] * __expf((float)(lm[q] - tt)) + 1.f;
+                            lm[q] = tt;
+                        } else if (tt != -INFINITY) {
+                            ls[q] += __expf((float)(tt - lm[q]));
+                        }
+                    }
+            }
+        } else {
+            int exk[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                float m = fmaxf(fmaxf(V[k][0], V[k][1]), fmaxf(V[k][2], V[k][3]));
+                m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+                m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+                int ex = 0;
+                if (m > 0.f) frexpf(m, &ex);
+                exk[k] = ex;
+                const float sc = ldexpf(1.f, -ex);
+                const int u = base + g + 8 * k;
+                if (u < n) {
+                    float* o = nd.of + ((size_t)cc * nd.ocs + u) * 16;
+                    *reinterpret_cast<float2*>(o + 2 * t) = make_float2(V[k][0] * sc, V[k][1] * sc);
+                    *reinterpret_cast<float2*>(o + 8 + 2 * t) = make_float2(V[k][2] * sc, V[k][3] * sc);
+                }
+            }
+            if (myvalid) {
+                const int ex = exk[0] * (t == 0) + exk[1] * (t == 1) + exk[2] * (t == 2) + exk[3] * (t == 3);
+                nd.oe[(size_t)cc * nd.ocs + myu] = e + ex;
+            }
+        }
+    }
+    if (ROOT && myvalid) {
+        const double res = (mm == -INFINITY) ? -INFINITY : mm + log((double)ss);
+        mix[myu] = (c0 == 0) ? res : lse_d(mix[myu], res);
+        if (per_lambda) {
+#pragma unroll
+            for (int q = 0; q < kMaxLambda; q++) {
+                const double rq = (lm[q] == -INFINITY) ? -INFINITY : lm[q] + log((double)ls[q]);
+                double* dst = mixlam + (size_t)q * nroot + myu;
+                *dst = (c0 == 0) ? rq : lse_d(*dst, rq);
+            }
+        }
+    }
+}
+
 int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
               const int* d_lam, int C, int nlam, bool per_lambda)
 {
     (void)nlam;
     const int chunk = ds->chunk;
+    const float* d_PT = d_P + (size_t)C * ds->numnodes * 256;
+    if (ctx->prune_kernel == 0) {
+        for (int c0 = 0; c0 < C; c0 += chunk) {
+            const int nc = std::min(chunk, C - c0);
+            for (int lv = 1; lv <= ds->H; lv++) {
+                const int nt = ds->tile_cnt[lv];
+                if (nt == 0) continue;
+                const int2* tiles = ds->d_tiles + ds->tile_off[lv];
+                if (ctx->profiling) {
+                    double units = 0.0;
+                    for (int v : ds->level_nodes[lv]) units += (double)ds->nunique[v] * nc;
+                    prof_begin(ctx, 0, units);
+                }
+                if (lv < ds->H) {
+                    prune_mma_kernel<false><<<nt, kTile, 0, ctx->stream>>>(
+                        ds->d_nodes, tiles, d_PT, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix,
+                        ds->d_mixlam, (int)ds->nroot, per_lambda ? 1 : 0);
+                    LAUNCH_CHECK(ctx, "prune_mma_kernel");
+                } else {
+                    prune_mma_kernel<true><<<nt, kTile, 0, ctx->stream>>>(
+                        ds->d_nodes, tiles, d_PT, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix,
+                        ds->d_mixlam, (int)ds->nroot, per_lambda ? 1 : 0);
+                    LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
+                }
+                prof_end(ctx);
+            }
+        }
+        return MESSI_OK;
+    }
     const size_t smem_max = (size_t)chunk * (128 * sizeof(float4) + 16 * sizeof(float));
     if (smem_max > 227 * 1024) return fail(ctx, MESSI_EINVAL, "category pass does not fit in shared memory");
     if (smem_max > 48 * 1024) {
