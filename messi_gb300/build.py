@@ -76,6 +76,12 @@ def build(verbose=False, force=False):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    # a shared library links with unresolved symbols; loading it resolves them
+    chk = subprocess.run([sys.executable, "-c", f"import ctypes; ctypes.CDLL({tmp!r})"], capture_output=True,
+                         text=True)
+    if chk.returncode != 0:
+        os.remove(tmp)
+        raise RuntimeError(f"built library does not load:\n{chk.stderr}")
     os.replace(tmp, LIB)
     return LIB
 

@@ -200,6 +200,8 @@ int finish(messi_ctx* ctx)
     if (!ctx->prof_pending.empty()) prof_collect(ctx);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel execution");
+    if (ctx->status_host && *ctx->status_host != 0u)
+        return fail(ctx, MESSI_ETIMEOUT, "wavefront grid barrier gave up waiting (bounded spin)");
     return MESSI_OK;
 }
 
@@ -208,6 +210,7 @@ int begin(messi_ctx* ctx)
     if (!ctx) return MESSI_EINVAL;
     ctx->launches = 0;
     ctx->last_error.clear();
+    if (ctx->status_host) *ctx->status_host = 0u;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
     return MESSI_OK;
@@ -290,6 +293,12 @@ int messi_ctx_create(int device, messi_ctx** out)
         return MESSI_ECUDA;
     }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMallocHost((void**)&ctx->status_host, 64) != cudaSuccess) {
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return MESSI_ENOMEM;
+    }
+    *ctx->status_host = 0u;
     {
         const char* k = std::getenv("MESSI_PRUNE_KERNEL");
         if (k && std::strcmp(k, "fma") == 0) ctx->prune_kernel = 1;
@@ -332,6 +341,7 @@ int messi_ctx_destroy(messi_ctx* ctx)
     for (auto& b : ctx->scratch)
         if (b.p) cudaFree(b.p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->status_host) cudaFreeHost(ctx->status_host);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MESSI_OK;

@@ -62,6 +62,7 @@ struct Band {
     float *PP, *SL, *nrm;
     double *b, *cb, *u, *Zd;
     int* maxspan;
+    unsigned int* sync;  // grid barrier of the wavefront kernels: count, generation, error flag, spare
 };
 
 // Rule log-probabilities times B (index 0..6 = r1..r7).
@@ -99,6 +100,7 @@ struct messi_ctx {
     messi::DevBuf scratch[24];
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    unsigned int* status_host = nullptr;  // pinned word: wavefront barrier status of the last call
 };
 
 struct messi_dataset {
@@ -187,5 +189,7 @@ int launch_dense_outside(messi_ctx* ctx, const Band& t, double* d_out);
 int launch_band_from_dense_inside(messi_ctx* ctx, const Band& t, const double* d_in);
 int launch_band_from_dense_outside(messi_ctx* ctx, const Band& t, const double* d_out);
 int launch_finish_Z(messi_ctx* ctx, const Band& t);
+// Queue a copy of the wavefront barrier status into ctx->status_host.
+int queue_status_readback(messi_ctx* ctx, const Band& t);
 
 }  // namespace messi

@@ -16,7 +16,9 @@
 //
 // Sharing.  All calls on a device use the same array and it keeps the last
 // call's contents; every cell a call reads is written by that call first (the
-// band tables are filled before use and the span counter is cleared).  Calls
+// band tables are filled before use, the span counter and the wavefront
+// barrier are cleared).  If the wavefront's bounded barrier wait gives up,
+// *d_Z is NaN.  Calls
 // that overlap on the GPU (two streams, or two host threads) race on the
 // array, so callers serialise them.
 //
@@ -107,6 +109,7 @@ extern "C" int messi_inside_noalloc(void* stream, int32_t L, const double* d_unp
     t.u = const_cast<double*>(d_unpaired);  // read only
     t.Zd = d_Z;
     t.maxspan = s->maxspan;
+    t.sync = reinterpret_cast<unsigned int*>(s->maxspan + 16);
     t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = nullptr;
     if ((rc = launch_baseline(&local, t, B))) return rc;
     if ((rc = launch_bandprep_from_dense(&local, t, d_paired, B))) return rc;

@@ -25,11 +25,15 @@
 // so the split sum of cell (i, j) reads row i of L and column j of S with
 // unit stride.  Outside tables mirror them (OSrow/OScol/OFrow/OFcol/OLrow/Osuf).
 //
-// Schedule.  One launch per span diagonal; a cell is reduced by a group of G
-// lanes (G grows with the number of split points) with shuffle log-sum-exp.
-// The suffix recurrences run in one CTA in blocks of 32 cells: the terms that
-// reach outside the block are summed by 32 warps in parallel, the in-block
-// triangle by one warp.
+// Schedule.  One persistent cooperative launch walks the band diagonals (a
+// wavefront): all cells of a span are independent, so each diagonal is spread
+// over the whole grid and a grid barrier separates diagonals.  The barrier
+// spins with a bounded iteration count; on timeout it raises an error flag,
+// every CTA leaves, Z becomes NaN and the host returns MESSI_ETIMEOUT.  A
+// cell's split sum is reduced by a group of G lanes (G grows with the number
+// of split points) with shuffle log-sum-exp.  The suffix recurrences run in
+// one CTA in blocks of 32 cells: the terms that reach outside the block are
+// summed by 32 warps in parallel, the in-block triangle by one warp.
 #include <algorithm>
 #include <cmath>
 
@@ -106,6 +110,7 @@ int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
     t->u = t->cb + (L + 1);
     t->Zd = t->u + L;
     t->maxspan = (int*)(t->Zd + 2);
+    t->sync = (unsigned int*)(t->Zd + 4);
     if (outside) {
         float** out_tabs[6] = {&t->OSrow, &t->OScol, &t->OFrow, &t->OFcol, &t->OLrow, &t->PP};
         for (int k = 0; k < 6; k++) {
@@ -244,52 +249,6 @@ int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_de
 // ---------------------------------------------------------------------------
 // inside
 // ---------------------------------------------------------------------------
-__global__ void inside_init_kernel(Band t, Rules R, double B)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= t.L) return;
-    const double ui = t.u[i];
-    const float S = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[1] - t.b[i]);
-    const float Lv = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[5] - t.b[i]);
-    const size_t o = (size_t)i * t.RS;
-    t.Srow[o] = S;
-    t.Scol[o] = S;
-    t.Lrow[o] = Lv;
-    t.Lcol[o] = Lv;
-    t.Frow[o] = -INFINITY;
-    if (i == t.L - 1) t.Ssuf[i] = S;
-}
-
-template <int G>
-__global__ void __launch_bounds__(256) inside_diag_kernel(Band t, Rules R, int d)
-{
-    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-    const int lane = threadIdx.x & (G - 1);
-    const int i = gid;
-    const bool valid = i < t.L - d;
-    float m = -INFINITY, s = 0.f;
-    if (valid) {
-        const int j = i + d;
-        const float* lrow = t.Lrow + (size_t)i * t.RS;
-        const float* scol = t.Scol + (size_t)j * t.RS + (d - 1);
-        for (int k = lane; k < d; k += G) lse_add(m, s, lrow[k] + scol[-k]);
-    }
-    group_reduce<G>(m, s);
-    if (!valid || lane != 0) return;
-    const int j = i + d;
-    const float tmp = lse_val(m, s);
-    const float v = (d >= 2) ? t.pb[(size_t)i * t.RS + d] + t.Frow[(size_t)(i + 1) * t.RS + (d - 2)] : -INFINITY;
-    const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
-    const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
-    const float Lv = R.r[6] + v;
-    t.Lrow[(size_t)i * t.RS + d] = Lv;
-    t.Lcol[(size_t)j * t.RS + d] = Lv;
-    t.Srow[(size_t)i * t.RS + d] = S;
-    t.Scol[(size_t)j * t.RS + d] = S;
-    t.Frow[(size_t)i * t.RS + d] = F;
-    if (j == t.L - 1) t.Ssuf[i] = S;
-}
-
 // Ssuf[i] for spans beyond the band (i < T = L-1-Wb), descending i:
 // Ssuf[i] = r1 + LSE_{k=0..Wb} (Lrow[i][k] + Ssuf[i+k+1]).
 __global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R)
@@ -329,45 +288,257 @@ __global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R)
 
 __global__ void finish_Z_kernel(Band t)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) t.Zd[0] = (double)t.Ssuf[0] + t.cb[t.L];
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        t.Zd[0] = (t.sync[2] != 0u) ? (double)NAN : (double)t.Ssuf[0] + t.cb[t.L];
 }
 
 int launch_finish_Z(messi_ctx* ctx, const Band& t)
 {
     finish_Z_kernel<<<1, 32, 0, ctx->stream>>>(t);
     LAUNCH_CHECK(ctx, "finish_Z_kernel");
+    return queue_status_readback(ctx, t);
+}
+
+
+// ---------------------------------------------------------------------------
+// grid barrier with a bounded wait (wavefront kernels)
+// ---------------------------------------------------------------------------
+constexpr unsigned int kSpinLimit = 1u << 22;  // x ~64-200 ns per spin: well under a second
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// sync[0] = arrivals, sync[1] = generation, sync[2] = error flag.  Returns
+// false (in every thread of the CTA) once any CTA has given up waiting.
+// Cells written by other CTAs before the barrier are read with __ldcg (L2,
+// coherent across SMs): the per-SM L1 may hold stale lines of those tables.
+__device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
+{
+    __shared__ int s_ok;
+    __threadfence();  // every thread publishes its cells device-wide
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned int target = gen + 1;
+        __threadfence();
+        if (atomicAdd(&sync[0], 1u) == gridDim.x - 1) {
+            atomicExch(&sync[0], 0u);
+            __threadfence();
+            atomicExch(&sync[1], target);
+        } else {
+            unsigned int spins = 0;
+            while (ld_acquire_u32(&sync[1]) != target) {
+                if (ld_acquire_u32(&sync[2]) != 0u || ++spins > kSpinLimit) {
+                    atomicExch(&sync[2], 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        gen = target;
+        s_ok = ok && (ld_acquire_u32(&sync[2]) == 0u);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ int group_width(int nterms)
+{
+    return nterms <= 8 ? 1 : (nterms <= 32 ? 4 : (nterms <= 96 ? 8 : (nterms <= 256 ? 16 : 32)));
+}
+
+__device__ __forceinline__ void group_reduce_rt(float& m, float& s, int G)
+{
+    for (int off = G >> 1; off > 0; off >>= 1) {
+        const float m2 = __shfl_xor_sync(0xffffffffu, m, off);
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+        lse_merge(m, s, m2, s2);
+    }
+}
+
+// All band diagonals of the inside pass (span 0 initialisation included).
+__global__ void __launch_bounds__(256) inside_wave_kernel(Band t, Rules R, double B)
+{
+    unsigned int gen = 0;
+    const int L = t.L, RS = t.RS;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        const double ui = t.u[i];
+        const float S = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[1] - t.b[i]);
+        const float Lv = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[5] - t.b[i]);
+        const size_t o = (size_t)i * RS;
+        t.Srow[o] = S;
+        t.Scol[o] = S;
+        t.Lrow[o] = Lv;
+        t.Lcol[o] = Lv;
+        t.Frow[o] = -INFINITY;
+        if (i == L - 1) t.Ssuf[i] = S;
+    }
+    if (!grid_sync(t.sync, gen)) return;
+    for (int d = 1; d <= t.Wb; d++) {
+        const int G = group_width(d);
+        const int gpb = blockDim.x / G;
+        const int total = gridDim.x * gpb;
+        const int lane = threadIdx.x & (G - 1);
+        const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
+        const int ncell = L - d;
+        for (int base = 0; base < ncell; base += total) {
+            const int i = base + gid0;
+            const bool valid = i < ncell;
+            float m = -INFINITY, s = 0.f;
+            if (valid) {
+                const float* lrow = t.Lrow + (size_t)i * RS;
+                const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
+                for (int k = lane; k < d; k += G) lse_add(m, s, __ldcg(lrow + k) + __ldcg(scol - k));
+            }
+            group_reduce_rt(m, s, G);
+            if (valid && lane == 0) {
+                const int j = i + d;
+                const float tmp = lse_val(m, s);
+                const float v = (d >= 2) ? t.pb[(size_t)i * RS + d] + __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2)) : -INFINITY;
+                const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
+                const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
+                const float Lv = R.r[6] + v;
+                t.Lrow[(size_t)i * RS + d] = Lv;
+                t.Lcol[(size_t)j * RS + d] = Lv;
+                t.Srow[(size_t)i * RS + d] = S;
+                t.Scol[(size_t)j * RS + d] = S;
+                t.Frow[(size_t)i * RS + d] = F;
+                if (j == L - 1) t.Ssuf[i] = S;
+            }
+        }
+        if (!grid_sync(t.sync, gen)) return;
+    }
+}
+
+// All band diagonals of the outside pass, descending spans.
+__global__ void __launch_bounds__(256) outside_wave_kernel(Band t, Rules R)
+{
+    unsigned int gen = 0;
+    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    for (int d = Wb; d >= 0; d--) {
+        const int G = group_width(2 * (Wb - d) + 2);
+        const int gpb = blockDim.x / G;
+        const int total = gridDim.x * gpb;
+        const int lane = threadIdx.x & (G - 1);
+        const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
+        const int ncell = L - d;
+        for (int base = 0; base < ncell; base += total) {
+            const int i = base + gid0;
+            const bool valid = i < ncell;
+            const int j = i + d;
+            float mL = -INFINITY, sL = 0.f, mS = -INFINITY, sS = 0.f;
+            if (valid) {
+                const int nL = min(i + Wb, L - 1) - j;
+                const float* osr = t.OSrow + (size_t)i * RS + d + 1;
+                const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
+                if (j + 1 <= L - 1) {
+                    const float* srw = t.Srow + (size_t)(j + 1) * RS;
+                    for (int q = lane; q < nL; q += G) {
+                        const float sib = srw[q];
+                        lse_add(mL, sL, R.r[0] + __ldcg(osr + q) + sib);
+                        lse_add(mL, sL, R.r[4] + __ldcg(ofr + q) + sib);
+                    }
+                    if (lane == 0 && L - 1 > i + Wb) lse_add(mL, sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
+                }
+                if (i >= 1) {
+                    const int ip0 = max(0, j - Wb);
+                    const int nS = i - ip0;
+                    const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
+                    const float* osc = t.OScol + (size_t)j * RS + d + 1;
+                    const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
+                    for (int q = lane; q < nS; q += G) {
+                        const float lft = lcol[q];
+                        lse_add(mS, sS, R.r[0] + __ldcg(osc + q) + lft);
+                        lse_add(mS, sS, R.r[4] + __ldcg(ofc + q) + lft);
+                    }
+                    if (j == L - 1) {
+                        const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
+                        for (int ip = a + lane; ip <= bnd; ip += G) lse_add(mS, sS, R.r[0] + __ldcg(t.Osuf + ip) + lcol[i - 1 - ip]);
+                    }
+                }
+            }
+            group_reduce_rt(mL, sL, G);
+            group_reduce_rt(mS, sS, G);
+            if (valid && lane == 0) {
+                const float oL = lse_val(mL, sL);
+                float oS = lse_val(mS, sS);
+                if (i == 0 && j == L - 1) oS = 0.f;
+                float oF = -INFINITY;
+                if (i >= 1 && j <= L - 2 && d + 2 <= Wb) {
+                    const size_t pr = (size_t)(i - 1) * RS + d + 2;
+                    const float pp = t.pb[pr];
+                    if (pp != -INFINITY) {
+                        float m = -INFINITY, s = 0.f;
+                        lse_add(m, s, R.r[2] + pp + __ldcg(t.OSrow + pr));
+                        lse_add(m, s, R.r[3] + pp + __ldcg(t.OFrow + pr));
+                        lse_add(m, s, R.r[6] + pp + __ldcg(t.OLrow + pr));
+                        oF = lse_val(m, s);
+                    }
+                }
+                t.OSrow[(size_t)i * RS + d] = oS;
+                t.OScol[(size_t)j * RS + d] = oS;
+                t.OFrow[(size_t)i * RS + d] = oF;
+                t.OFcol[(size_t)j * RS + d] = oF;
+                t.OLrow[(size_t)i * RS + d] = oL;
+                if (j == L - 1) t.Osuf[i] = oS;
+            }
+        }
+        if (!grid_sync(t.sync, gen)) return;
+    }
+}
+
+static int wave_grid(messi_ctx* ctx, const void* kernel, int L)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int sms = ctx->num_sms;
+    if (sms <= 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        ctx->num_sms = sms;
+    }
+    // one CTA per SM keeps the barrier cheap; more only when a diagonal needs it
+    const int useful = (int)std::min<long long>((long long)L * 32 / 256 + 1, (long long)per_sm * sms);
+    return std::max(1, std::min(useful, sms));
+}
+
+static int launch_wave(messi_ctx* ctx, const void* kernel, int grid, void** args, const Band& t, const char* what)
+{
+    cudaError_t e = cudaMemsetAsync(t.sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
+    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(256), args, 0, ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, what);
     return MESSI_OK;
 }
 
-template <int G>
-static int launch_inside_diag(messi_ctx* ctx, const Band& t, const Rules& R, int d)
+int queue_status_readback(messi_ctx* ctx, const Band& t)
 {
-    const long long threads = (long long)(t.L - d) * G;
-    inside_diag_kernel<G><<<(unsigned)((threads + 255) / 256), 256, 0, ctx->stream>>>(t, R, d);
-    LAUNCH_CHECK(ctx, "inside_diag_kernel");
-    return MESSI_OK;
-}
-
-static int inside_diag(messi_ctx* ctx, const Band& t, const Rules& R, int d, int nterms)
-{
-    if (nterms <= 8) return launch_inside_diag<1>(ctx, t, R, d);
-    if (nterms <= 32) return launch_inside_diag<4>(ctx, t, R, d);
-    if (nterms <= 96) return launch_inside_diag<8>(ctx, t, R, d);
-    if (nterms <= 256) return launch_inside_diag<16>(ctx, t, R, d);
-    return launch_inside_diag<32>(ctx, t, R, d);
+    if (!ctx->status_host) return MESSI_OK;
+    cudaError_t e = cudaMemcpyAsync(ctx->status_host, t.sync + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                    ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "status readback");
 }
 
 int run_inside(messi_ctx* ctx, const Band& t, double B)
 {
-    const Rules R = make_rules(B);
-    inside_init_kernel<<<(t.L + 255) / 256, 256, 0, ctx->stream>>>(t, R, B);
-    LAUNCH_CHECK(ctx, "inside_init_kernel");
-    int rc;
-    for (int d = 1; d <= t.Wb; d++) {
-        prof_begin(ctx, 1, (double)(t.L - d));
-        if ((rc = inside_diag(ctx, t, R, d, d))) return rc;
-        prof_end(ctx);
-    }
+    Rules R = make_rules(B);
+    Band tt = t;
+    double Bv = B;
+    void* args[] = {&tt, &R, &Bv};
+    const int grid = wave_grid(ctx, (const void*)inside_wave_kernel, t.L);
+    prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
+    int rc = launch_wave(ctx, (const void*)inside_wave_kernel, grid, args, t, "inside_wave_kernel");
+    if (rc) return rc;
+    prof_end(ctx);
     if (t.L - 1 > t.Wb) {
         prof_begin(ctx, 2, (double)(t.L - 1 - t.Wb));
         inside_suffix_kernel<<<1, 1024, 0, ctx->stream>>>(t, R);
@@ -420,103 +591,21 @@ __global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
     }
 }
 
-template <int G>
-__global__ void __launch_bounds__(256) outside_diag_kernel(Band t, Rules R, int d)
-{
-    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-    const int lane = threadIdx.x & (G - 1);
-    const int i = gid;
-    const int L = t.L, Wb = t.Wb, RS = t.RS;
-    const bool valid = i < L - d;
-    const int j = i + d;
-    float mL = -INFINITY, sL = 0.f, mS = -INFINITY, sS = 0.f;
-    if (valid) {
-        // L(i,j) as left child of S->LS / F->LS at parents (i, jp), jp in (j, min(i+Wb, L-1)]
-        const int nL = min(i + Wb, L - 1) - j;
-        const float* osr = t.OSrow + (size_t)i * RS + d + 1;
-        const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
-        if (j + 1 <= L - 1) {
-            const float* srw = t.Srow + (size_t)(j + 1) * RS;
-            for (int q = lane; q < nL; q += G) {
-                const float sib = srw[q];
-                lse_add(mL, sL, R.r[0] + osr[q] + sib);
-                lse_add(mL, sL, R.r[4] + ofr[q] + sib);
-            }
-            if (lane == 0 && L - 1 > i + Wb) lse_add(mL, sL, R.r[0] + t.Osuf[i] + t.Ssuf[j + 1]);
-        }
-        // S(i,j) as right child at parents (ip, j), ip in [max(0, j-Wb), i)
-        if (i >= 1) {
-            const int ip0 = max(0, j - Wb);
-            const int nS = i - ip0;
-            const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
-            const float* osc = t.OScol + (size_t)j * RS + d + 1;
-            const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
-            for (int q = lane; q < nS; q += G) {
-                const float lft = lcol[q];
-                lse_add(mS, sS, R.r[0] + osc[q] + lft);
-                lse_add(mS, sS, R.r[4] + ofc[q] + lft);
-            }
-            if (j == L - 1) {
-                const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
-                for (int ip = a + lane; ip <= bnd; ip += G) lse_add(mS, sS, R.r[0] + t.Osuf[ip] + lcol[i - 1 - ip]);
-            }
-        }
-    }
-    group_reduce<G>(mL, sL);
-    group_reduce<G>(mS, sS);
-    if (!valid || lane != 0) return;
-    const float oL = lse_val(mL, sL);
-    float oS = lse_val(mS, sS);
-    if (i == 0 && j == L - 1) oS = 0.f;
-    float oF = -INFINITY;
-    if (i >= 1 && j <= L - 2 && d + 2 <= Wb) {
-        const size_t pr = (size_t)(i - 1) * RS + d + 2;
-        const float pp = t.pb[pr];
-        if (pp != -INFINITY) {
-            float m = -INFINITY, s = 0.f;
-            lse_add(m, s, R.r[2] + pp + t.OSrow[pr]);
-            lse_add(m, s, R.r[3] + pp + t.OFrow[pr]);
-            lse_add(m, s, R.r[6] + pp + t.OLrow[pr]);
-            oF = lse_val(m, s);
-        }
-    }
-    t.OSrow[(size_t)i * RS + d] = oS;
-    t.OScol[(size_t)j * RS + d] = oS;
-    t.OFrow[(size_t)i * RS + d] = oF;
-    t.OFcol[(size_t)j * RS + d] = oF;
-    t.OLrow[(size_t)i * RS + d] = oL;
-    if (j == L - 1) t.Osuf[i] = oS;
-}
-
-template <int G>
-static int launch_outside_diag(messi_ctx* ctx, const Band& t, const Rules& R, int d)
-{
-    const long long threads = (long long)(t.L - d) * G;
-    outside_diag_kernel<G><<<(unsigned)((threads + 255) / 256), 256, 0, ctx->stream>>>(t, R, d);
-    LAUNCH_CHECK(ctx, "outside_diag_kernel");
-    return MESSI_OK;
-}
-
 int run_outside(messi_ctx* ctx, const Band& t, double B)
 {
-    const Rules R = make_rules(B);
-    int rc;
+    Rules R = make_rules(B);
     if (t.L - 1 > t.Wb) {
         outside_suffix_kernel<<<1, 1024, 0, ctx->stream>>>(t, R);
         LAUNCH_CHECK(ctx, "outside_suffix_kernel");
     }
-    for (int d = t.Wb; d >= 0; d--) {
-        const int nterms = 2 * (t.Wb - d) + 2;
-        prof_begin(ctx, 3, (double)(t.L - d));
-        if (nterms <= 8) rc = launch_outside_diag<1>(ctx, t, R, d);
-        else if (nterms <= 32) rc = launch_outside_diag<4>(ctx, t, R, d);
-        else if (nterms <= 96) rc = launch_outside_diag<8>(ctx, t, R, d);
-        else if (nterms <= 256) rc = launch_outside_diag<16>(ctx, t, R, d);
-        else rc = launch_outside_diag<32>(ctx, t, R, d);
-        if (rc) return rc;
-        prof_end(ctx);
-    }
-    return MESSI_OK;
+    Band tt = t;
+    void* args[] = {&tt, &R};
+    const int grid = wave_grid(ctx, (const void*)outside_wave_kernel, t.L);
+    prof_begin(ctx, 3, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
+    int rc = launch_wave(ctx, (const void*)outside_wave_kernel, grid, args, t, "outside_wave_kernel");
+    if (rc) return rc;
+    prof_end(ctx);
+    return queue_status_readback(ctx, t);
 }
 
 // ---------------------------------------------------------------------------
