@@ -288,12 +288,55 @@ __device__ __forceinline__ void child_mma(const float4 (&X)[4], const float4 (&B
     }
 }
 
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Exact power-of-two rescale of a row max m > 0: m * 2^-ex in [0.5, 1).
+__device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
+{
+    const unsigned bits = __float_as_uint(m);
+    const int E = (int)((bits >> 23) & 0xffu);
+    if (E >= 1 && E <= 252) {  // normal, and 2^-ex representable
+        ex = E - 126;
+        sc = __uint_as_float((unsigned)(127 - ex) << 23);
+    } else if (m > 0.f) {
+        frexpf(m, &ex);
+        sc = ldexpf(1.f, -ex);
+    } else {
+        ex = 0;
+        sc = 1.f;
+    }
+}
+
+constexpr int kStages = 3;  // categories in flight per warp (cp.async pipeline)
+
+// Per-warp staging of one category: 8 float4 per lane (child rows) + 2 exponents.
+struct WarpStage {
+    float4 x[8][32];
+    int e[2][32];
+};
+
 template <bool ROOT>
 __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ PT, int numnodes,
     int c0, int nc, const float* __restrict__ pi16, const double* __restrict__ logw, const int* __restrict__ lam,
     double* __restrict__ mix, double* __restrict__ mixlam, int nroot, int per_lambda)
 {
+    extern __shared__ float4 smem_raw[];
     const int2 tile = tiles[blockIdx.x];
     const NodeDev& nd = nodes[tile.x];
     const int n = nd.n;
@@ -301,6 +344,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     const int g = lane >> 2, t = lane & 3;
     const int base = tile.y + warp * 32;  // first pair of this warp
     if (base >= n) return;                // whole warp idle (warp-uniform)
+    WarpStage* stage = reinterpret_cast<WarpStage*>(smem_raw) + (size_t)warp * kStages;
     // child rows of pairs g + 8k (clamped to a valid row past the end)
     int li[4], ri[4];
 #pragma unroll
@@ -316,7 +360,25 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     const int myr = ri[0] * (t == 0) + ri[1] * (t == 1) + ri[2] * (t == 2) + ri[3] * (t == 3);
     const float* lf = nd.lf;
     const float* rf = nd.rf;
+    const int* le = nd.le;
+    const int* re = nd.re;
     const long long lcs = nd.lcs, rcs = nd.rcs;
+    // issue the copies of category cc into its stage (each lane copies what it later reads)
+    auto issue = [&](int cc) {
+        WarpStage& st = stage[cc % kStages];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            cp_async16(&st.x[k][lane], lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
+            cp_async16(&st.x[4 + k][lane], rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
+        }
+        if (le) cp_async4(&st.e[0][lane], le + (size_t)cc * lcs + myl);
+        if (re) cp_async4(&st.e[1][lane], re + (size_t)cc * rcs + myr);
+    };
+#pragma unroll
+    for (int s0 = 0; s0 < kStages - 1; s0++) {
+        if (s0 < nc) issue(s0);
+        cp_async_commit();
+    }
     double mm = -INFINITY;
     float ss = 0.f;
     double lm[kMaxLambda];
@@ -326,14 +388,17 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
         for (int q = 0; q < kMaxLambda; q++) { lm[q] = -INFINITY; ls[q] = 0.f; }
     }
     for (int cc = 0; cc < nc; cc++) {
+        if (cc + kStages - 1 < nc) issue(cc + kStages - 1);
+        cp_async_commit();
+        cp_async_wait<kStages - 1>();
+        const WarpStage& st = stage[cc % kStages];
         float4 XL[4], XR[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            XL[k] = ldg4(lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
-            XR[k] = ldg4(rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
+            XL[k] = st.x[k][lane];
+            XR[k] = st.x[4 + k][lane];
         }
-        int e = 0;
-        if (myvalid) e = (nd.le ? __ldg(nd.le + (size_t)cc * lcs + myl) : 0) + (nd.re ? __ldg(nd.re + (size_t)cc * rcs + myr) : 0);
+        const int e = (le ? st.e[0][lane] : 0) + (re ? st.e[1][lane] : 0);
         const float* ptl = PT + ((size_t)(c0 + cc) * numnodes + nd.left) * 512;
         const float* ptr = PT + ((size_t)(c0 + cc) * numnodes + nd.right) * 512;
         float4 Bh[2], Bl[2];
@@ -407,10 +472,10 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
                 float m = fmaxf(fmaxf(V[k][0], V[k][1]), fmaxf(V[k][2], V[k][3]));
                 m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
                 m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
-                int ex = 0;
-                if (m > 0.f) frexpf(m, &ex);
+                int ex;
+                float sc;
+                pow2_scale(m, ex, sc);
                 exk[k] = ex;
-                const float sc = ldexpf(1.f, -ex);
                 const int u = base + g + 8 * k;
                 if (u < n) {
                     float* o = nd.of + ((size_t)cc * nd.ocs + u) * 16;
@@ -424,6 +489,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
             }
         }
     }
+    cp_async_wait<0>();
     if (ROOT && myvalid) {
         const double res = (mm == -INFINITY) ? -INFINITY : mm + log((double)ss);
         mix[myu] = (c0 == 0) ? res : lse_d(mix[myu], res);
@@ -445,6 +511,9 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
     const int chunk = ds->chunk;
     const float* d_PT = d_P + (size_t)C * ds->numnodes * 256;
     if (ctx->prune_kernel == 0) {
+        const size_t smem = (size_t)(kTile / 32) * kStages * sizeof(WarpStage);
+        cudaFuncSetAttribute(prune_mma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(prune_mma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         for (int c0 = 0; c0 < C; c0 += chunk) {
             const int nc = std::min(chunk, C - c0);
             for (int lv = 1; lv <= ds->H; lv++) {
@@ -457,12 +526,12 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
                     prof_begin(ctx, 0, units);
                 }
                 if (lv < ds->H) {
-                    prune_mma_kernel<false><<<nt, kTile, 0, ctx->stream>>>(
+                    prune_mma_kernel<false><<<nt, kTile, smem, ctx->stream>>>(
                         ds->d_nodes, tiles, d_PT, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix,
                         ds->d_mixlam, (int)ds->nroot, per_lambda ? 1 : 0);
                     LAUNCH_CHECK(ctx, "prune_mma_kernel");
                 } else {
-                    prune_mma_kernel<true><<<nt, kTile, 0, ctx->stream>>>(
+                    prune_mma_kernel<true><<<nt, kTile, smem, ctx->stream>>>(
                         ds->d_nodes, tiles, d_PT, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix,
                         ds->d_mixlam, (int)ds->nroot, per_lambda ? 1 : 0);
                     LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");

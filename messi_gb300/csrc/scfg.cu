@@ -53,6 +53,19 @@ __device__ __forceinline__ void lse_add(float& m, float& s, float x)
     }
 }
 
+// Four terms at once: the loads feeding them are independent, so a lane keeps
+// four L2 requests in flight instead of one.
+__device__ __forceinline__ void lse_add4(float& m, float& s, float x0, float x1, float x2, float x3)
+{
+    const float mx = fmaxf(fmaxf(x0, x1), fmaxf(x2, x3));
+    if (mx == -INFINITY) return;
+    if (mx > m) {
+        s *= __expf(m - mx);
+        m = mx;
+    }
+    s += (__expf(x0 - m) + __expf(x1 - m)) + (__expf(x2 - m) + __expf(x3 - m));
+}
+
 __device__ __forceinline__ void lse_merge(float& m, float& s, float m2, float s2)
 {
     if (m2 > m) {
@@ -262,7 +275,11 @@ __global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R)
         if (i >= lo) {
             float m = -INFINITY, s = 0.f;
             const float* lrow = t.Lrow + (size_t)i * t.RS;
-            for (int k = (i0 - i) + lane; k <= t.Wb; k += 32) lse_add(m, s, lrow[k] + t.Ssuf[i + k + 1]);
+            int k = (i0 - i) + lane;
+            for (; k + 96 <= t.Wb; k += 128)
+                lse_add4(m, s, lrow[k] + t.Ssuf[i + k + 1], lrow[k + 32] + t.Ssuf[i + k + 33],
+                         lrow[k + 64] + t.Ssuf[i + k + 65], lrow[k + 96] + t.Ssuf[i + k + 97]);
+            for (; k <= t.Wb; k += 32) lse_add(m, s, lrow[k] + t.Ssuf[i + k + 1]);
             group_reduce<32>(m, s);
             if (lane == 0) known[w] = lse_val(m, s);
         }
@@ -394,7 +411,12 @@ __global__ void __launch_bounds__(256) inside_wave_kernel(Band t, Rules R, doubl
             if (valid) {
                 const float* lrow = t.Lrow + (size_t)i * RS;
                 const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
-                for (int k = lane; k < d; k += G) lse_add(m, s, __ldcg(lrow + k) + __ldcg(scol - k));
+                int k = lane;
+                for (; k + 3 * G < d; k += 4 * G)
+                    lse_add4(m, s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
+                             __ldcg(lrow + k + 2 * G) + __ldcg(scol - k - 2 * G),
+                             __ldcg(lrow + k + 3 * G) + __ldcg(scol - k - 3 * G));
+                for (; k < d; k += G) lse_add(m, s, __ldcg(lrow + k) + __ldcg(scol - k));
             }
             group_reduce_rt(m, s, G);
             if (valid && lane == 0) {
@@ -439,7 +461,13 @@ __global__ void __launch_bounds__(256) outside_wave_kernel(Band t, Rules R)
                 const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
                 if (j + 1 <= L - 1) {
                     const float* srw = t.Srow + (size_t)(j + 1) * RS;
-                    for (int q = lane; q < nL; q += G) {
+                    int q = lane;
+                    for (; q + G < nL; q += 2 * G) {
+                        const float sib0 = srw[q], sib1 = srw[q + G];
+                        lse_add4(mL, sL, R.r[0] + __ldcg(osr + q) + sib0, R.r[4] + __ldcg(ofr + q) + sib0,
+                                 R.r[0] + __ldcg(osr + q + G) + sib1, R.r[4] + __ldcg(ofr + q + G) + sib1);
+                    }
+                    for (; q < nL; q += G) {
                         const float sib = srw[q];
                         lse_add(mL, sL, R.r[0] + __ldcg(osr + q) + sib);
                         lse_add(mL, sL, R.r[4] + __ldcg(ofr + q) + sib);
@@ -452,7 +480,13 @@ __global__ void __launch_bounds__(256) outside_wave_kernel(Band t, Rules R)
                     const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
                     const float* osc = t.OScol + (size_t)j * RS + d + 1;
                     const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
-                    for (int q = lane; q < nS; q += G) {
+                    int q = lane;
+                    for (; q + G < nS; q += 2 * G) {
+                        const float l0 = lcol[q], l1 = lcol[q + G];
+                        lse_add4(mS, sS, R.r[0] + __ldcg(osc + q) + l0, R.r[4] + __ldcg(ofc + q) + l0,
+                                 R.r[0] + __ldcg(osc + q + G) + l1, R.r[4] + __ldcg(ofc + q + G) + l1);
+                    }
+                    for (; q < nS; q += G) {
                         const float lft = lcol[q];
                         lse_add(mS, sS, R.r[0] + __ldcg(osc + q) + lft);
                         lse_add(mS, sS, R.r[4] + __ldcg(ofc + q) + lft);
@@ -566,7 +600,11 @@ __global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
             if (i >= 1) {
                 const float* lcol = t.Lcol + (size_t)(i - 1) * t.RS;
                 const int kmax = min(t.Wb, i - 1);
-                for (int k = (i - i0) + lane; k <= kmax; k += 32) lse_add(m, s, t.Osuf[i - k - 1] + lcol[k]);
+                int k = (i - i0) + lane;
+                for (; k + 96 <= kmax; k += 128)
+                    lse_add4(m, s, t.Osuf[i - k - 1] + lcol[k], t.Osuf[i - k - 33] + lcol[k + 32],
+                             t.Osuf[i - k - 65] + lcol[k + 64], t.Osuf[i - k - 97] + lcol[k + 96]);
+                for (; k <= kmax; k += 32) lse_add(m, s, t.Osuf[i - k - 1] + lcol[k]);
             }
             group_reduce<32>(m, s);
             if (lane == 0) known[w] = lse_val(m, s);
