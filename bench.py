@@ -19,6 +19,7 @@ path (oracle/) on this host's cores.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -397,6 +398,45 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_mcmc(args):
+    """Config 5: plain move-8 random walk vs the learned mixture proposal on
+    the c2 alignment, each for --mcmc-iters iterations (first third burn-in;
+    the learned proposal trains during burn-in and is frozen after)."""
+    import numpy as np
+
+    from messi_gb300 import mcmc, synth
+    s = synth.make_workload(args.workload, seed=1)
+    ds = s.dataset
+    n = args.mcmc_iters
+    burn = n // 3
+    theta0 = mcmc.theta_from_p15(s.params15)
+    out = {}
+    means = {}
+    for kind in ("plain", "learned"):
+        tgt = mcmc.Target(ds, s.params15[11:14], s.W)
+        learned = mcmc.LearnedProposal(mcmc.alignment_summaries(ds), seed=3) if kind == "learned" else None
+        res = mcmc.run_chain(tgt, theta0, n, burn, proposal=kind, seed=11, learned=learned,
+                             fit_every=max(25, burn // 10), fit_steps=150)
+        Z = np.array([mcmc.to_z(t) for t in res.samples])
+        ess = np.array([mcmc.ess(Z[:, k]) for k in range(mcmc.NFREE)])
+        se = np.array([mcmc.mcse(res.samples[:, k]) for k in range(mcmc.NFREE)])
+        out[kind] = {"ess_per_s": (ess / res.seconds).tolist(), "ess": ess.tolist(), "seconds": res.seconds,
+                     "median_ess_per_s": float(np.median(ess / res.seconds)),
+                     "min_ess_per_s": float(np.min(ess / res.seconds)), "accept": res.accept,
+                     "likelihood_evals": res.evals, "gpu_launches": tgt.launches, **res.extra}
+        means[kind] = (res.samples.mean(axis=0), se)
+    (mp, sp), (ml, sl) = means["plain"], means["learned"]
+    z = np.abs(mp - ml) / np.sqrt(sp ** 2 + sl ** 2)
+    ratio = out["learned"]["median_ess_per_s"] / out["plain"]["median_ess_per_s"]
+    line = {"metric": "MCMC ESS/s learned vs plain proposal", "value": ratio, "unit": "x (median over parameters)",
+            "higher_is_better": True, "n_gpus": 1, "iterations": n, "burnin": burn, "data": "synthetic",
+            "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories", "parameters": list(mcmc.FREE)},
+            "plain": out["plain"], "learned": out["learned"],
+            "posterior_mean_agreement_z": z.tolist(), "max_z": float(z.max()),
+            "within_2_mcse": bool(np.all(z <= 2.0 * math.sqrt(2.0)))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,13 +445,17 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--mcmc", action="store_true", help="run the MCMC comparison (config 5) instead")
+    ap.add_argument("--mcmc-iters", type=int, default=3000)
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT))
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up + timed steps only (for ncu), print a short line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.mcmc:
+        run_mcmc(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -160,6 +160,30 @@ int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const do
 int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const double* gapfrequency,
                      double gapcutoff, double* Z, double* unpaired);
 
+/* ---- Learned MCMC proposal network (HP3; no counterpart in the reference,
+ * whose MCMC moves are all hand-tuned random walks, src/MCMC.jl:1307-1674).
+ * A BF16 MLP (three linear layers in -> width -> width -> out, SiLU) whose
+ * head is a diagonal Gaussian mixture of `ncomp` components over `dim`
+ * values: [ncomp logits | ncomp*dim means | ncomp*dim log-sd].  Forward,
+ * backward and Adam run in the library's own kernels. */
+typedef struct messi_mlp messi_mlp;
+int messi_mlp_create(messi_ctx* ctx, int32_t in_dim, int32_t width, int32_t ncomp, int32_t dim, uint64_t seed,
+                     messi_mlp** mlp);
+int messi_mlp_destroy(messi_mlp* mlp);
+int messi_mlp_nparams(messi_mlp* mlp, int32_t* n);
+/* FP32 master parameters in the layout W1[w][in] b1 W2[w][w] b2 W3[out][w] b3. */
+int messi_mlp_get_params(messi_ctx* ctx, messi_mlp* mlp, float* params);
+int messi_mlp_set_params(messi_ctx* ctx, messi_mlp* mlp, const float* params);
+/* y[batch][out] = head(x[batch][in]). */
+int messi_mlp_forward(messi_ctx* ctx, messi_mlp* mlp, int32_t batch, const float* x, float* y);
+/* Mean mixture negative log-likelihood of target[batch][dim] and its
+ * gradient w.r.t. the FP32 parameters (grads nullable). */
+int messi_mlp_gradients(messi_ctx* ctx, messi_mlp* mlp, int32_t batch, const float* x, const float* target,
+                        float* loss, float* grads);
+/* One Adam step on that loss (gradient norm clipped to max_grad_norm if > 0). */
+int messi_mlp_train_step(messi_ctx* ctx, messi_mlp* mlp, int32_t batch, const float* x, const float* target,
+                         float lr, float max_grad_norm, float* loss);
+
 /* KH99 inside pass that allocates nothing (no counterpart in the reference;
  * computeinsideKH99 always allocates its tables).  For callers that must not
  * call cudaMalloc -- code running under CUDA stream capture, inside a

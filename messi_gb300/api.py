@@ -300,3 +300,69 @@ def computestructureintegratedlikelihood(dataset, params, maxbasepairdistance=10
         params.lambdaGT = saved
     total = params.logprior + Z.value
     return (total, Z.value, u) if return_unpaired else total
+
+
+# ---------------------------------------------------------------------------
+# HP3: the learned-proposal network
+# ---------------------------------------------------------------------------
+class MLP:
+    """BF16 MLP with a Gaussian-mixture head, trained and run by the
+    library's kernels (include/messi_gb300.h, messi_mlp_*)."""
+
+    def __init__(self, in_dim, width, ncomp, dim, seed=1, ctx=None):
+        self.ctx = ctx or get_context()
+        self.in_dim, self.width, self.ncomp, self.dim = in_dim, width, ncomp, dim
+        self.out_dim = ncomp + 2 * ncomp * dim
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.messi_mlp_create(self.ctx.handle, in_dim, width, ncomp, dim, seed, ctypes.byref(h)),
+                       "messi_mlp_create")
+        self.handle = h
+        n = ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.messi_mlp_nparams(h, ctypes.byref(n)), "messi_mlp_nparams")
+        self.nparams = n.value
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.messi_mlp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        out = np.empty(self.nparams, np.float32)
+        self.ctx.check(self.ctx.lib.messi_mlp_get_params(self.ctx.handle, self.handle, _p(out)), "messi_mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self.ctx.check(self.ctx.lib.messi_mlp_set_params(self.ctx.handle, self.handle, _p(p)), "messi_mlp_set_params")
+
+    def forward(self, x):
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float32)
+        y = np.empty((x.shape[0], self.out_dim), np.float32)
+        self.ctx.check(self.ctx.lib.messi_mlp_forward(self.ctx.handle, self.handle, x.shape[0], _p(x), _p(y)),
+                       "messi_mlp_forward")
+        return y
+
+    def gradients(self, x, target):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(target, np.float32)
+        g = np.empty(self.nparams, np.float32)
+        loss = ctypes.c_float()
+        self.ctx.check(self.ctx.lib.messi_mlp_gradients(self.ctx.handle, self.handle, x.shape[0], _p(x), _p(t),
+                                                        ctypes.byref(loss), _p(g)), "messi_mlp_gradients")
+        return loss.value, g
+
+    def train_step(self, x, target, lr=1e-3, max_grad_norm=10.0):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(target, np.float32)
+        loss = ctypes.c_float()
+        self.ctx.check(self.ctx.lib.messi_mlp_train_step(self.ctx.handle, self.handle, x.shape[0], _p(x), _p(t),
+                                                         float(lr), float(max_grad_norm), ctypes.byref(loss)),
+                       "messi_mlp_train_step")
+        return loss.value
+

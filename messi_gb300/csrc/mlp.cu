@@ -1,0 +1,508 @@
+// mlp.cu -- the learned MCMC proposal network (HP3): a BF16 MLP with a
+// Gaussian-mixture head, trained and evaluated on the GPU.
+//
+// The reference's MCMC moves (src/MCMC.jl:1307-1674) have no learned part;
+// this network is the proposal described for the learned chain: input = the
+// current model parameters (transformed) + alignment summary statistics,
+// output = a K-component diagonal Gaussian mixture over the free parameters.
+//
+// Layout: three linear layers in -> H -> H -> out with SiLU after the first
+// two.  Weights are kept in FP32 (Adam master copy) and BF16 (the copy the
+// forward/backward kernels read); activations are BF16, every product is
+// accumulated in FP32.  The GEMMs are tiny (batch <= a few hundred, width
+// 256) and latency bound, so they run as 32x32-tiled CUDA-core kernels.
+//
+// Head per sample: [K logits | K*D means | K*D log-sd]; the loss is the
+// negative log-likelihood of a target vector under the mixture.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+struct messi_mlp {
+    int in = 0, H = 0, out = 0, K = 0, D = 0;
+    int cap = 0;                       // batch capacity of the activation buffers
+    // parameters: W1[H][in] b1[H] W2[H][H] b2[H] W3[out][H] b3[out]
+    int nparam = 0;
+    float* p32 = nullptr;              // FP32 master
+    __nv_bfloat16* p16 = nullptr;      // BF16 copy
+    float* grad = nullptr;
+    float* m1 = nullptr;               // Adam moments
+    float* m2 = nullptr;
+    int64_t steps = 0;
+    // activations
+    __nv_bfloat16 *x = nullptr, *a1 = nullptr, *a2 = nullptr;   // inputs / post-SiLU (BF16)
+    float *z1 = nullptr, *z2 = nullptr, *y = nullptr;           // pre-activations, head (FP32)
+    float *dy = nullptr, *d2 = nullptr, *d1 = nullptr;          // gradients w.r.t. y, a2/z2, a1/z1
+    float* target = nullptr;
+    float* loss = nullptr;             // [cap]
+    float* stage = nullptr;            // host-pinned staging
+};
+
+namespace messi {
+
+namespace {
+
+constexpr int kT = 32;  // GEMM tile
+
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// C[m][n] = sum_k A(m, k) * B(k, n), A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn].
+// mode 0: C = acc + bias[n] (FP32 out); mode 1: C += acc (FP32 accumulate into C).
+template <typename TA, typename TB>
+__global__ void gemm_kernel(int M, int N, int K, const TA* __restrict__ A, long long sam, long long sak,
+                            const TB* __restrict__ B, long long sbk, long long sbn, const float* __restrict__ bias,
+                            float* __restrict__ C, long long scm, int mode)
+{
+    __shared__ float As[kT][kT + 1];
+    __shared__ float Bs[kT][kT + 1];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+    const int m0 = blockIdx.y * kT, n0 = blockIdx.x * kT;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k0 = 0; k0 < K; k0 += kT) {
+        for (int r = ty; r < kT; r += 8) {
+            const int m = m0 + r, k = k0 + tx;
+            As[r][tx] = (m < M && k < K) ? to_f(A[m * sam + k * sak]) : 0.f;
+            const int kk = k0 + r, n = n0 + tx;
+            Bs[r][tx] = (kk < K && n < N) ? to_f(B[kk * sbk + n * sbn]) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int k = 0; k < kT; k++) {
+            const float b = Bs[k][tx];
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[q] = fmaf(As[ty + 8 * q][k], b, acc[q]);
+        }
+        __syncthreads();
+    }
+    const int n = n0 + tx;
+    if (n >= N) return;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int m = m0 + ty + 8 * q;
+        if (m >= M) continue;
+        float* c = C + m * scm + n;
+        if (mode == 0) *c = acc[q] + (bias ? bias[n] : 0.f);
+        else *c += acc[q];
+    }
+}
+
+template <typename TA, typename TB>
+int gemm(messi_ctx* ctx, int M, int N, int K, const TA* A, long long sam, long long sak, const TB* B, long long sbk,
+         long long sbn, const float* bias, float* C, long long scm, int mode)
+{
+    dim3 grid((N + kT - 1) / kT, (M + kT - 1) / kT);
+    gemm_kernel<TA, TB><<<grid, 256, 0, ctx->stream>>>(M, N, K, A, sam, sak, B, sbk, sbn, bias, C, scm, mode);
+    LAUNCH_CHECK(ctx, "gemm_kernel");
+    return MESSI_OK;
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z)
+{
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+
+__global__ void silu_kernel(const float* __restrict__ z, __nv_bfloat16* __restrict__ a, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = __float2bfloat16(silu(z[i]));
+}
+
+__global__ void dsilu_kernel(const float* __restrict__ z, float* __restrict__ d, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] *= dsilu(z[i]);
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ s, __nv_bfloat16* __restrict__ d, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = __float2bfloat16(s[i]);
+}
+
+__global__ void colsum_kernel(const float* __restrict__ dY, int M, int N, float* __restrict__ db)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    float s = 0.f;
+    for (int m = 0; m < M; m++) s += dY[(long long)m * N + n];
+    db[n] += s;
+}
+
+// Mixture negative log-likelihood per sample and its gradient w.r.t. the head.
+// y: [K logits | K*D means | K*D log-sd], log-sd clamped to [-7, 5].
+__global__ void mixture_nll_kernel(const float* __restrict__ y, const float* __restrict__ tgt, int M, int K, int D,
+                                   float* __restrict__ loss, float* __restrict__ dy, float inv_batch)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const int O = K + 2 * K * D;
+    const float* ym = y + (long long)m * O;
+    const float* x = tgt + (long long)m * D;
+    float* g = dy + (long long)m * O;
+    float lw[8], lp[8];
+    float mx = -INFINITY;
+    for (int k = 0; k < K; k++) mx = fmaxf(mx, ym[k]);
+    float se = 0.f;
+    for (int k = 0; k < K; k++) se += __expf(ym[k] - mx);
+    const float lse_w = mx + __logf(se);
+    const float c = -0.91893853320467274f * D;  // -D/2 log(2 pi)
+    float best = -INFINITY;
+    for (int k = 0; k < K; k++) {
+        lw[k] = ym[k] - lse_w;
+        float s = c;
+        for (int d = 0; d < D; d++) {
+            const float ls = fminf(fmaxf(ym[K + K * D + k * D + d], -7.f), 5.f);
+            const float r = (x[d] - ym[K + k * D + d]) * __expf(-ls);
+            s += -0.5f * r * r - ls;
+        }
+        lp[k] = lw[k] + s;
+        best = fmaxf(best, lp[k]);
+    }
+    float tot = 0.f;
+    for (int k = 0; k < K; k++) tot += __expf(lp[k] - best);
+    const float ll = best + __logf(tot);
+    loss[m] = -ll;
+    for (int k = 0; k < K; k++) {
+        const float r_k = __expf(lp[k] - ll);        // responsibility
+        const float w_k = __expf(lw[k]);
+        g[k] = (w_k - r_k) * inv_batch;              // d(-ll)/d logit
+        for (int d = 0; d < D; d++) {
+            const float raw = ym[K + K * D + k * D + d];
+            const float ls = fminf(fmaxf(raw, -7.f), 5.f);
+            const float iv = __expf(-2.f * ls);
+            const float diff = x[d] - ym[K + k * D + d];
+            g[K + k * D + d] = -r_k * diff * iv * inv_batch;
+            const float gls = -r_k * (diff * diff * iv - 1.f);
+            g[K + K * D + k * D + d] = (raw > -7.f && raw < 5.f) ? gls * inv_batch : 0.f;
+        }
+    }
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m1,
+                            float* __restrict__ m2, __nv_bfloat16* __restrict__ p16, int n, float lr, float b1,
+                            float b2, float c1, float c2, float eps, float clip_scale)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float g = gr[i] * clip_scale;
+    const float a = b1 * m1[i] + (1.f - b1) * g;
+    const float b = b2 * m2[i] + (1.f - b2) * g * g;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = p[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+    p[i] = v;
+    p16[i] = __float2bfloat16(v);
+}
+
+__global__ void sumsq_kernel(const float* __restrict__ g, int n, float* __restrict__ out)
+{
+    __shared__ float red[256];
+    float s = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += g[i] * g[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(out, red[0]);
+}
+
+}  // namespace
+
+static int mlp_offsets(const messi_mlp* m, size_t off[6])
+{
+    off[0] = 0;                                    // W1
+    off[1] = off[0] + (size_t)m->H * m->in;        // b1
+    off[2] = off[1] + m->H;                        // W2
+    off[3] = off[2] + (size_t)m->H * m->H;         // b2
+    off[4] = off[3] + m->H;                        // W3
+    off[5] = off[4] + (size_t)m->out * m->H;       // b3
+    return (int)(off[5] + m->out);
+}
+
+static int mlp_reserve(messi_ctx* ctx, messi_mlp* m, int batch)
+{
+    if (batch <= m->cap) return MESSI_OK;
+    cudaFree(m->x);
+    cudaFree(m->a1);
+    cudaFree(m->a2);
+    cudaFree(m->z1);
+    cudaFree(m->z2);
+    cudaFree(m->y);
+    cudaFree(m->dy);
+    cudaFree(m->d2);
+    cudaFree(m->d1);
+    cudaFree(m->target);
+    cudaFree(m->loss);
+    cudaFreeHost(m->stage);
+    const size_t B = (size_t)batch;
+    cudaError_t e = cudaSuccess;
+    auto al = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    al((void**)&m->x, B * m->in * 2);
+    al((void**)&m->a1, B * m->H * 2);
+    al((void**)&m->a2, B * m->H * 2);
+    al((void**)&m->z1, B * m->H * 4);
+    al((void**)&m->z2, B * m->H * 4);
+    al((void**)&m->y, B * m->out * 4);
+    al((void**)&m->dy, B * m->out * 4);
+    al((void**)&m->d2, B * m->H * 4);
+    al((void**)&m->d1, B * m->H * 4);
+    al((void**)&m->target, B * m->D * 4);
+    al((void**)&m->loss, B * 4 + 64);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&m->stage, B * (m->in + m->out + m->D + 2) * 4 + 64);
+    if (e != cudaSuccess) {
+        m->cap = 0;
+        return cuda_fail(ctx, e, "mlp activations");
+    }
+    m->cap = batch;
+    return MESSI_OK;
+}
+
+static inline unsigned blocks(long long n) { return (unsigned)((n + 255) / 256); }
+
+// forward pass on the batch already in m->x (BF16)
+static int mlp_forward_dev(messi_ctx* ctx, messi_mlp* m, int Bn)
+{
+    size_t off[6];
+    mlp_offsets(m, off);
+    const __nv_bfloat16* W1 = m->p16 + off[0];
+    const __nv_bfloat16* W2 = m->p16 + off[2];
+    const __nv_bfloat16* W3 = m->p16 + off[4];
+    int rc;
+    // z1 = x W1^T + b1 : A = x [B x in], B(k, n) = W1[n][k]
+    if ((rc = gemm(ctx, Bn, m->H, m->in, m->x, m->in, 1, W1, 1, m->in, m->p32 + off[1], m->z1, m->H, 0))) return rc;
+    silu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z1, m->a1, (long long)Bn * m->H);
+    LAUNCH_CHECK(ctx, "silu_kernel");
+    if ((rc = gemm(ctx, Bn, m->H, m->H, m->a1, m->H, 1, W2, 1, m->H, m->p32 + off[3], m->z2, m->H, 0))) return rc;
+    silu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z2, m->a2, (long long)Bn * m->H);
+    LAUNCH_CHECK(ctx, "silu_kernel");
+    return gemm(ctx, Bn, m->out, m->H, m->a2, m->H, 1, W3, 1, m->H, m->p32 + off[5], m->y, m->out, 0);
+}
+
+// loss + gradients into m->grad (zeroed first); returns via m->loss
+static int mlp_backward_dev(messi_ctx* ctx, messi_mlp* m, int Bn)
+{
+    size_t off[6];
+    mlp_offsets(m, off);
+    const __nv_bfloat16* W2 = m->p16 + off[2];
+    const __nv_bfloat16* W3 = m->p16 + off[4];
+    cudaError_t e = cudaMemsetAsync(m->grad, 0, sizeof(float) * m->nparam, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "grad reset");
+    mixture_nll_kernel<<<blocks(Bn), 256, 0, ctx->stream>>>(m->y, m->target, Bn, m->K, m->D, m->loss, m->dy,
+                                                            1.f / (float)Bn);
+    LAUNCH_CHECK(ctx, "mixture_nll_kernel");
+    int rc;
+    // layer 3: dW3[o][h] = sum_b dy[b][o] a2[b][h]; db3 = colsum dy; d2 = dy W3
+    if ((rc = gemm(ctx, m->out, m->H, Bn, m->dy, 1, m->out, m->a2, m->H, 1, nullptr, m->grad + off[4], m->H, 1)))
+        return rc;
+    colsum_kernel<<<blocks(m->out), 256, 0, ctx->stream>>>(m->dy, Bn, m->out, m->grad + off[5]);
+    LAUNCH_CHECK(ctx, "colsum_kernel");
+    if ((rc = gemm(ctx, Bn, m->H, m->out, m->dy, m->out, 1, W3, m->H, 1, nullptr, m->d2, m->H, 0))) return rc;
+    dsilu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z2, m->d2, (long long)Bn * m->H);
+    LAUNCH_CHECK(ctx, "dsilu_kernel");
+    // layer 2
+    if ((rc = gemm(ctx, m->H, m->H, Bn, m->d2, 1, m->H, m->a1, m->H, 1, nullptr, m->grad + off[2], m->H, 1)))
+        return rc;
+    colsum_kernel<<<blocks(m->H), 256, 0, ctx->stream>>>(m->d2, Bn, m->H, m->grad + off[3]);
+    LAUNCH_CHECK(ctx, "colsum_kernel");
+    if ((rc = gemm(ctx, Bn, m->H, m->H, m->d2, m->H, 1, W2, m->H, 1, nullptr, m->d1, m->H, 0))) return rc;
+    dsilu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z1, m->d1, (long long)Bn * m->H);
+    LAUNCH_CHECK(ctx, "dsilu_kernel");
+    // layer 1
+    if ((rc = gemm(ctx, m->H, m->in, Bn, m->d1, 1, m->H, m->x, m->in, 1, nullptr, m->grad + off[0], m->in, 1)))
+        return rc;
+    colsum_kernel<<<blocks(m->H), 256, 0, ctx->stream>>>(m->d1, Bn, m->H, m->grad + off[1]);
+    LAUNCH_CHECK(ctx, "colsum_kernel");
+    return MESSI_OK;
+}
+
+static int upload_batch(messi_ctx* ctx, messi_mlp* m, int Bn, const float* x, const float* target)
+{
+    int rc;
+    if ((rc = mlp_reserve(ctx, m, Bn))) return rc;
+    float* st = m->stage;
+    std::memcpy(st, x, sizeof(float) * Bn * m->in);
+    cudaError_t e = cudaMemcpyAsync(m->z1, st, sizeof(float) * Bn * m->in, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mlp input upload");
+    // inputs to BF16 (z1 is free at this point and large enough: H >= in)
+    to_bf16_kernel<<<blocks((long long)Bn * m->in), 256, 0, ctx->stream>>>(m->z1, m->x, (long long)Bn * m->in);
+    LAUNCH_CHECK(ctx, "to_bf16_kernel");
+    if (target) {
+        float* sp = st + (size_t)Bn * m->in;
+        std::memcpy(sp, target, sizeof(float) * Bn * m->D);
+        e = cudaMemcpyAsync(m->target, sp, sizeof(float) * Bn * m->D, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "mlp target upload");
+    }
+    return MESSI_OK;
+}
+
+}  // namespace messi
+
+using namespace messi;
+
+extern "C" {
+
+int messi_mlp_create(messi_ctx* ctx, int32_t in_dim, int32_t width, int32_t ncomp, int32_t dim, uint64_t seed,
+                     messi_mlp** out)
+{
+    if (!ctx || !out || in_dim < 1 || width < 1 || ncomp < 1 || ncomp > 8 || dim < 1) return MESSI_EINVAL;
+    if (width < in_dim) return fail(ctx, MESSI_EINVAL, "mlp: width must be >= input size");
+    cudaSetDevice(ctx->device);
+    messi_mlp* m = new messi_mlp();
+    m->in = in_dim;
+    m->H = width;
+    m->K = ncomp;
+    m->D = dim;
+    m->out = ncomp + 2 * ncomp * dim;
+    size_t off[6];
+    m->nparam = mlp_offsets(m, off);
+    // He-style initialisation from a splitmix64 stream (deterministic in seed)
+    std::vector<float> p(m->nparam, 0.f);
+    uint64_t st = seed ? seed : 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto fill = [&](size_t o, size_t n, double scale) {
+        for (size_t i = 0; i < n; i++) p[o + i] = (float)((2.0 * next() - 1.0) * scale);
+    };
+    fill(off[0], (size_t)m->H * m->in, std::sqrt(3.0 / m->in));
+    fill(off[2], (size_t)m->H * m->H, std::sqrt(3.0 / m->H));
+    fill(off[4], (size_t)m->out * m->H, 0.1 * std::sqrt(3.0 / m->H));
+    cudaError_t e = cudaMalloc((void**)&m->p32, sizeof(float) * m->nparam);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->p16, sizeof(__nv_bfloat16) * m->nparam);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->grad, sizeof(float) * (m->nparam + 16));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->m1, sizeof(float) * m->nparam);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->m2, sizeof(float) * m->nparam);
+    if (e == cudaSuccess) e = cudaMemcpy(m->p32, p.data(), sizeof(float) * m->nparam, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(m->m1, 0, sizeof(float) * m->nparam);
+    if (e == cudaSuccess) e = cudaMemset(m->m2, 0, sizeof(float) * m->nparam);
+    if (e != cudaSuccess) {
+        messi_mlp_destroy(m);
+        return cuda_fail(ctx, e, "mlp parameters");
+    }
+    to_bf16_kernel<<<blocks(m->nparam), 256, 0, ctx->stream>>>(m->p32, m->p16, m->nparam);
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        messi_mlp_destroy(m);
+        return cuda_fail(ctx, e, "mlp init");
+    }
+    *out = m;
+    return MESSI_OK;
+}
+
+int messi_mlp_destroy(messi_mlp* m)
+{
+    if (!m) return MESSI_EINVAL;
+    void* ptrs[] = {m->p32, m->p16, m->grad, m->m1, m->m2, m->x, m->a1, m->a2, m->z1,
+                    m->z2,  m->y,   m->dy,   m->d2, m->d1, m->target, m->loss};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (m->stage) cudaFreeHost(m->stage);
+    delete m;
+    return MESSI_OK;
+}
+
+int messi_mlp_nparams(messi_mlp* m, int32_t* n)
+{
+    if (!m || !n) return MESSI_EINVAL;
+    *n = m->nparam;
+    return MESSI_OK;
+}
+
+int messi_mlp_get_params(messi_ctx* ctx, messi_mlp* m, float* host)
+{
+    if (!ctx || !m || !host) return MESSI_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMemcpy(host, m->p32, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "mlp get params");
+}
+
+int messi_mlp_set_params(messi_ctx* ctx, messi_mlp* m, const float* host)
+{
+    if (!ctx || !m || !host) return MESSI_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMemcpy(m->p32, host, sizeof(float) * m->nparam, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mlp set params");
+    to_bf16_kernel<<<blocks(m->nparam), 256, 0, ctx->stream>>>(m->p32, m->p16, m->nparam);
+    e = cudaStreamSynchronize(ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "mlp set params");
+}
+
+int messi_mlp_forward(messi_ctx* ctx, messi_mlp* m, int32_t batch, const float* x, float* y)
+{
+    if (!ctx || !m || batch < 1 || !x || !y) return MESSI_EINVAL;
+    ctx->launches = 0;
+    cudaSetDevice(ctx->device);
+    int rc;
+    if ((rc = upload_batch(ctx, m, batch, x, nullptr))) return rc;
+    if ((rc = mlp_forward_dev(ctx, m, batch))) return rc;
+    cudaError_t e = cudaMemcpyAsync(y, m->y, sizeof(float) * batch * m->out, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "mlp forward");
+}
+
+int messi_mlp_gradients(messi_ctx* ctx, messi_mlp* m, int32_t batch, const float* x, const float* target,
+                        float* loss, float* grads)
+{
+    if (!ctx || !m || batch < 1 || !x || !target) return MESSI_EINVAL;
+    ctx->launches = 0;
+    cudaSetDevice(ctx->device);
+    int rc;
+    if ((rc = upload_batch(ctx, m, batch, x, target))) return rc;
+    if ((rc = mlp_forward_dev(ctx, m, batch))) return rc;
+    if ((rc = mlp_backward_dev(ctx, m, batch))) return rc;
+    std::vector<float> l(batch);
+    cudaError_t e = cudaMemcpyAsync(l.data(), m->loss, sizeof(float) * batch, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && grads)
+        e = cudaMemcpyAsync(grads, m->grad, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mlp gradients");
+    if (loss) {
+        double s = 0.0;
+        for (float v : l) s += v;
+        *loss = (float)(s / batch);
+    }
+    return MESSI_OK;
+}
+
+int messi_mlp_train_step(messi_ctx* ctx, messi_mlp* m, int32_t batch, const float* x, const float* target, float lr,
+                         float max_grad_norm, float* loss)
+{
+    int rc = messi_mlp_gradients(ctx, m, batch, x, target, loss, nullptr);
+    if (rc) return rc;
+    float* d_norm = m->grad + m->nparam;  // spare slot
+    cudaMemsetAsync(d_norm, 0, sizeof(float), ctx->stream);
+    sumsq_kernel<<<64, 256, 0, ctx->stream>>>(m->grad, m->nparam, d_norm);
+    LAUNCH_CHECK(ctx, "sumsq_kernel");
+    float h = 0.f;
+    cudaError_t e = cudaMemcpyAsync(&h, d_norm, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "grad norm");
+    const float gn = std::sqrt(h);
+    const float clip = (max_grad_norm > 0.f && gn > max_grad_norm) ? max_grad_norm / gn : 1.f;
+    m->steps++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)m->steps), c2 = 1.f - std::pow(b2, (float)m->steps);
+    adam_kernel<<<blocks(m->nparam), 256, 0, ctx->stream>>>(m->p32, m->grad, m->m1, m->m2, m->p16, m->nparam, lr, b1,
+                                                            b2, c1, c2, 1e-8f, clip);
+    LAUNCH_CHECK(ctx, "adam_kernel");
+    e = cudaStreamSynchronize(ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "adam");
+}
+
+}  // extern "C"
