@@ -53,10 +53,11 @@ def lib():
             L.mo_maskgapped.argtypes = [_f64pF, _f64p, c_int, c_double, c_double]
             L.mo_kh99_logprobs.argtypes = [_f64p]
             L.mo_inside.argtypes = [_f64p, _f64pF, c_int, c_double, _f64pF, c_int]
+            L.mo_inside_banded.argtypes = [_f64p, _f64pF, c_int, c_int, c_double, ctypes.POINTER(c_double), c_int]
             L.mo_outside.argtypes = [_f64pF, _f64p, _f64pF, c_int, _f64pF, c_int]
             L.mo_basepairprobs.argtypes = [_f64pF, _f64pF, _f64p, _f64pF, c_int, _f64p, _f64pF]
             for name in ("mo_reversible_eig", "mo_transition_matrices", "mo_subcolumnrefs", "mo_pair_matrix",
-                         "mo_unpaired", "mo_inside", "mo_outside", "mo_basepairprobs"):
+                         "mo_unpaired", "mo_inside", "mo_inside_banded", "mo_outside", "mo_basepairprobs"):
                 getattr(L, name).restype = c_int
             _lib = L
     return _lib
@@ -182,6 +183,15 @@ def inside(u, p, B=1.0, nthreads=0):
     ins = np.zeros((3, L, L), order="F")
     _check(lib().mo_inside(u, p, L, float(B), ins, int(nthreads)), "inside")
     return ins
+
+
+def inside_banded_Z(u, p, W, B=1.0, nthreads=0):
+    """Z of the banded inside pass (pairs of span > W must be -Inf in p)."""
+    u = np.ascontiguousarray(u, np.float64)
+    Z = ctypes.c_double()
+    _check(lib().mo_inside_banded(u, np.asfortranarray(p, np.float64), len(u), int(W), float(B), ctypes.byref(Z),
+                                  int(nthreads)), "inside_banded")
+    return Z.value
 
 
 def outside(ins, u, p, nthreads=0):

@@ -708,3 +708,67 @@ int mo_basepairprobs(const double* inside, const double* outside, const double* 
     }
     return MO_OK;
 }
+
+/*
+ * Banded inside pass (FP64): the same recurrences as mo_inside when every
+ * pair of span > W is -Inf.  Only cells of span <= W and the S cells of the
+ * last column reach Z (an S->LS chain ends at j = L-1; F and L need an
+ * enclosing or own pair), so the band plus that column gives the dense Z
+ * in O(L W^2).  Used to check Z at genome scale, where the dense O(L^3)
+ * pass is out of reach; tests pin it to mo_inside at small sizes.
+ */
+int mo_inside_banded(const double* u, const double* p, int L, int W, double B, double* Zout, int nthreads)
+{
+    double r[7];
+    mo_kh99_logprobs(r);
+    if (L < 1) return MO_EINVAL;
+    if (W > L - 1) W = L - 1;
+    if (W < 0) W = 0;
+    const size_t W1 = (size_t)W + 1;
+    double* S = (double*)malloc(sizeof(double) * L * W1);
+    double* F = (double*)malloc(sizeof(double) * L * W1);
+    double* Lt = (double*)malloc(sizeof(double) * L * W1);
+    double* suf = (double*)malloc(sizeof(double) * L);
+    if (!S || !F || !Lt || !suf) { free(S); free(F); free(Lt); free(suf); return MO_ENOMEM; }
+    for (size_t k = 0; k < (size_t)L * W1; k++) S[k] = F[k] = Lt[k] = -INFINITY;
+    for (int i = 0; i < L; i++) {
+        S[i * W1] = (u[i] + r[1]) * B;
+        Lt[i * W1] = (u[i] + r[5]) * B;
+        suf[i] = -INFINITY;
+    }
+    suf[L - 1] = S[(size_t)(L - 1) * W1];
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    for (int d = 1; d <= W; d++) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < L - d; i++) {
+            int j = i + d;
+            double tmp = -INFINITY;
+            for (int k = 0; k < d; k++) tmp = lse2(tmp, Lt[i * W1 + k] + S[(size_t)(i + k + 1) * W1 + (d - 1 - k)]);
+            double fin = (d >= 2) ? F[(size_t)(i + 1) * W1 + (d - 2)] : -INFINITY;
+            double pij = p[i + (size_t)j * L];
+            double s = lse2(-INFINITY, r[0] * B + tmp);
+            double f = lse2(-INFINITY, r[4] * B + tmp);
+            s = lse2(s, (r[2] + pij) * B + fin);
+            f = lse2(f, (r[3] + pij) * B + fin);
+            S[i * W1 + d] = s;
+            F[i * W1 + d] = f;
+            Lt[i * W1 + d] = lse2(-INFINITY, (r[6] + pij) * B + fin);
+            if (j == L - 1) suf[i] = s;
+        }
+    }
+    for (int i = L - 2 - W; i >= 0; i--) {
+        double tmp = -INFINITY;
+        for (int k = 0; k <= W; k++) tmp = lse2(tmp, Lt[i * W1 + k] + suf[i + k + 1]);
+        suf[i] = r[0] * B + tmp;
+    }
+    *Zout = suf[0];
+    free(S);
+    free(F);
+    free(Lt);
+    free(suf);
+    return MO_OK;
+}

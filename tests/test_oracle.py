@@ -212,3 +212,16 @@ def test_maskgapped():
     gf = np.array([0.0, 1.0, 0.2, 1.0, 0.0])
     m = co.maskgapped(p, gf, 1.0)
     assert np.isneginf(m[1, 0]) and np.isneginf(m[4, 3]) and m[0, 2] == 0.0
+
+
+@pytest.mark.parametrize("L,W", [(1, 3), (2, 1), (9, 3), (40, 7), (60, 59), (75, 20)])
+def test_banded_inside_equals_dense(L, W):
+    rng = np.random.default_rng(L * 7 + W)
+    u = rng.uniform(-40, -5, L)
+    p = np.full((L, L), -np.inf)
+    for i in range(L):
+        for j in range(i + 1, min(L, i + W + 1)):
+            p[i, j] = p[j, i] = u[i] + u[j] + rng.normal(0, 5)
+    Zd = co.inside(u, p)[0, 0, L - 1]
+    Zb = co.inside_banded_Z(u, p, W)
+    assert abs(Zd - Zb) <= 1e-12 * abs(Zd)
