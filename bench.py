@@ -437,6 +437,100 @@ def run_mcmc(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Batched evaluation (config 3: many alignments, W = L - 1 each): one
+    messi_batch_likelihood per step against the same alignments evaluated one
+    messi_likelihood call at a time.  Prints its own JSON line."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from messi_gb300 import api, synth
+    from messi_gb300 import model as M
+
+    t0 = time.perf_counter()
+    wl = synth.make_batch(args.batch, seed=1)
+    t_synth = time.perf_counter() - t0
+    datasets = [w.dataset for w in wl]
+    params = [M.getparams(w.params15, w.dataset.branchlengths) for w in wl]
+    npairs = sum(total_pairs(d.numcols, d.numcols - 1) for d in datasets)
+    ctx = api.get_context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", 0))
+    t0 = time.perf_counter()
+    b = api.Batch(datasets, ctx=ctx)
+    t_plan = time.perf_counter() - t0
+    st = b.stats()
+    for _ in range(args.warmup):
+        Z = b.likelihood(params)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches = 0
+    wall = 0.0
+    with Clocks(0) as clk:
+        for k in range(args.steps):
+            torch.cuda.synchronize()
+            t_host = time.perf_counter()
+            ev[k][0].record(stream)
+            Z = b.likelihood(params)
+            ev[k][1].record(stream)
+            torch.cuda.synchronize()
+            wall += time.perf_counter() - t_host
+            launches += ctx.last_launches()
+    ms_batch = sum(a.elapsed_time(c) for a, c in ev) / args.steps
+    wall_batch = 1e3 * wall / args.steps
+    ctx.profile(True)
+    b.likelihood(params)
+    p_ms, _, p_units = ctx.profile_read(0)
+    i_ms, _, i_cells = ctx.profile_read(1)
+    ctx.profile(False)
+    b.close()
+    # the same alignments one call at a time (plans built outside the timing)
+    seq_ms = 0.0
+    seq_wall = 0.0
+    seq_launches = 0
+    Zs = np.empty(len(datasets))
+    Zc = ctypes.c_double()
+    for k, (d, p) in enumerate(zip(datasets, params)):
+        h = api.DatasetHandle(ctx, d, d.numcols - 1)
+        m = api.ModelArgs(p)
+        gf = np.ascontiguousarray(d.gapfrequency, np.float64)
+
+        def one():
+            ctx.check(ctx.lib.messi_likelihood(ctx.handle, h.handle, ctypes.byref(m.struct),
+                                               gf.ctypes.data_as(ctypes.c_void_p), 1.0, ctypes.byref(Zc), None),
+                      "messi_likelihood")
+        one()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_host = time.perf_counter()
+        e0.record(stream)
+        one()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        seq_wall += 1e3 * (time.perf_counter() - t_host)
+        seq_ms += e0.elapsed_time(e1)
+        seq_launches += ctx.last_launches()
+        Zs[k] = Zc.value
+        h.close()
+    rel = float(np.max(np.abs(Z - Zs) / np.abs(Zs)))
+    line = {"metric": METRIC, "value": npairs / (ms_batch / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "dtype": "fp32/fp64",
+            "data": "synthetic",
+            "config": {"workload": f"{args.batch}: {len(datasets)} alignments, W = L - 1 each",
+                       "pairs": npairs, "columns": int(sum(d.numcols for d in datasets)),
+                       "sequences": int(sum(d.numseqs for d in datasets))},
+            "wall_ms_per_step": wall_batch,
+            "sequential": {"value": npairs / (seq_ms / 1e3), "ms_per_step": seq_ms, "wall_ms_per_step": seq_wall,
+                           "gpu_launches": seq_launches},
+            "speedup_vs_sequential": seq_ms / ms_batch, "wall_speedup_vs_sequential": seq_wall / wall_batch,
+            "gpu_launches": launches // max(1, args.steps),
+            "max_rel_diff_vs_sequential": rel, "plan_seconds": t_plan, "synth_seconds": t_synth, "stats": st,
+            "kernels": {"prune_ms": p_ms, "prune_updates": p_units, "inside_ms": i_ms, "inside_cells": i_cells,
+                        "prune_GBps_algorithmic": (p_units * BYTES_PER_UPDATE / 1e9) / (p_ms / 1e3) if p_ms else None},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -446,8 +540,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--mcmc", action="store_true", help="run the MCMC comparison (config 5) instead")
-    ap.add_argument("--mcmc-iters", type=int, default=3000)
+    ap.add_argument("--mcmc-iters", type=int, default=20000)
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT))
+    ap.add_argument("--batch", choices=["c3", "c3s"], default=None,
+                    help="time the batched evaluation of a batch workload instead (own JSON line)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run warm-up + timed steps only (for ncu), print a short line")
     args = ap.parse_args()
@@ -455,6 +551,8 @@ def main():
         args.warmup = 3
     if args.mcmc:
         run_mcmc(args)
+    elif args.batch:
+        run_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -152,6 +152,30 @@ int messi_basepairprobs(messi_ctx* ctx, int32_t L, const double* inside, const d
 int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,
                      double* Z, double* single, double* pairprobs);
 
+/* computeposteriordecodingcuda (src/InsideCUDA.jl:183-215) followed by
+ * posteriordecodingtraceback (src/RNATools.jl:43-72): maximum expected
+ * accuracy structure from posterior probabilities, in FP32 as the
+ * reference's GPU path.  singleprobs [L], pairprobs [L x L] (symmetric).
+ *   ematrix: optional [L x L] (e[i, j], zeros below the diagonal);
+ *   smatrix: optional [L x L] traceback codes (-1: i unpaired, -2: i pairs j,
+ *            k > 0: i pairs column k (1-based), bifurcation), 0 where unused;
+ *   paired:  optional [L] 1-based partner of each column, 0 when unpaired
+ *            (the reference's Julia vector). */
+int messi_posterior_decoding(messi_ctx* ctx, int32_t L, const double* singleprobs, const double* pairprobs,
+                             double alpha, double* ematrix, int32_t* smatrix, int32_t* paired);
+/* getPosteriorDecodingConsensusStructure from scores (the --processmax chain
+ * of src/MESSI.jl:1101-1103: inside, outside, basepairprobs, posterior
+ * decoding, traceback), device-resident throughout.  structure: [L] 1-based
+ * partners, 0 when unpaired. */
+int messi_consensus_structure(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired,
+                              int32_t maxspan, double alpha, int32_t* structure);
+/* samplestructure (src/InsideOutsideAlgorithm.jl:570-635, B = 1 as every
+ * caller uses it): nstruct structures drawn independently from the KH99
+ * posterior given the scores.  structures: [nstruct][L] 1-based partners, 0
+ * when unpaired.  Random numbers: SplitMix64 streams keyed by (seed, index),
+ * so a (seed, nstruct) pair always gives the same structures. */
+int messi_sample_structures(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired,
+                            int32_t maxspan, int32_t nstruct, uint64_t seed, int32_t* structures);
 /* computestructureintegratedlikelihood without the prior
  * (src/FARCE.jl:2322-2345, with maskgapped! as at src/MESSI.jl:310): unpaired
  * likelihoods, pair pruning, gap masking and the inside pass, all on the
@@ -159,6 +183,30 @@ int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const do
  * pair.  Z: log marginal likelihood.  unpaired: optional [L] output. */
 int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const double* gapfrequency,
                      double gapcutoff, double* Z, double* unpaired);
+
+/* ---- Batches of alignments (no single counterpart in the reference, which
+ * evaluates one alignment per call; this is the batched form of the
+ * felsensteincuda + computeinsideKH99 chain of src/FARCE.jl:2322-2345).
+ * A batch holds the pair plans of n alignments.  messi_batch_likelihood
+ * evaluates messi_likelihood for all of them in one pass: the tree levels of
+ * all alignments are pruned together and all inside passes run in one
+ * persistent launch.  Results equal n separate messi_likelihood calls. */
+typedef struct messi_batch messi_batch;
+/* maxbasepairdistance: [n] per-alignment band (nullable: numcols - 1 each). */
+int messi_batch_create(messi_ctx* ctx, int32_t n, const messi_alignment* alns, const int32_t* maxbasepairdistance,
+                       messi_batch** batch);
+int messi_batch_destroy(messi_batch* batch);
+/* out[0..7]: pairs in band, unique root pairs, executed and naive node
+ * updates per category, deepest tree level, partial-buffer rows per
+ * category, categories per pass, tree nodes (sums over the batch). */
+int messi_batch_stats(messi_batch* batch, int64_t* out, int32_t n);
+/* models: [n], one per alignment (its own branch lengths); models equal in
+ * everything but their branch lengths share their category eigensystems,
+ * and every model must have the same nsite and nlambda.
+ * gapfrequency: nullable, the alignments' [numcols] vectors concatenated in
+ * batch order.  Z: [n] log marginal likelihoods. */
+int messi_batch_likelihood(messi_ctx* ctx, messi_batch* batch, const messi_model* models,
+                           const double* gapfrequency, double gapcutoff, double* Z);
 
 /* ---- Learned MCMC proposal network (HP3; no counterpart in the reference,
  * whose MCMC moves are all hand-tuned random walks, src/MCMC.jl:1307-1674).

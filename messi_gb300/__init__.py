@@ -19,7 +19,9 @@ __version__ = "0.1.0"
 
 _API_NAMES = ("felsensteincuda", "coevolutionall", "computeunpairedlikelihoods", "maskgapped", "computeinsideKH99",
               "computeoutsideKH99", "computebasepairprobs", "computeposteriors",
-              "computestructureintegratedlikelihood", "Context", "get_context")
+              "computestructureintegratedlikelihood", "computestructureintegratedlikelihoods", "Batch", "Context",
+              "get_context", "computeposteriordecodingcuda", "getPosteriorDecodingConsensusStructure",
+              "consensusstructure", "samplestructures")
 
 
 def __getattr__(name):

@@ -275,6 +275,65 @@ def computeposteriors(unpairedlogprobs, pairedlogprobs, maxspan=-1, ctx=None):
 
 
 # ---------------------------------------------------------------------------
+# structures: posterior decoding and sampling
+# ---------------------------------------------------------------------------
+def computeposteriordecodingcuda(singleprobs, pairprobs, alpha=2.0, ctx=None):
+    """src/InsideCUDA.jl:183-215: (ematrix, smatrix) of the maximum expected
+    accuracy recursion (FP32 on the device, as the reference)."""
+    ctx = ctx or get_context()
+    s = _f64c(singleprobs)
+    L = len(s)
+    e = np.empty((L, L), order="F")
+    sm = np.empty((L, L), dtype=np.int32, order="F")
+    ctx.check(ctx.lib.messi_posterior_decoding(ctx.handle, L, _p(s), _p(_f64f(pairprobs)), float(alpha), _p(e),
+                                               _p(sm), None), "messi_posterior_decoding")
+    return e, sm.astype(np.int64)
+
+
+def getPosteriorDecodingConsensusStructure(pairedposteriorprobs, unpairedposteriorprobs, usecuda=True, alpha=2.0,
+                                           ctx=None):
+    """src/RNATools.jl:74-83 (GPU branch): consensus structure as 1-based
+    partners, 0 when unpaired (decoding and traceback on the device)."""
+    _need_cuda(usecuda)
+    ctx = ctx or get_context()
+    s = _f64c(unpairedposteriorprobs)
+    L = len(s)
+    paired = np.empty(L, np.int32)
+    ctx.check(ctx.lib.messi_posterior_decoding(ctx.handle, L, _p(s), _p(_f64f(pairedposteriorprobs)), float(alpha),
+                                               None, None, _p(paired)), "messi_posterior_decoding")
+    return paired.astype(np.int64)
+
+
+def consensusstructure(unpairedlogprobs, pairedlogprobs, maxspan=-1, alpha=2.0, ctx=None):
+    """Scores -> inside -> outside -> posteriors -> posterior decoding ->
+    traceback, device-resident (the --processmax chain, src/MESSI.jl:1101-1103
+    and src/RNATools.jl:74-83).  1-based partners, 0 when unpaired."""
+    ctx = ctx or get_context()
+    u = _f64c(unpairedlogprobs)
+    L = len(u)
+    out = np.empty(L, np.int32)
+    ctx.check(ctx.lib.messi_consensus_structure(ctx.handle, L, _p(u), _p(_f64f(pairedlogprobs)), int(maxspan),
+                                                float(alpha), _p(out)), "messi_consensus_structure")
+    return out.astype(np.int64)
+
+
+def samplestructures(unpairedlogprobs, pairedlogprobs, count, seed=1, maxspan=-1, ctx=None):
+    """samplestructure (src/InsideOutsideAlgorithm.jl:570-635), `count`
+    independent draws on the device.  Returns (structures [count, L] as
+    1-based partners / 0, log KH99 prior of each)."""
+    from .structures import calculateKH99prior
+    ctx = ctx or get_context()
+    u = _f64c(unpairedlogprobs)
+    L = len(u)
+    out = np.empty((int(count), L), np.int32)
+    ctx.check(ctx.lib.messi_sample_structures(ctx.handle, L, _p(u), _p(_f64f(pairedlogprobs)), int(maxspan),
+                                              int(count), int(seed) & 0xFFFFFFFFFFFFFFFF, _p(out)),
+              "messi_sample_structures")
+    priors = np.array([calculateKH99prior(row) for row in out])
+    return out.astype(np.int64), priors
+
+
+# ---------------------------------------------------------------------------
 # the likelihood evaluation of every NLopt / MCMC step
 # ---------------------------------------------------------------------------
 def computestructureintegratedlikelihood(dataset, params, maxbasepairdistance=1000000, samplebranchlengths=False,
@@ -300,6 +359,81 @@ def computestructureintegratedlikelihood(dataset, params, maxbasepairdistance=10
         params.lambdaGT = saved
     total = params.logprior + Z.value
     return (total, Z.value, u) if return_unpaired else total
+
+
+# ---------------------------------------------------------------------------
+# batches of alignments
+# ---------------------------------------------------------------------------
+class Batch:
+    """Pair plans of many alignments evaluated together
+    (include/messi_gb300.h, messi_batch_*): the batched form of
+    computestructureintegratedlikelihood (src/FARCE.jl:2322-2345)."""
+
+    def __init__(self, datasets, maxbasepairdistance=None, ctx=None):
+        self.ctx = ctx or get_context()
+        self.datasets = list(datasets)
+        n = len(self.datasets)
+        self._keep = []
+        alns = (_lib.Alignment * n)()
+        for k, d in enumerate(self.datasets):
+            m = np.ascontiguousarray(d.masks, np.uint8)
+            c = np.ascontiguousarray(d.children, np.int32)
+            si = np.ascontiguousarray(d.seqindex, np.int32)
+            self._keep += [m, c, si]
+            alns[k] = _lib.Alignment(d.numseqs, d.numcols, d.numnodes, _p(m), _p(c), _p(si))
+        W = None
+        if maxbasepairdistance is not None:
+            W = np.empty(n, np.int32)
+            for k, d in enumerate(self.datasets):
+                w = maxbasepairdistance[k] if np.ndim(maxbasepairdistance) else maxbasepairdistance
+                W[k] = int(min(max(1, w), max(1, d.numcols - 1)))
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.messi_batch_create(self.ctx.handle, n, ctypes.cast(alns, ctypes.c_void_p),
+                                                       _p(W), ctypes.byref(h)), "messi_batch_create")
+        self.handle = h
+        self.n = n
+        self._gf = np.ascontiguousarray(np.concatenate([np.asarray(d.gapfrequency, np.float64)
+                                                        for d in self.datasets]))
+
+    def stats(self):
+        out = np.zeros(8, np.int64)
+        self.ctx.check(self.ctx.lib.messi_batch_stats(self.handle, _p(out), 8), "messi_batch_stats")
+        keys = ("band_pairs", "unique_root_pairs", "executed_updates_per_category", "naive_updates_per_category",
+                "levels", "arena_rows", "categories_per_pass", "nodes")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def likelihood(self, params_list, gapcutoff=1.0):
+        """Z of every alignment (no prior).  params_list: one ModelParameters
+        per alignment (its own branch lengths)."""
+        if len(params_list) != self.n:
+            raise ValueError("one parameter set per alignment")
+        margs = [ModelArgs(p) for p in params_list]
+        models = (_lib.Model * self.n)(*[m.struct for m in margs])
+        Z = np.empty(self.n)
+        self.ctx.check(self.ctx.lib.messi_batch_likelihood(self.ctx.handle, self.handle,
+                                                           ctypes.cast(models, ctypes.c_void_p), _p(self._gf),
+                                                           float(gapcutoff), _p(Z)), "messi_batch_likelihood")
+        return Z
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx.lib.messi_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def computestructureintegratedlikelihoods(datasets, params_list, maxbasepairdistance=None, gapcutoff=1.0,
+                                          batch=None, ctx=None):
+    """computestructureintegratedlikelihood for every (dataset, params) pair
+    in one batched evaluation: logprior + Z per alignment."""
+    b = batch or Batch(datasets, maxbasepairdistance, ctx=ctx)
+    Z = b.likelihood(params_list, gapcutoff)
+    return np.array([computeprior(p) + z for p, z in zip(params_list, Z)])
 
 
 # ---------------------------------------------------------------------------

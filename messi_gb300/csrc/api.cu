@@ -103,21 +103,9 @@ static void prof_collect(messi_ctx* ctx)
 namespace {
 
 // Scratch slots (grow-only, per context).  0..14 belong to the band tables.
-enum Slot { kSlotStage = 15, kSlotP16 = 16, kSlotDense = 17, kSlotVec = 18, kSlotTable = 19, kSlotP4 = 21 };
-
-struct Staged {
-    size_t off = 0;
-    std::vector<char> host;
-    template <typename T>
-    size_t add(const T* src, size_t n)
-    {
-        off = (off + 15) & ~size_t(15);
-        size_t at = off;
-        host.resize(off + n * sizeof(T));
-        std::memcpy(host.data() + at, src, n * sizeof(T));
-        off += n * sizeof(T);
-        return at;
-    }
+enum Slot {
+    kSlotStage = 15, kSlotP16 = 16, kSlotDense = 17, kSlotVec = 18, kSlotTable = 19, kSlotP4 = 21,
+    kSlotDecodeF = 22, kSlotDecodeI = 23
 };
 
 struct ModelDev {
@@ -170,13 +158,14 @@ int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool p
         // FP32 matrices followed by their TF32 hi/lo split
         if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * 3 * sizeof(float), &p))) return rc;
         md->P16 = (float*)p;
-        if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, ds->numnodes, c.C, md->P16))) return rc;
+        if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, nullptr, ds->numnodes, c.C, md->P16,
+                                    md->P16 + (size_t)c.C * ds->numnodes * 256))) return rc;
     }
     if (unpaired) {
         void* p;
         if ((rc = ensure(ctx, kSlotP4, (size_t)c.nsite * ds->numnodes * 16 * sizeof(double), &p))) return rc;
         md->P4 = (double*)p;
-        if ((rc = launch_build_P4(ctx, (const double*)(base + o_eig4), d_bl, ds->numnodes, c.nsite, md->P4)))
+        if ((rc = launch_build_P4(ctx, (const double*)(base + o_eig4), d_bl, nullptr, ds->numnodes, c.nsite, md->P4)))
             return rc;
     }
     return MESSI_OK;
@@ -192,6 +181,8 @@ int prepare_arena(messi_ctx* ctx, messi_dataset* ds, int C)
     }
     return MESSI_OK;
 }
+
+}  // namespace
 
 int finish(messi_ctx* ctx)
 {
@@ -254,7 +245,6 @@ int dense_pairs_to_band(messi_ctx* ctx, int L, const double* unpaired, const dou
     return launch_bandprep_from_dense(ctx, *t, d_dense, B);
 }
 
-}  // namespace
 }  // namespace messi
 
 using namespace messi;
@@ -300,8 +290,8 @@ int messi_ctx_create(int device, messi_ctx** out)
     }
     *ctx->status_host = 0u;
     {
-        const char* k = std::getenv("MESSI_PRUNE_KERNEL");
-        if (k && std::strcmp(k, "fma") == 0) ctx->prune_kernel = 1;
+        const char* w = std::getenv("MESSI_WAVE_CTAS");
+        if (w) ctx->wave_ctas = std::max(0, std::atoi(w));
     }
     *out = ctx;
     return MESSI_OK;
@@ -443,7 +433,7 @@ int messi_unpaired(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, 
     if ((rc = upload_model(ctx, ds, model, false, true, nullptr, &md))) return rc;
     void* p;
     if ((rc = ensure(ctx, kSlotVec, (size_t)ds->L * sizeof(double), &p))) return rc;
-    if ((rc = launch_unpaired(ctx, ds, md.P4, md.pi4, md.logw_site, md.cat.nsite, (double*)p))) return rc;
+    if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, (double*)p, nullptr))) return rc;
     if ((rc = d2h(ctx, unpairedlogprobs, p, (size_t)ds->L * sizeof(double)))) return rc;
     return finish(ctx);
 }
@@ -466,7 +456,7 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     Band t;
     const int Wb = std::max(0, std::min(ds->W, ds->L - 1));
     if ((rc = band_alloc(ctx, ds->L, Wb, false, &t))) return rc;
-    if ((rc = launch_unpaired(ctx, ds, md.P4, md.pi4, md.logw_site, md.cat.nsite, t.u))) return rc;
+    if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, t.u, nullptr))) return rc;
     if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
     if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0))) return rc;
     if ((rc = run_inside(ctx, t, 1.0))) return rc;
@@ -538,6 +528,109 @@ int messi_basepairprobs(messi_ctx* ctx, int32_t L, const double* inside, const d
     if ((rc = d2h(ctx, single, ds_single, (size_t)L * sizeof(double)))) return rc;
     if ((rc = d2h(ctx, pairprobs, ds_pair, (size_t)L * L * sizeof(double)))) return rc;
     return finish(ctx);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Posterior decoding of device-resident posteriors; copies the requested
+// outputs to the host buffers (queued on the context stream).
+int decode_device(messi_ctx* ctx, int L, const double* d_single, const double* d_pair, double alpha,
+                  double* ematrix, int32_t* smatrix, int32_t* paired)
+{
+    int rc;
+    void *work, *ints;
+    const size_t LL = (size_t)L * L;
+    if ((rc = ensure(ctx, kSlotDecodeF, ((size_t)L + 3 * LL) * sizeof(float), &work))) return rc;
+    if ((rc = ensure(ctx, kSlotDecodeI, (LL + 3 * (size_t)L + 16) * sizeof(int), &ints))) return rc;
+    int* scol = (int*)ints;
+    int* stack = scol + LL;
+    int* d_paired = stack + 2 * ((size_t)L + 1);
+    unsigned int* sync = (unsigned int*)(d_paired + L);
+    double* eout = nullptr;
+    if (ematrix) {
+        void* q;
+        if ((rc = ensure(ctx, kSlotTable, LL * sizeof(double), &q))) return rc;
+        eout = (double*)q;
+    }
+    if ((rc = run_posterior_decoding(ctx, L, d_single, d_pair, alpha, (float*)work, scol, sync,
+                                     paired ? d_paired : nullptr, stack, eout)))
+        return rc;
+    if (ematrix && (rc = d2h(ctx, ematrix, eout, LL * sizeof(double)))) return rc;
+    if (smatrix && (rc = d2h(ctx, smatrix, scol, LL * sizeof(int32_t)))) return rc;
+    if (paired && (rc = d2h(ctx, paired, d_paired, (size_t)L * sizeof(int32_t)))) return rc;
+    return MESSI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int messi_posterior_decoding(messi_ctx* ctx, int32_t L, const double* singleprobs, const double* pairprobs,
+                             double alpha, double* ematrix, int32_t* smatrix, int32_t* paired)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !singleprobs || !pairprobs || !(std::isfinite(alpha)))
+        return fail(ctx, MESSI_EINVAL, "posterior decoding: bad arguments");
+    if ((size_t)L * L > (size_t)1 << 31) return fail(ctx, MESSI_ETOOBIG, "posterior decoding: L*L above 2^31");
+    void *ds, *dp;
+    if ((rc = ensure(ctx, kSlotVec, (size_t)L * sizeof(double), &ds))) return rc;
+    if ((rc = ensure(ctx, kSlotDense, (size_t)L * L * sizeof(double), &dp))) return rc;
+    if ((rc = h2d(ctx, ds, singleprobs, (size_t)L * sizeof(double)))) return rc;
+    if ((rc = h2d(ctx, dp, pairprobs, (size_t)L * L * sizeof(double)))) return rc;
+    if ((rc = decode_device(ctx, L, (const double*)ds, (const double*)dp, alpha, ematrix, smatrix, paired)))
+        return rc;
+    return finish(ctx);
+}
+
+int messi_consensus_structure(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired,
+                              int32_t maxspan, double alpha, int32_t* structure)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !unpaired || !paired || !structure || !std::isfinite(alpha))
+        return fail(ctx, MESSI_EINVAL, "consensus structure: bad arguments");
+    if ((size_t)L * L > (size_t)1 << 31) return fail(ctx, MESSI_ETOOBIG, "consensus structure: L*L above 2^31");
+    Band t;
+    if ((rc = dense_pairs_to_band(ctx, L, unpaired, paired, maxspan, 1.0, true, &t))) return rc;
+    if ((rc = run_inside(ctx, t, 1.0))) return rc;
+    if ((rc = run_outside(ctx, t, 1.0))) return rc;
+    void *ds_single, *ds_pair;
+    if ((rc = ensure(ctx, kSlotVec, (size_t)L * sizeof(double), &ds_single))) return rc;
+    if ((rc = ensure(ctx, kSlotDense, (size_t)L * L * sizeof(double), &ds_pair))) return rc;
+    if ((rc = run_posteriors(ctx, t, 1.0, (double*)ds_single, (double*)ds_pair))) return rc;
+    if ((rc = decode_device(ctx, L, (const double*)ds_single, (const double*)ds_pair, alpha, nullptr, nullptr,
+                            structure)))
+        return rc;
+    return finish(ctx);
+}
+
+int messi_sample_structures(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired,
+                            int32_t maxspan, int32_t nstruct, uint64_t seed, int32_t* structures)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (L < 1 || !unpaired || !paired || nstruct < 1 || !structures)
+        return fail(ctx, MESSI_EINVAL, "sample structures: bad arguments");
+    Band t;
+    if ((rc = dense_pairs_to_band(ctx, L, unpaired, paired, maxspan, 1.0, false, &t))) return rc;
+    if ((rc = run_inside(ctx, t, 1.0))) return rc;
+    void* ints;
+    const size_t per = (size_t)L + 3 * ((size_t)L + 1);
+    if ((rc = ensure(ctx, kSlotDecodeI, (per * nstruct + 16) * sizeof(int), &ints))) return rc;
+    int* d_out = (int*)ints;
+    int* d_stack = d_out + (size_t)L * nstruct;
+    unsigned int* d_status = (unsigned int*)(d_stack + 3 * ((size_t)L + 1) * nstruct);
+    if ((rc = run_sample_structures(ctx, t, 1.0, nstruct, (unsigned long long)seed, d_out, d_stack, d_status)))
+        return rc;
+    unsigned int status = 0;
+    if ((rc = d2h(ctx, structures, d_out, (size_t)L * nstruct * sizeof(int32_t)))) return rc;
+    if ((rc = d2h(ctx, &status, d_status, sizeof(unsigned int)))) return rc;
+    if ((rc = finish(ctx))) return rc;
+    if (status != 0u) return fail(ctx, MESSI_ESTATE, "sample structures: a span had no derivation (check the inputs)");
+    return MESSI_OK;
 }
 
 int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,

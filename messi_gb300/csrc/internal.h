@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -23,6 +24,22 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// Host staging of several arrays for one host-to-device copy (16-byte aligned).
+struct Staged {
+    size_t off = 0;
+    std::vector<char> host;
+    template <typename T>
+    size_t add(const T* src, size_t n)
+    {
+        off = (off + 15) & ~size_t(15);
+        size_t at = off;
+        host.resize(off + n * sizeof(T));
+        if (n) std::memcpy(host.data() + at, src, n * sizeof(T));
+        off += n * sizeof(T);
+        return at;
+    }
+};
+
 // Per-internal-node descriptor of one pruning step (device resident).
 struct NodeDev {
     const int* li;     // [n] row of the left child for each unique pair
@@ -36,10 +53,12 @@ struct NodeDev {
     float* of;         // output rows (unused at the root)
     int* oe;
     long long ocs;
+    double* mix;       // root only: [n] category mixture per unique root pair
+    double* mixlam;    // root only: [kMaxLambda][n] per-lambda mixtures (nullable)
     int n;             // unique pairs at this node
     int left;          // child node ids (index of their transition matrices)
     int right;
-    int pad;
+    int grp;           // model group (index of the category tables pi16/logw)
 };
 
 // Discretised model categories built on the host for one call.
@@ -65,6 +84,22 @@ struct Band {
     unsigned int* sync;  // grid barrier of the wavefront kernels: count, generation, error flag, spare
 };
 
+// Band tables of a batch of alignments for the batched inside pass.  Bands
+// are kept sorted by band width, descending (band k holds alignment order[k]).
+struct BandBatch {
+    int n = 0;
+    long long total_cols = 0;
+    std::vector<Band> host;
+    std::vector<int> order, slot;  // slot[alignment] = band index
+    Band* d_bands = nullptr;
+    long long* d_cumL = nullptr;   // [n+1] exclusive prefix of the lengths
+    int* d_wbs = nullptr;          // [n] band widths
+    unsigned int* d_sync = nullptr;
+    double* d_Z = nullptr;         // [n] in band order
+    void* mem = nullptr;           // one device allocation holding all of the above
+    size_t bytes = 0;
+};
+
 // Rule log-probabilities times B (index 0..6 = r1..r7).
 struct Rules {
     float r[7];
@@ -83,8 +118,8 @@ constexpr int kProfKernels = 4;
 
 struct messi_ctx {
     int device = 0;
-    // pair node-update kernel: 0 = tensor cores (3xTF32 mma.sync), 1 = FP32 FMA
-    int prune_kernel = 0;
+    // CTAs of the persistent wavefront kernels (0 = one per SM, fewer for short sequences)
+    int wave_ctas = 0;
     // per-kernel event timing (messi_ctx_profile)
     bool profiling = false;
     std::vector<messi::ProfRec> prof_pending;
@@ -148,6 +183,11 @@ int fail(messi_ctx* ctx, int code, const std::string& msg);
 int cuda_fail(messi_ctx* ctx, cudaError_t e, const char* what);
 int ensure(messi_ctx* ctx, int slot, size_t bytes, void** p);
 int ensure_pinned(messi_ctx* ctx, size_t bytes, void** p);
+// Start of every entry point (device, counters) and its end (stream sync, status checks).
+int begin(messi_ctx* ctx);
+int finish(messi_ctx* ctx);
+int h2d(messi_ctx* ctx, void* dst, const void* src, size_t bytes);
+int d2h(messi_ctx* ctx, void* dst, const void* src, size_t bytes);
 // Event pair around one launch of a timed kernel family (no-op unless profiling).
 int prof_begin(messi_ctx* ctx, int kernel, double units);
 void prof_end(messi_ctx* ctx);
@@ -164,14 +204,31 @@ int host_reversible_eig(int n, const double* Q, const double* pi, double* w, dou
 int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8_t* pairmask, std::string* err);
 int allocate_arena(messi_dataset* ds, int C, std::string* err);
 
+// Node descriptors of one dataset whose partial rows live at `arena_f/e` +
+// row_base rows, category stride `cstride` rows; transition matrices of local
+// node v are those of node node_base + v; model group `grp`.
+void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e, int64_t row_base, int64_t cstride,
+                           int node_base, int grp, NodeDev* out);
+
 // ---- pruning kernels (prune.cu) ----
-int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, int numnodes, int C, float* d_P);
-int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, int numnodes, int nsite,
-                    double* d_P4);
+// nodegrp: [numnodes] model group of each node, -1 for a root (nullptr: one
+// tree, root = node 0, group 0).  Category tables are [group][C][...].
+// d_P (nullable): FP32 matrices [C][numnodes][256]; d_PT: their 3xTF32 split
+// [C][numnodes][2][256].
+int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, const int* d_nodegrp, int numnodes,
+                     int C, float* d_P, float* d_PT);
+int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, const int* d_nodegrp, int numnodes,
+                    int nsite, double* d_P4);
+// The tensor-core node update over `nt` tiles of one level (root tiles when root).
+int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
+                       const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
+                       const double* d_logw, const int* d_lam, bool per_lambda);
 int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
               const int* d_lam, int C, int nlam, bool per_lambda);
-int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, const double* d_pi4,
-                    const double* d_logw_site, int nsite, double* d_u);
+// Unpaired column likelihoods of one tree whose transition matrices start at
+// d_P4 with node stride `pstride` (nodes of all site categories: [s][pstride][16]).
+int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int pstride, const double* d_pi4,
+                    const double* d_logw_site, int nsite, double* d_u, double* d_scratch);
 int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, double* d_out);
 int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask,
                              double B);
@@ -189,6 +246,24 @@ int launch_dense_outside(messi_ctx* ctx, const Band& t, double* d_out);
 int launch_band_from_dense_inside(messi_ctx* ctx, const Band& t, const double* d_in);
 int launch_band_from_dense_outside(messi_ctx* ctx, const Band& t, const double* d_out);
 int launch_finish_Z(messi_ctx* ctx, const Band& t);
+// KH99 rule log-probabilities times B.
+Rules make_rules(double B);
+// Posterior decoding (decode.cu).  d_work: (L + 3 L^2) floats; d_scol: L^2
+// ints (the column-major s output); d_sync: 4 uints; d_paired (nullable):
+// [L]; d_stack: 2 (L + 1) ints; d_eout (nullable): L^2 doubles.
+int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const double* d_pair, double alpha,
+                           float* d_work, int* d_scol, unsigned int* d_sync, int* d_paired, int* d_stack,
+                           double* d_eout);
+// Structure sampling through the inside band tables of t (computed with B).
+// d_paired: [nstruct][L]; d_stack: [nstruct][3 (L + 1)] ints; d_status: 1 uint.
+int run_sample_structures(messi_ctx* ctx, const Band& t, double B, int nstruct, unsigned long long seed,
+                          int* d_paired, int* d_stack, unsigned int* d_status);
+// Grid size of a persistent wavefront kernel (cooperative launch, 256 threads).
+int wave_grid(messi_ctx* ctx, const void* kernel, int L);
+int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandBatch* bb, std::string* err);
+void bandbatch_free(BandBatch* bb);
+int launch_baseline_batch(messi_ctx* ctx, const BandBatch& bb, double B);
+int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B);
 // Queue a copy of the wavefront barrier status into ctx->status_host.
 int queue_status_readback(messi_ctx* ctx, const Band& t);
 

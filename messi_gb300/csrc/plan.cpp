@@ -327,6 +327,48 @@ cuda_error:
     return (e == cudaErrorMemoryAllocation) ? MESSI_ENOMEM : MESSI_ECUDA;
 }
 
+void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e, int64_t row_base, int64_t cstride,
+                           int node_base, int grp, NodeDev* out)
+{
+    for (int v = 0; v < ds->numnodes; v++) {
+        NodeDev& d = out[v];
+        d = NodeDev{};
+        if (ds->children[2 * v] < 0) continue;
+        d.n = (int)ds->nunique[v];
+        d.li = ds->d_lr + ds->lr_off[v];
+        d.ri = ds->d_lr + ds->lr_off[v] + ds->nunique[v];
+        const int c0 = ds->children[2 * v], c1 = ds->children[2 * v + 1];
+        d.left = node_base + c0;
+        d.right = node_base + c1;
+        d.grp = grp;
+        for (int side = 0; side < 2; side++) {
+            const int c = side ? c1 : c0;
+            const float* f;
+            const int* ex;
+            long long cs;
+            if (ds->children[2 * c] < 0) {
+                f = ds->d_leaf + (size_t)ds->leaf_off[c] * 16;
+                ex = nullptr;
+                cs = 0;
+            } else {
+                f = arena_f + (size_t)(row_base + ds->row_off[c]) * 16;
+                ex = arena_e + row_base + ds->row_off[c];
+                cs = cstride;
+            }
+            if (side) { d.rf = f; d.re = ex; d.rcs = cs; }
+            else { d.lf = f; d.le = ex; d.lcs = cs; }
+        }
+        if (v != 0) {
+            d.of = arena_f + (size_t)(row_base + ds->row_off[v]) * 16;
+            d.oe = arena_e + row_base + ds->row_off[v];
+            d.ocs = cstride;
+        } else {
+            d.mix = ds->d_mix;
+            d.mixlam = ds->d_mixlam;
+        }
+    }
+}
+
 // Allocate the partial-row arena for C categories (as many per pass as fit)
 // and fill the node descriptors.
 int allocate_arena(messi_dataset* ds, int C, std::string* err)
@@ -351,41 +393,9 @@ int allocate_arena(messi_dataset* ds, int C, std::string* err)
         }
         ds->chunk = chunk;
     }
-    // descriptors
+    ds->nodes_host.assign(ds->numnodes, NodeDev{});
+    fill_node_descriptors(ds, ds->d_arena_f, ds->d_arena_e, 0, ds->arena_rows, 0, 0, ds->nodes_host.data());
     const int nn = ds->numnodes;
-    ds->nodes_host.assign(nn, NodeDev{});
-    for (int v = 0; v < nn; v++) {
-        if (ds->children[2 * v] < 0) continue;
-        NodeDev& d = ds->nodes_host[v];
-        d.n = (int)ds->nunique[v];
-        d.li = ds->d_lr + ds->lr_off[v];
-        d.ri = ds->d_lr + ds->lr_off[v] + ds->nunique[v];
-        int c0 = ds->children[2 * v], c1 = ds->children[2 * v + 1];
-        d.left = c0;
-        d.right = c1;
-        for (int side = 0; side < 2; side++) {
-            int c = side ? c1 : c0;
-            const float* f;
-            const int* ex;
-            long long cs;
-            if (ds->children[2 * c] < 0) {
-                f = ds->d_leaf + (size_t)ds->leaf_off[c] * 16;
-                ex = nullptr;
-                cs = 0;
-            } else {
-                f = ds->d_arena_f + (size_t)ds->row_off[c] * 16;
-                ex = ds->d_arena_e + ds->row_off[c];
-                cs = ds->arena_rows;
-            }
-            if (side) { d.rf = f; d.re = ex; d.rcs = cs; }
-            else { d.lf = f; d.le = ex; d.lcs = cs; }
-        }
-        if (v != 0) {
-            d.of = ds->d_arena_f + (size_t)ds->row_off[v] * 16;
-            d.oe = ds->d_arena_e + ds->row_off[v];
-            d.ocs = ds->arena_rows;
-        }
-    }
     cudaError_t e = cudaMemcpy(ds->d_nodes, ds->nodes_host.data(), sizeof(NodeDev) * nn, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         *err = std::string("node descriptors: ") + cudaGetErrorString(e);

@@ -5,13 +5,14 @@
 // felsensteinhelper16 :153-200, sumfinal :428-442, storearr/logsumexparr
 // :135-151) with:
 //   * build_P16_kernel: P = exp(Qt) per (category, branch) in FP64 from the
-//     host eigensystem, stored as FP32 rows (row = parent state);
-//   * prune_level_kernel: one launch per tree level and category pass; a CTA
-//     owns a tile of unique pairs of one node, stages that node's 2 x C
-//     transition matrices in shared memory, gathers the child rows with
-//     16-byte loads and writes the rescaled node rows.  Rows are rescaled by
-//     an exact power of two (exponent kept as an int), which computes the
-//     same likelihood as the reference's divide-by-max (felsenstein.cu:193-198);
+//     host eigensystem, stored as FP32 rows (row = parent state) and as their
+//     3xTF32 hi/lo split;
+//   * prune_mma_kernel: one launch per tree level and category pass; a warp
+//     owns 32 unique pairs of one node, gathers the child rows with cp.async
+//     (three categories in flight) and does both child mat-vecs on the tensor
+//     cores (3xTF32 mma.sync).  Rows are rescaled by an exact power of two
+//     (exponent kept as an int), which computes the same likelihood as the
+//     reference's divide-by-max (felsenstein.cu:193-198);
 //   * the root variant folds sumfinal and the category log-sum-exp into the
 //     same pass (FP64 log-likelihood reduction).
 // unpaired_kernel restates computeunpairedlikelihoodscat (src/FARCE.jl:742-773)
@@ -32,11 +33,13 @@ __device__ __forceinline__ uint32_t f32_to_tf32(float x)
 
 // P[c][v][a][d] in FP32 and, for the tensor-core pruning kernel, its 3xTF32
 // split PT[c][v][0|1][a][d] = hi, lo with P ~= hi + lo (both TF32 values).
-__global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl, int numnodes,
-                                 float* __restrict__ P, float* __restrict__ PT)
+__global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl,
+                                 const int* __restrict__ nodegrp, int numnodes, int C, float* __restrict__ P,
+                                 float* __restrict__ PT)
 {
     const int v = blockIdx.x, c = blockIdx.y, t = threadIdx.x;
-    const double* e = eig + (size_t)c * kEigStride;
+    const int grp = nodegrp ? nodegrp[v] : (v == 0 ? -1 : 0);
+    const double* e = eig + ((size_t)max(grp, 0) * C + c) * kEigStride;
     __shared__ double ex[16], U[256], sp[16];
     const double tl = bl[v];
     U[t] = e[16 + t];
@@ -47,8 +50,8 @@ __global__ void build_P16_kernel(const double* __restrict__ eig, const double* _
     __syncthreads();
     const int a = t >> 4, d = t & 15;
     float out;
-    if (v == 0) {
-        out = 0.f;  // the root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
+    if (grp < 0) {
+        out = 0.f;  // a root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
     } else if (tl == 0.0) {
         out = (a == d) ? 1.f : 0.f;
     } else {
@@ -58,22 +61,23 @@ __global__ void build_P16_kernel(const double* __restrict__ eig, const double* _
         s *= sp[d] / sp[a];
         out = (s <= 0.0) ? 0.f : (float)s;  // absmat clamp (1e-50 rounds to 0 in FP32)
     }
-    P[((size_t)c * numnodes + v) * 256 + t] = out;
+    if (P) P[((size_t)c * numnodes + v) * 256 + t] = out;
     const uint32_t hi = f32_to_tf32(out);
     const uint32_t lo = f32_to_tf32(out - __uint_as_float(hi));
     PT[(((size_t)c * numnodes + v) * 2 + 0) * 256 + t] = __uint_as_float(hi);
     PT[(((size_t)c * numnodes + v) * 2 + 1) * 256 + t] = __uint_as_float(lo);
 }
 
-__global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl, int numnodes,
-                                double* __restrict__ P4)
+__global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl,
+                                const int* __restrict__ nodegrp, int numnodes, int nsite, double* __restrict__ P4)
 {
     const int v = blockIdx.x, s = blockIdx.y, t = threadIdx.x;  // 16 threads
-    const double* e = eig4 + (size_t)s * kEig4Stride;
+    const int grp = nodegrp ? nodegrp[v] : (v == 0 ? -1 : 0);
+    const double* e = eig4 + ((size_t)max(grp, 0) * nsite + s) * kEig4Stride;
     const double tl = bl[v];
     const int a = t >> 2, d = t & 3;
     double out;
-    if (v == 0) {
+    if (grp < 0) {
         out = 0.0;
     } else if (tl == 0.0) {
         out = (a == d) ? 1.0 : 0.0;
@@ -86,18 +90,18 @@ __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* _
     P4[((size_t)s * numnodes + v) * 16 + t] = out;
 }
 
-int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, int numnodes, int C, float* d_P)
+int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, const int* d_nodegrp, int numnodes,
+                     int C, float* d_P, float* d_PT)
 {
-    // d_P holds C*numnodes*256 FP32 values followed by the hi/lo split
-    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, numnodes, d_P,
-                                                                  d_P + (size_t)C * numnodes * 256);
+    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, d_nodegrp, numnodes, C, d_P, d_PT);
     LAUNCH_CHECK(ctx, "build_P16_kernel");
     return MESSI_OK;
 }
 
-int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, int numnodes, int nsite, double* d_P4)
+int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, const int* d_nodegrp, int numnodes,
+                    int nsite, double* d_P4)
 {
-    build_P4_kernel<<<dim3(numnodes, nsite), 16, 0, ctx->stream>>>(d_eig4, d_bl, numnodes, d_P4);
+    build_P4_kernel<<<dim3(numnodes, nsite), 16, 0, ctx->stream>>>(d_eig4, d_bl, d_nodegrp, numnodes, nsite, d_P4);
     LAUNCH_CHECK(ctx, "build_P4_kernel");
     return MESSI_OK;
 }
@@ -110,129 +114,6 @@ __device__ __forceinline__ double lse_d(double a, double b)
     if (a == -INFINITY) return b;
     return (a < b) ? b + log1p(exp(a - b)) : a + log1p(exp(b - a));
 }
-
-// One tree level, one pass over categories [c0, c0 + nc).
-template <bool ROOT>
-__global__ void __launch_bounds__(kTile) prune_level_kernel(
-    const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ P, int numnodes,
-    int c0, int nc, const float* __restrict__ pi16, const double* __restrict__ logw, const int* __restrict__ lam,
-    double* __restrict__ mix, double* __restrict__ mixlam, int nroot, int per_lambda)
-{
-    extern __shared__ float4 smem4[];
-    const float* sP = reinterpret_cast<const float*>(smem4);  // [nc][2][256]
-    const int2 tile = tiles[blockIdx.x];
-    const NodeDev& nd = nodes[tile.x];
-    const int left = nd.left, right = nd.right, n = nd.n;
-    for (int idx = threadIdx.x; idx < nc * 128; idx += blockDim.x) {
-        const int cc = idx >> 7, r = idx & 127;
-        const int node = (r >> 6) ? right : left;
-        smem4[idx] = __ldg(reinterpret_cast<const float4*>(P + ((size_t)(c0 + cc) * numnodes + node) * 256) + (r & 63));
-    }
-    float* sPi = reinterpret_cast<float*>(smem4 + nc * 128);  // [nc][16] (root only)
-    if (ROOT)
-        for (int idx = threadIdx.x; idx < nc * 16; idx += blockDim.x) sPi[idx] = pi16[(size_t)c0 * 16 + idx];
-    __syncthreads();
-    const int u = tile.y + threadIdx.x;
-    if (u >= n) return;
-    const int l = __ldg(nd.li + u), r = __ldg(nd.ri + u);
-    const float* lf = nd.lf;
-    const float* rf = nd.rf;
-    const int* le = nd.le;
-    const int* re = nd.re;
-    const long long lcs = nd.lcs, rcs = nd.rcs;
-
-    double mm = -INFINITY;  // root: running max of logw + loglik (FP64)
-    float ss = 0.f;         // root: running sum of exp(term - max)
-    double lm[kMaxLambda];
-    float ls[kMaxLambda];
-    if (ROOT) {
-#pragma unroll
-        for (int k = 0; k < kMaxLambda; k++) { lm[k] = -INFINITY; ls[k] = 0.f; }
-    }
-    for (int cc = 0; cc < nc; cc++) {
-        const float* lrow = lf + ((size_t)cc * lcs + l) * 16;
-        const float* rrow = rf + ((size_t)cc * rcs + r) * 16;
-        float4 Lv[4], Rv[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            Lv[q] = ldg4(lrow + 4 * q);
-            Rv[q] = ldg4(rrow + 4 * q);
-        }
-        int e = (le ? __ldg(le + (size_t)cc * lcs + l) : 0) + (re ? __ldg(re + (size_t)cc * rcs + r) : 0);
-        const float4* pl = reinterpret_cast<const float4*>(sP + cc * 512);
-        const float4* pr = pl + 64;
-        float v[16];
-#pragma unroll
-        for (int a = 0; a < 16; a++) {
-            float sl = 0.f, sr = 0.f;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float4 x = pl[a * 4 + q];
-                const float4 y = pr[a * 4 + q];
-                sl = fmaf(x.x, Lv[q].x, sl);
-                sl = fmaf(x.y, Lv[q].y, sl);
-                sl = fmaf(x.z, Lv[q].z, sl);
-                sl = fmaf(x.w, Lv[q].w, sl);
-                sr = fmaf(y.x, Rv[q].x, sr);
-                sr = fmaf(y.y, Rv[q].y, sr);
-                sr = fmaf(y.z, Rv[q].z, sr);
-                sr = fmaf(y.w, Rv[q].w, sr);
-            }
-            v[a] = sl * sr;
-        }
-        if (ROOT) {
-            float dot = 0.f;
-#pragma unroll
-            for (int a = 0; a < 16; a++) dot = fmaf(sPi[cc * 16 + a], v[a], dot);
-            const double ll = (dot > 0.f) ? (double)logf(dot) + (double)e * 0.69314718055994530942 : -INFINITY;
-            const double t = __ldg(logw + c0 + cc) + ll;
-            if (t > mm) {
-                ss = ss * __expf((float)(mm - t)) + 1.f;
-                mm = t;
-            } else if (t != -INFINITY) {
-                ss += __expf((float)(t - mm));
-            }
-            if (per_lambda) {
-                const int k = __ldg(lam + c0 + cc);
-#pragma unroll
-                for (int q = 0; q < kMaxLambda; q++)
-                    if (q == k) {
-                        if (t > lm[q]) {
-                            ls[q] = ls[q] * __expf((float)(lm[q] - t)) + 1.f;
-                            lm[q] = t;
-                        } else if (t != -INFINITY) {
-                            ls[q] += __expf((float)(t - lm[q]));
-                        }
-                    }
-            }
-        } else {
-            float m = 0.f;
-#pragma unroll
-            for (int a = 0; a < 16; a++) m = fmaxf(m, v[a]);
-            int ex = 0;
-            if (m > 0.f) frexpf(m, &ex);
-            const float sc = ldexpf(1.f, -ex);
-            float4* o = reinterpret_cast<float4*>(nd.of + ((size_t)cc * nd.ocs + u) * 16);
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                o[q] = make_float4(v[4 * q] * sc, v[4 * q + 1] * sc, v[4 * q + 2] * sc, v[4 * q + 3] * sc);
-            nd.oe[(size_t)cc * nd.ocs + u] = e + ex;
-        }
-    }
-    if (ROOT) {
-        const double res = (mm == -INFINITY) ? -INFINITY : mm + log((double)ss);
-        mix[u] = (c0 == 0) ? res : lse_d(mix[u], res);
-        if (per_lambda) {
-#pragma unroll
-            for (int q = 0; q < kMaxLambda; q++) {
-                const double rq = (lm[q] == -INFINITY) ? -INFINITY : lm[q] + log((double)ls[q]);
-                double* dst = mixlam + (size_t)q * nroot + u;
-                *dst = (c0 == 0) ? rq : lse_d(*dst, rq);
-            }
-        }
-    }
-}
-
 
 // ---------------------------------------------------------------------------
 // Tensor-core node update (3xTF32 mma.sync).  A warp owns 32 unique pairs of
@@ -333,8 +214,8 @@ struct WarpStage {
 template <bool ROOT>
 __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ PT, int numnodes,
-    int c0, int nc, const float* __restrict__ pi16, const double* __restrict__ logw, const int* __restrict__ lam,
-    double* __restrict__ mix, double* __restrict__ mixlam, int nroot, int per_lambda)
+    int c0, int nc, int C, const float* __restrict__ pi16, const double* __restrict__ logw,
+    const int* __restrict__ lam, int per_lambda)
 {
     extern __shared__ float4 smem_raw[];
     const int2 tile = tiles[blockIdx.x];
@@ -432,7 +313,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
             V[k][3] = DL[mt][1][2 * h + 1] * DR[mt][1][2 * h + 1];
         }
         if (ROOT) {
-            const float* pc = pi16 + (size_t)(c0 + cc) * 16;
+            const float* pc = pi16 + ((size_t)nd.grp * C + c0 + cc) * 16;
             const float p0 = __ldg(pc + 2 * t), p1 = __ldg(pc + 2 * t + 1), p2 = __ldg(pc + 8 + 2 * t),
                         p3 = __ldg(pc + 9 + 2 * t);
             float dots[4];
@@ -445,7 +326,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
             }
             const float dot = dots[0] * (t == 0) + dots[1] * (t == 1) + dots[2] * (t == 2) + dots[3] * (t == 3);
             const double ll = (dot > 0.f) ? (double)logf(dot) + (double)e * 0.69314718055994530942 : -INFINITY;
-            const double tt = __ldg(logw + c0 + cc) + ll;
+            const double tt = __ldg(logw + (size_t)nd.grp * C + c0 + cc) + ll;
             if (tt > mm) {
                 ss = ss * __expf((float)(mm - tt)) + 1.f;
                 mm = tt;
@@ -492,16 +373,40 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     cp_async_wait<0>();
     if (ROOT && myvalid) {
         const double res = (mm == -INFINITY) ? -INFINITY : mm + log((double)ss);
-        mix[myu] = (c0 == 0) ? res : lse_d(mix[myu], res);
+        nd.mix[myu] = (c0 == 0) ? res : lse_d(nd.mix[myu], res);
         if (per_lambda) {
 #pragma unroll
             for (int q = 0; q < kMaxLambda; q++) {
                 const double rq = (lm[q] == -INFINITY) ? -INFINITY : lm[q] + log((double)ls[q]);
-                double* dst = mixlam + (size_t)q * nroot + myu;
+                double* dst = nd.mixlam + (size_t)q * n + myu;
                 *dst = (c0 == 0) ? rq : lse_d(*dst, rq);
             }
         }
     }
+}
+
+int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
+                       const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
+                       const double* d_logw, const int* d_lam, bool per_lambda)
+{
+    static thread_local int smem_set_device = -1;
+    const size_t smem = (size_t)(kTile / 32) * kStages * sizeof(WarpStage);
+    if (smem_set_device != ctx->device) {
+        cudaFuncSetAttribute(prune_mma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(prune_mma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        smem_set_device = ctx->device;
+    }
+    if (nt <= 0) return MESSI_OK;
+    if (root) {
+        prune_mma_kernel<true><<<nt, kTile, smem, ctx->stream>>>(d_nodes, d_tiles, d_PT, numnodes, c0, nc, C, d_pi16,
+                                                                 d_logw, d_lam, per_lambda ? 1 : 0);
+        LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
+    } else {
+        prune_mma_kernel<false><<<nt, kTile, smem, ctx->stream>>>(d_nodes, d_tiles, d_PT, numnodes, c0, nc, C,
+                                                                  d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
+        LAUNCH_CHECK(ctx, "prune_mma_kernel");
+    }
+    return MESSI_OK;
 }
 
 int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
@@ -510,67 +415,19 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
     (void)nlam;
     const int chunk = ds->chunk;
     const float* d_PT = d_P + (size_t)C * ds->numnodes * 256;
-    if (ctx->prune_kernel == 0) {
-        const size_t smem = (size_t)(kTile / 32) * kStages * sizeof(WarpStage);
-        cudaFuncSetAttribute(prune_mma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(prune_mma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        for (int c0 = 0; c0 < C; c0 += chunk) {
-            const int nc = std::min(chunk, C - c0);
-            for (int lv = 1; lv <= ds->H; lv++) {
-                const int nt = ds->tile_cnt[lv];
-                if (nt == 0) continue;
-                const int2* tiles = ds->d_tiles + ds->tile_off[lv];
-                if (ctx->profiling) {
-                    double units = 0.0;
-                    for (int v : ds->level_nodes[lv]) units += (double)ds->nunique[v] * nc;
-                    prof_begin(ctx, 0, units);
-                }
-                if (lv < ds->H) {
-                    prune_mma_kernel<false><<<nt, kTile, smem, ctx->stream>>>(
-                        ds->d_nodes, tiles, d_PT, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix,
-                        ds->d_mixlam, (int)ds->nroot, per_lambda ? 1 : 0);
-                    LAUNCH_CHECK(ctx, "prune_mma_kernel");
-                } else {
-                    prune_mma_kernel<true><<<nt, kTile, smem, ctx->stream>>>(
-                        ds->d_nodes, tiles, d_PT, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix,
-                        ds->d_mixlam, (int)ds->nroot, per_lambda ? 1 : 0);
-                    LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
-                }
-                prof_end(ctx);
-            }
-        }
-        return MESSI_OK;
-    }
-    const size_t smem_max = (size_t)chunk * (128 * sizeof(float4) + 16 * sizeof(float));
-    if (smem_max > 227 * 1024) return fail(ctx, MESSI_EINVAL, "category pass does not fit in shared memory");
-    if (smem_max > 48 * 1024) {
-        cudaFuncSetAttribute(prune_level_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-        cudaFuncSetAttribute(prune_level_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    }
     for (int c0 = 0; c0 < C; c0 += chunk) {
         const int nc = std::min(chunk, C - c0);
         for (int lv = 1; lv <= ds->H; lv++) {
             const int nt = ds->tile_cnt[lv];
             if (nt == 0) continue;
-            const int2* tiles = ds->d_tiles + ds->tile_off[lv];
             if (ctx->profiling) {
                 double units = 0.0;
                 for (int v : ds->level_nodes[lv]) units += (double)ds->nunique[v] * nc;
                 prof_begin(ctx, 0, units);
             }
-            if (lv < ds->H) {
-                const size_t smem = (size_t)nc * 128 * sizeof(float4);
-                prune_level_kernel<false><<<nt, kTile, smem, ctx->stream>>>(
-                    ds->d_nodes, tiles, d_P, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix, ds->d_mixlam,
-                    (int)ds->nroot, per_lambda ? 1 : 0);
-                LAUNCH_CHECK(ctx, "prune_level_kernel");
-            } else {
-                const size_t smem = (size_t)nc * (128 * sizeof(float4) + 16 * sizeof(float));
-                prune_level_kernel<true><<<nt, kTile, smem, ctx->stream>>>(
-                    ds->d_nodes, tiles, d_P, ds->numnodes, c0, nc, d_pi16, d_logw, d_lam, ds->d_mix, ds->d_mixlam,
-                    (int)ds->nroot, per_lambda ? 1 : 0);
-                LAUNCH_CHECK(ctx, "prune_level_kernel<root>");
-            }
+            int rc = launch_prune_tiles(ctx, ds->d_nodes, ds->d_tiles + ds->tile_off[lv], nt, lv == ds->H, d_PT,
+                                        ds->numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda);
+            if (rc) return rc;
             prof_end(ctx);
         }
     }
@@ -583,14 +440,15 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
 // ---------------------------------------------------------------------------
 __global__ void unpaired_kernel(const uint8_t* __restrict__ masks, const int* __restrict__ tree,
                                 const int* __restrict__ post, int nn, int L, const double* __restrict__ P4,
-                                const double* __restrict__ pi4, const double* __restrict__ logw_site, int nsite,
-                                double* __restrict__ part, double* __restrict__ lmv, double* __restrict__ u)
+                                int pstride, const double* __restrict__ pi4, const double* __restrict__ logw_site,
+                                int nsite, double* __restrict__ part, double* __restrict__ lmv,
+                                double* __restrict__ u)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= L) return;
     double acc = -INFINITY;
     for (int s = 0; s < nsite; s++) {
-        const double* Ps = P4 + (size_t)s * nn * 16;
+        const double* Ps = P4 + (size_t)s * pstride * 16;
         for (int t = 0; t < nn; t++) {
             const int v = post[t];
             const int c0 = tree[4 * v], c1 = tree[4 * v + 1];
@@ -640,19 +498,23 @@ __global__ void unpaired_kernel(const uint8_t* __restrict__ masks, const int* __
     u[x] = acc;
 }
 
-int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, const double* d_pi4,
-                    const double* d_logw_site, int nsite, double* d_u)
+int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int pstride, const double* d_pi4,
+                    const double* d_logw_site, int nsite, double* d_u, double* d_scratch)
 {
-    void* scratch;
+    // d_scratch: numnodes * L * 5 doubles, or nullptr for the context's buffer
     const size_t n = (size_t)ds->numnodes * ds->L;
-    int rc = ensure(ctx, 20, n * 5 * sizeof(double), &scratch);
-    if (rc) return rc;
-    double* part = (double*)scratch;
+    if (!d_scratch) {
+        void* scratch;
+        int rc = ensure(ctx, 20, n * 5 * sizeof(double), &scratch);
+        if (rc) return rc;
+        d_scratch = (double*)scratch;
+    }
+    double* part = d_scratch;
     double* lmv = part + n * 4;
     const int bs = 128;
     unpaired_kernel<<<(ds->L + bs - 1) / bs, bs, 0, ctx->stream>>>(ds->d_masks, ds->d_tree, ds->d_post,
-                                                                   ds->numnodes, ds->L, d_P4, d_pi4, d_logw_site,
-                                                                   nsite, part, lmv, d_u);
+                                                                   ds->numnodes, ds->L, d_P4, pstride, d_pi4,
+                                                                   d_logw_site, nsite, part, lmv, d_u);
     LAUNCH_CHECK(ctx, "unpaired_kernel");
     return MESSI_OK;
 }

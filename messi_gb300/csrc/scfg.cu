@@ -38,6 +38,7 @@
 #include <cmath>
 
 #include "internal.h"
+#include "wave.cuh"
 
 namespace messi {
 
@@ -139,7 +140,7 @@ int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
     return MESSI_OK;
 }
 
-static Rules make_rules(double B)
+Rules make_rules(double B)
 {
     static const double p[7] = {0.868534, 0.117609877998, 0.013856122002, 0.787640, 0.21236, 0.894603, 0.105397};
     Rules r;
@@ -152,8 +153,8 @@ static double baseline_c() { return std::log(0.868534) + std::log(0.894603); }
 // ---------------------------------------------------------------------------
 // baseline b_k and prefix sums cb (one block, deterministic FP64 scan)
 // ---------------------------------------------------------------------------
-__global__ void baseline_kernel(const double* __restrict__ u, int L, double B, double c, double* __restrict__ b,
-                                double* __restrict__ cb)
+__device__ void baseline_body(const double* __restrict__ u, int L, double B, double c, double* __restrict__ b,
+                              double* __restrict__ cb)
 {
     __shared__ double part[1024];
     const int t = threadIdx.x, nt = blockDim.x;
@@ -180,6 +181,19 @@ __global__ void baseline_kernel(const double* __restrict__ u, int L, double B, d
         run += b[k];
     }
     if (t == nt - 1) cb[L] = part[nt - 1];
+}
+
+__global__ void baseline_kernel(const double* __restrict__ u, int L, double B, double c, double* __restrict__ b,
+                                double* __restrict__ cb)
+{
+    baseline_body(u, L, B, c, b, cb);
+}
+
+// one block per alignment of a batch
+__global__ void baseline_batch_kernel(const Band* __restrict__ bands, double B, double c)
+{
+    const Band t = bands[blockIdx.x];
+    baseline_body(t.u, t.L, B, c, t.b, t.cb);
 }
 
 int launch_baseline(messi_ctx* ctx, const Band& t, double B)
@@ -264,7 +278,7 @@ int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_de
 // ---------------------------------------------------------------------------
 // Ssuf[i] for spans beyond the band (i < T = L-1-Wb), descending i:
 // Ssuf[i] = r1 + LSE_{k=0..Wb} (Lrow[i][k] + Ssuf[i+k+1]).
-__global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R)
+__device__ void inside_suffix_body(const Band& t, const Rules& R)
 {
     const int T = t.L - 1 - t.Wb;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -303,10 +317,28 @@ __global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R)
     }
 }
 
+__global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R) { inside_suffix_body(t, R); }
+
+// one block per alignment of a batch (alignments whose band reaches the last column skip)
+__global__ void __launch_bounds__(1024) inside_suffix_batch_kernel(const Band* __restrict__ bands, Rules R)
+{
+    const Band t = bands[blockIdx.x];
+    if (t.L - 1 > t.Wb) inside_suffix_body(t, R);
+}
+
 __global__ void finish_Z_kernel(Band t)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0)
         t.Zd[0] = (t.sync[2] != 0u) ? (double)NAN : (double)t.Ssuf[0] + t.cb[t.L];
+}
+
+__global__ void finish_Z_batch_kernel(const Band* __restrict__ bands, int n, const unsigned int* __restrict__ sync,
+                                      double* __restrict__ Z)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const Band& t = bands[b];
+    Z[b] = (sync[2] != 0u) ? (double)NAN : (double)t.Ssuf[0] + t.cb[t.L];
 }
 
 int launch_finish_Z(messi_ctx* ctx, const Band& t)
@@ -317,59 +349,6 @@ int launch_finish_Z(messi_ctx* ctx, const Band& t)
 }
 
 
-// ---------------------------------------------------------------------------
-// grid barrier with a bounded wait (wavefront kernels)
-// ---------------------------------------------------------------------------
-constexpr unsigned int kSpinLimit = 1u << 22;  // x ~64-200 ns per spin: well under a second
-
-__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
-{
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// sync[0] = arrivals, sync[1] = generation, sync[2] = error flag.  Returns
-// false (in every thread of the CTA) once any CTA has given up waiting.
-// Cells written by other CTAs before the barrier are read with __ldcg (L2,
-// coherent across SMs): the per-SM L1 may hold stale lines of those tables.
-__device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
-{
-    __shared__ int s_ok;
-    __threadfence();  // every thread publishes its cells device-wide
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        const unsigned int target = gen + 1;
-        __threadfence();
-        if (atomicAdd(&sync[0], 1u) == gridDim.x - 1) {
-            atomicExch(&sync[0], 0u);
-            __threadfence();
-            atomicExch(&sync[1], target);
-        } else {
-            unsigned int spins = 0;
-            while (ld_acquire_u32(&sync[1]) != target) {
-                if (ld_acquire_u32(&sync[2]) != 0u || ++spins > kSpinLimit) {
-                    atomicExch(&sync[2], 1u);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        gen = target;
-        s_ok = ok && (ld_acquire_u32(&sync[2]) == 0u);
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-__device__ __forceinline__ int group_width(int nterms)
-{
-    return nterms <= 8 ? 1 : (nterms <= 32 ? 4 : (nterms <= 96 ? 8 : (nterms <= 256 ? 16 : 32)));
-}
-
 __device__ __forceinline__ void group_reduce_rt(float& m, float& s, int G)
 {
     for (int off = G >> 1; off > 0; off >>= 1) {
@@ -379,23 +358,66 @@ __device__ __forceinline__ void group_reduce_rt(float& m, float& s, int G)
     }
 }
 
+// Span-0 cells of row i.
+__device__ __forceinline__ void inside_init_cell(const Band& t, int i, const Rules& R, double B)
+{
+    const double ui = t.u[i];
+    const float S = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[1] - t.b[i]);
+    const float Lv = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[5] - t.b[i]);
+    const size_t o = (size_t)i * t.RS;
+    t.Srow[o] = S;
+    t.Scol[o] = S;
+    t.Lrow[o] = Lv;
+    t.Lcol[o] = Lv;
+    t.Frow[o] = -INFINITY;
+    if (i == t.L - 1) t.Ssuf[i] = S;
+}
+
+// Cell (i, i+d) by a group of G lanes (every lane of the warp calls this,
+// `valid` false for padding groups: the shuffles need the whole warp).
+__device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool valid, int lane, int G, const Rules& R)
+{
+    const int RS = t.RS;
+    float m = -INFINITY, s = 0.f;
+    // pair score and enclosed F (two diagonals back) issued before the split sum
+    float pbv = -INFINITY, fin = -INFINITY;
+    if (valid && lane == 0 && d >= 2) {
+        pbv = t.pb[(size_t)i * RS + d];
+        fin = __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2));
+    }
+    if (valid) {
+        const float* lrow = t.Lrow + (size_t)i * RS;
+        const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
+        int k = lane;
+        for (; k + 3 * G < d; k += 4 * G)
+            lse_add4(m, s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
+                     __ldcg(lrow + k + 2 * G) + __ldcg(scol - k - 2 * G),
+                     __ldcg(lrow + k + 3 * G) + __ldcg(scol - k - 3 * G));
+        for (; k < d; k += G) lse_add(m, s, __ldcg(lrow + k) + __ldcg(scol - k));
+    }
+    group_reduce_rt(m, s, G);
+    if (valid && lane == 0) {
+        const int j = i + d;
+        const float tmp = lse_val(m, s);
+        const float v = pbv + fin;
+        const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
+        const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
+        const float Lv = R.r[6] + v;
+        t.Lrow[(size_t)i * RS + d] = Lv;
+        t.Lcol[(size_t)j * RS + d] = Lv;
+        t.Srow[(size_t)i * RS + d] = S;
+        t.Scol[(size_t)j * RS + d] = S;
+        t.Frow[(size_t)i * RS + d] = F;
+        if (j == t.L - 1) t.Ssuf[i] = S;
+    }
+}
+
 // All band diagonals of the inside pass (span 0 initialisation included).
 __global__ void __launch_bounds__(256) inside_wave_kernel(Band t, Rules R, double B)
 {
     unsigned int gen = 0;
-    const int L = t.L, RS = t.RS;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
-        const double ui = t.u[i];
-        const float S = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[1] - t.b[i]);
-        const float Lv = (ui == -INFINITY) ? -INFINITY : (float)(B * ui + (double)R.r[5] - t.b[i]);
-        const size_t o = (size_t)i * RS;
-        t.Srow[o] = S;
-        t.Scol[o] = S;
-        t.Lrow[o] = Lv;
-        t.Lcol[o] = Lv;
-        t.Frow[o] = -INFINITY;
-        if (i == L - 1) t.Ssuf[i] = S;
-    }
+    const int L = t.L;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
     if (!grid_sync(t.sync, gen)) return;
     for (int d = 1; d <= t.Wb; d++) {
         const int G = group_width(d);
@@ -406,35 +428,70 @@ __global__ void __launch_bounds__(256) inside_wave_kernel(Band t, Rules R, doubl
         const int ncell = L - d;
         for (int base = 0; base < ncell; base += total) {
             const int i = base + gid0;
-            const bool valid = i < ncell;
-            float m = -INFINITY, s = 0.f;
-            if (valid) {
-                const float* lrow = t.Lrow + (size_t)i * RS;
-                const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
-                int k = lane;
-                for (; k + 3 * G < d; k += 4 * G)
-                    lse_add4(m, s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
-                             __ldcg(lrow + k + 2 * G) + __ldcg(scol - k - 2 * G),
-                             __ldcg(lrow + k + 3 * G) + __ldcg(scol - k - 3 * G));
-                for (; k < d; k += G) lse_add(m, s, __ldcg(lrow + k) + __ldcg(scol - k));
-            }
-            group_reduce_rt(m, s, G);
-            if (valid && lane == 0) {
-                const int j = i + d;
-                const float tmp = lse_val(m, s);
-                const float v = (d >= 2) ? t.pb[(size_t)i * RS + d] + __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2)) : -INFINITY;
-                const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
-                const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
-                const float Lv = R.r[6] + v;
-                t.Lrow[(size_t)i * RS + d] = Lv;
-                t.Lcol[(size_t)j * RS + d] = Lv;
-                t.Srow[(size_t)i * RS + d] = S;
-                t.Scol[(size_t)j * RS + d] = S;
-                t.Frow[(size_t)i * RS + d] = F;
-                if (j == L - 1) t.Ssuf[i] = S;
-            }
+            inside_cell(t, i, d, i < ncell, lane, G, R);
         }
         if (!grid_sync(t.sync, gen)) return;
+    }
+}
+
+// Batched inside over n alignments in one persistent launch: diagonal d of
+// every alignment whose band reaches it is one step of the wavefront.  Bands
+// are sorted by band width, descending, so the alignments active at span d
+// are a prefix [0, nact) and the cells of diagonal d, flattened in band order,
+// start at cumL[b] - d*b for band b (cumL: exclusive prefix of the lengths).
+__device__ __forceinline__ int batch_active(const int* __restrict__ wbs, int n, int d)
+{
+    int lo = 0, hi = n;  // first band with Wb < d
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (wbs[mid] >= d) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int batch_band(const long long* __restrict__ cumL, int nact, int d, long long item)
+{
+    int lo = 0, hi = nact - 1;  // last band b with cumL[b] - d*b <= item
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cumL[mid] - (long long)d * mid <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) inside_wave_batch_kernel(const Band* __restrict__ bands,
+                                                                const long long* __restrict__ cumL,
+                                                                const int* __restrict__ wbs, int n, Rules R,
+                                                                double B, unsigned int* sync)
+{
+    unsigned int gen = 0;
+    {
+        const long long total = cumL[n];
+        for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
+             it += (long long)gridDim.x * blockDim.x) {
+            const int b = batch_band(cumL, n, 0, it);
+            inside_init_cell(bands[b], (int)(it - cumL[b]), R, B);
+        }
+    }
+    if (!grid_sync(sync, gen)) return;
+    const int maxW = n > 0 ? wbs[0] : 0;
+    for (int d = 1; d <= maxW; d++) {
+        const int nact = batch_active(wbs, n, d);
+        const long long ncell = cumL[nact] - (long long)d * nact;
+        const int G = group_width(d);
+        const int gpb = blockDim.x / G;
+        const long long total = (long long)gridDim.x * gpb;
+        const int lane = threadIdx.x & (G - 1);
+        const long long gid0 = (long long)blockIdx.x * gpb + threadIdx.x / G;
+        for (long long base = 0; base < ncell; base += total) {
+            const long long it = base + gid0;
+            const bool valid = it < ncell;
+            const int b = valid ? batch_band(cumL, nact, d, it) : 0;
+            inside_cell(bands[b], valid ? (int)(it - (cumL[b] - (long long)d * b)) : 0, d, valid, lane, G, R);
+        }
+        if (!grid_sync(sync, gen)) return;
     }
 }
 
@@ -527,7 +584,7 @@ __global__ void __launch_bounds__(256) outside_wave_kernel(Band t, Rules R)
     }
 }
 
-static int wave_grid(messi_ctx* ctx, const void* kernel, int L)
+int wave_grid(messi_ctx* ctx, const void* kernel, int L)
 {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1)
@@ -539,9 +596,11 @@ static int wave_grid(messi_ctx* ctx, const void* kernel, int L)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         ctx->num_sms = sms;
     }
-    // one CTA per SM keeps the barrier cheap; more only when a diagonal needs it
+    // one CTA per SM at most keeps the barrier cheap; a context may cap it lower
     const int useful = (int)std::min<long long>((long long)L * 32 / 256 + 1, (long long)per_sm * sms);
-    return std::max(1, std::min(useful, sms));
+    int grid = std::max(1, std::min(useful, sms));
+    if (ctx->wave_ctas > 0) grid = std::min(grid, ctx->wave_ctas);
+    return grid;
 }
 
 static int launch_wave(messi_ctx* ctx, const void* kernel, int grid, void** args, const Band& t, const char* what)
@@ -580,6 +639,144 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
         prof_end(ctx);
     }
     return launch_finish_Z(ctx, t);
+}
+
+// ---------------------------------------------------------------------------
+// batched inside
+// ---------------------------------------------------------------------------
+int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandBatch* bb, std::string* err)
+{
+    const int n = (int)L.size();
+    bb->n = n;
+    bb->order.resize(n);
+    for (int a = 0; a < n; a++) bb->order[a] = a;
+    std::stable_sort(bb->order.begin(), bb->order.end(), [&](int x, int y) { return Wb[x] > Wb[y]; });
+    bb->slot.assign(n, 0);
+    for (int k = 0; k < n; k++) bb->slot[bb->order[k]] = k;
+    // one allocation: per band 6 tables, Ssuf/Osuf, b/cb/u/Zd; then the batch arrays
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    std::vector<size_t> off_tab(n), off_suf(n), off_dbl(n);
+    size_t bytes = 0;
+    for (int k = 0; k < n; k++) {
+        const int a = bb->order[k];
+        const size_t RS = ((size_t)Wb[a] + 1 + 31) / 32 * 32;
+        off_tab[k] = bytes;
+        bytes = al(bytes + 6 * (size_t)L[a] * RS * sizeof(float));
+        off_suf[k] = bytes;
+        bytes = al(bytes + (size_t)(L[a] + 1) * 2 * sizeof(float));
+        off_dbl[k] = bytes;
+        bytes = al(bytes + (size_t)(3 * L[a] + 8) * sizeof(double));
+    }
+    const size_t off_bands = bytes;
+    bytes = al(bytes + (size_t)n * sizeof(Band));
+    const size_t off_cum = bytes;
+    bytes = al(bytes + (size_t)(n + 1) * sizeof(long long));
+    const size_t off_wbs = bytes;
+    bytes = al(bytes + (size_t)n * sizeof(int));
+    const size_t off_sync = bytes;
+    bytes = al(bytes + 4 * sizeof(unsigned int));
+    const size_t off_Z = bytes;
+    bytes = al(bytes + (size_t)n * sizeof(double));
+    cudaError_t e = cudaMalloc(&bb->mem, bytes);
+    if (e != cudaSuccess) {
+        bb->mem = nullptr;
+        *err = std::string("batch band tables: ") + cudaGetErrorString(e);
+        return MESSI_ENOMEM;
+    }
+    bb->bytes = bytes;
+    char* base = (char*)bb->mem;
+    bb->host.assign(n, Band{});
+    std::vector<long long> cum(n + 1, 0);
+    std::vector<int> wbs(n);
+    bb->d_sync = (unsigned int*)(base + off_sync);
+    for (int k = 0; k < n; k++) {
+        const int a = bb->order[k];
+        Band& t = bb->host[k];
+        t.L = L[a];
+        t.Wb = Wb[a];
+        t.RS = ((Wb[a] + 1 + 31) / 32) * 32;
+        const size_t tab = (size_t)t.L * t.RS;
+        float* f = (float*)(base + off_tab[k]);
+        t.Lrow = f;
+        t.Lcol = f + tab;
+        t.Srow = f + 2 * tab;
+        t.Scol = f + 3 * tab;
+        t.Frow = f + 4 * tab;
+        t.pb = f + 5 * tab;
+        t.Ssuf = (float*)(base + off_suf[k]);
+        t.Osuf = t.Ssuf + (t.L + 1);
+        t.b = (double*)(base + off_dbl[k]);
+        t.cb = t.b + t.L;
+        t.u = t.cb + (t.L + 1);
+        t.Zd = t.u + t.L;
+        t.maxspan = nullptr;
+        t.sync = bb->d_sync;
+        t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = nullptr;
+        cum[k + 1] = cum[k] + t.L;
+        wbs[k] = t.Wb;
+    }
+    bb->total_cols = cum[n];
+    bb->d_bands = (Band*)(base + off_bands);
+    bb->d_cumL = (long long*)(base + off_cum);
+    bb->d_wbs = (int*)(base + off_wbs);
+    bb->d_Z = (double*)(base + off_Z);
+    e = cudaMemcpy(bb->d_bands, bb->host.data(), (size_t)n * sizeof(Band), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(bb->d_cumL, cum.data(), (size_t)(n + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(bb->d_wbs, wbs.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        *err = std::string("batch band descriptors: ") + cudaGetErrorString(e);
+        return MESSI_ECUDA;
+    }
+    return MESSI_OK;
+}
+
+void bandbatch_free(BandBatch* bb)
+{
+    if (bb->mem) cudaFree(bb->mem);
+    bb->mem = nullptr;
+    bb->host.clear();
+}
+
+int launch_baseline_batch(messi_ctx* ctx, const BandBatch& bb, double B)
+{
+    if (bb.n == 0) return MESSI_OK;
+    baseline_batch_kernel<<<bb.n, 1024, 0, ctx->stream>>>(bb.d_bands, B, baseline_c());
+    LAUNCH_CHECK(ctx, "baseline_batch_kernel");
+    return MESSI_OK;
+}
+
+int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
+{
+    if (bb.n == 0) return MESSI_OK;
+    Rules R = make_rules(B);
+    const Band* bands = bb.d_bands;
+    const long long* cum = bb.d_cumL;
+    const int* wbs = bb.d_wbs;
+    int n = bb.n;
+    double Bv = B;
+    unsigned int* sync = bb.d_sync;
+    void* args[] = {&bands, &cum, &wbs, &n, &R, &Bv, &sync};
+    const int grid = wave_grid(ctx, (const void*)inside_wave_batch_kernel,
+                               (int)std::min<long long>(bb.total_cols, 1 << 30));
+    double cells = 0.0;
+    for (const Band& t : bb.host) cells += (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0);
+    prof_begin(ctx, 1, cells);
+    cudaError_t e = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
+    e = cudaLaunchCooperativeKernel((const void*)inside_wave_batch_kernel, dim3(grid), dim3(256), args, 0,
+                                    ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_wave_batch_kernel");
+    prof_end(ctx);
+    prof_begin(ctx, 2, 0.0);
+    inside_suffix_batch_kernel<<<n, 1024, 0, ctx->stream>>>(bands, R);
+    LAUNCH_CHECK(ctx, "inside_suffix_batch_kernel");
+    prof_end(ctx);
+    finish_Z_batch_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(bands, n, sync, bb.d_Z);
+    LAUNCH_CHECK(ctx, "finish_Z_batch_kernel");
+    if (!ctx->status_host) return MESSI_OK;
+    e = cudaMemcpyAsync(ctx->status_host, sync + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "status readback");
 }
 
 // ---------------------------------------------------------------------------

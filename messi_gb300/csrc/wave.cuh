@@ -1,0 +1,63 @@
+// wave.cuh -- device helpers shared by the persistent wavefront kernels
+// (SCFG inside/outside, posterior decoding): a grid barrier with a bounded
+// wait and the split-sum group width.
+#pragma once
+
+#include "internal.h"
+
+namespace messi {
+
+// ---------------------------------------------------------------------------
+// grid barrier with a bounded wait (wavefront kernels)
+// ---------------------------------------------------------------------------
+// each spin is an L2 round trip plus a 32 ns sleep (~0.3-0.5 us): a wait gives
+// up after one to two seconds
+constexpr unsigned int kSpinLimit = 1u << 22;
+
+static __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// sync[0] = arrivals, monotonic within a launch (barrier g completes when it
+// reaches g * gridDim.x, so the last arrival's add is the release itself);
+// sync[2] = error flag.  Returns false (in every thread of the CTA) once any
+// CTA has given up waiting.  The CTA barrier orders every thread's cells
+// before thread 0's fence and arrival (the cooperative-groups grid barrier
+// pattern).  Cells written by other CTAs before the barrier are read with
+// __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
+// those tables.
+static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned int target = (gen + 1) * gridDim.x;
+        __threadfence();
+        atomicAdd(&sync[0], 1u);
+        unsigned int spins = 0;
+        while (ld_acquire_u32(&sync[0]) < target) {
+            if ((++spins & 63u) == 0u && (ld_acquire_u32(&sync[2]) != 0u || spins > kSpinLimit)) {
+                atomicExch(&sync[2], 1u);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        gen++;
+        s_ok = ok && (ld_acquire_u32(&sync[2]) == 0u);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+static __device__ __forceinline__ int group_width(int nterms)
+{
+    return nterms <= 8 ? 1 : (nterms <= 32 ? 4 : (nterms <= 96 ? 8 : (nterms <= 256 ? 16 : 32)));
+}
+
+}  // namespace messi

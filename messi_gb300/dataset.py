@@ -32,6 +32,10 @@ def char_mask(c: str) -> int:
     return IUPAC_MASK.get(c.upper(), 15)
 
 
+_MASK_LUT = np.array([char_mask(chr(b)) for b in range(256)], dtype=np.uint8)
+_NUC_LUT = np.array([NUCMAPPING.get(chr(b), -1) for b in range(256)], dtype=np.int8)
+
+
 class TreeNode:
     """src/Tree.jl:20-30."""
 
@@ -175,14 +179,16 @@ class Dataset:
         L = len(seqs[0])
         if any(len(s) != L for s in seqs):
             raise ValueError("sequences are not aligned (unequal lengths)")
-        masks = np.array([[char_mask(c) for c in s] for s in seqs], dtype=np.uint8).reshape(len(seqs), L)
-        gap = np.array([[c not in NUCMAPPING for c in s] for s in seqs], dtype=np.float64).reshape(len(seqs), L)
-        obs = np.zeros(4)
-        for s in seqs:
-            for c in s:
-                k = NUCMAPPING.get(c)
-                if k is not None:
-                    obs[k] += 1.0
+        if all(s.isascii() for s in seqs):
+            # byte lookup tables (same mapping as char_mask / NUCMAPPING)
+            raw = np.frombuffer("".join(seqs).encode("ascii"), dtype=np.uint8).reshape(len(seqs), L)
+            masks = _MASK_LUT[raw]
+            nuc = _NUC_LUT[raw]
+        else:
+            masks = np.array([[char_mask(c) for c in s] for s in seqs], dtype=np.uint8).reshape(len(seqs), L)
+            nuc = np.array([[NUCMAPPING.get(c, -1) for c in s] for s in seqs], dtype=np.int8).reshape(len(seqs), L)
+        gap = (nuc < 0).astype(np.float64)
+        obs = np.bincount(nuc[nuc >= 0].astype(np.int64), minlength=4).astype(np.float64)[:4]
         obs = obs / obs.sum() if obs.sum() > 0 else np.full(4, 0.25)
         root = parse_newick(newick)
         if doroottree:

@@ -220,36 +220,60 @@ class LearnedProposal:
 
     name = "learned"
 
-    def __init__(self, summaries, ncomp=4, width=256, seed=1, ctx=None, lr=2e-3, inflate=1.25):
-        from . import api
+    def __init__(self, summaries, ncomp=4, width=256, seed=1, ctx=None, lr=2e-3, inflate=1.25, net=None,
+                 local_w=0.25, wide_w=0.1, wide_scale=2.0):
         self.summ = np.asarray(summaries, np.float64)
         self.K = ncomp
         self.D = NFREE
         self.in_dim = NFREE + 1 + len(self.summ)  # the 12 parameters (p10 tied) + summaries
-        self.net = api.MLP(self.in_dim, width, ncomp, self.D, seed=seed, ctx=ctx)
+        if net is None:
+            from . import api
+            net = api.MLP(self.in_dim, width, ncomp, self.D, seed=seed, ctx=ctx)
+        self.net = net
         self.lr = lr
         # proposal scales are the fitted ones times `inflate` (in both the
         # draw and the density), which keeps a fit to an under-dispersed
         # burn-in sample from starving the tails
         self.log_inflate = math.log(inflate)
+        self.local_w = float(local_w)
+        self.wide_w = float(wide_w)
+        self.wide_scale = float(wide_scale)
+        # affine whitening z = zmu + Lw @ zn (Lw: Cholesky factor of the
+        # covariance of the recent burn-in states), so the diagonal mixture
+        # works in coordinates where the posterior is close to isotropic
         self.zmu = np.zeros(self.D)
-        self.zsd = np.ones(self.D)
+        self.Lw = np.eye(self.D)
+        self.Lw_inv = np.eye(self.D)
+        self.logdet = 0.0
         self.train_time = 0.0
         self.train_steps = 0
         self.frozen = False
 
     def _inputs(self, Z):
         Z = np.atleast_2d(Z)
-        zn = (Z - self.zmu) / self.zsd
+        zn = self._whiten(Z)
         tied = zn[:, 8:9]  # p10 = lambda_GC
         return np.hstack([zn, tied, np.tile(self.summ, (Z.shape[0], 1))])
 
-    def _mixture(self, head):
+    def _whiten(self, Z):
+        return (np.atleast_2d(Z) - self.zmu) @ self.Lw_inv.T
+
+    def _mixture(self, head, zn_from):
+        """Mixture over the K network components plus one local component
+        N(zn_from, (2.38^2 / D) I) of weight `local_w` (the adaptive-Metropolis
+        step in whitened coordinates), which keeps the chain moving where the
+        fitted components are poor.  Both directions of the Metropolis-Hastings
+        ratio evaluate this same density."""
         K, D = self.K, self.D
         logits = head[:, :K].astype(np.float64)
         mu = head[:, K:K + K * D].astype(np.float64).reshape(-1, K, D)
         ls = np.clip(head[:, K + K * D:].astype(np.float64).reshape(-1, K, D), -7.0, 5.0) + self.log_inflate
-        lw = logits - np.logaddexp.reduce(logits, axis=1, keepdims=True)
+        lw = logits - np.logaddexp.reduce(logits, axis=1, keepdims=True) + math.log1p(-self.local_w - self.wide_w)
+        n = head.shape[0]
+        lw = np.hstack([lw, np.full((n, 1), math.log(self.local_w)), np.full((n, 1), math.log(self.wide_w))])
+        mu = np.concatenate([mu, np.atleast_2d(zn_from)[:, None, :], np.zeros((n, 1, D))], axis=1)
+        ls = np.concatenate([ls, np.full((n, 1, D), math.log(2.38 / math.sqrt(D))),
+                             np.full((n, 1, D), math.log(self.wide_scale))], axis=1)
         return lw, mu, ls
 
     def _logq_norm(self, lw, mu, ls, zn):
@@ -259,20 +283,20 @@ class LearnedProposal:
 
     def logq(self, z_to, z_from):
         """log q(z_to | z_from) in z coordinates (includes the normalisation
-        scale of the standardised space)."""
+        scale of the whitened space)."""
         head = self.net.forward(self._inputs(z_from))
-        lw, mu, ls = self._mixture(head)
-        zn = (np.atleast_2d(z_to) - self.zmu) / self.zsd
-        return self._logq_norm(lw, mu, ls, zn) - float(np.sum(np.log(self.zsd)))
+        lw, mu, ls = self._mixture(head, self._whiten(z_from))
+        return self._logq_norm(lw, mu, ls, self._whiten(z_to)) - self.logdet
 
     def propose(self, rng, theta):
         z = to_z(theta)
         head = self.net.forward(self._inputs(z))
-        lw, mu, ls = self._mixture(head)
-        k = rng.choice(self.K, p=np.exp(lw[0]) / np.exp(lw[0]).sum())
+        lw, mu, ls = self._mixture(head, self._whiten(z))
+        w = np.exp(lw[0])
+        k = rng.choice(len(w), p=w / w.sum())
         zn_new = mu[0, k] + np.exp(ls[0, k]) * rng.standard_normal(self.D)
-        z_new = zn_new * self.zsd + self.zmu
-        fwd = self._logq_norm(lw, mu, ls, zn_new[None, :])[0] - float(np.sum(np.log(self.zsd)))
+        z_new = self.zmu + self.Lw @ zn_new
+        fwd = self._logq_norm(lw, mu, ls, zn_new[None, :])[0] - self.logdet
         rev = self.logq(z, z_new)[0]
         # target density in z-space carries the Jacobian of theta(z)
         hastings = rev - fwd + log_jacobian(z_new) - log_jacobian(z)
@@ -285,13 +309,18 @@ class LearnedProposal:
             return None
         t0 = time.perf_counter()
         Z = np.asarray(Zbuf)
+        Z = Z[len(Z) // 2:]  # the recent half: the early burn-in is a transient
         self.zmu = Z.mean(axis=0)
-        self.zsd = np.maximum(Z.std(axis=0), 1e-3)
+        cov = np.cov(Z.T) + 1e-8 * np.eye(self.D)
+        cov += np.diag(np.maximum(np.diag(cov), 1e-6) * 1e-3)
+        self.Lw = np.linalg.cholesky(cov)
+        self.Lw_inv = np.linalg.inv(self.Lw)
+        self.logdet = float(np.sum(np.log(np.diag(self.Lw))))
         loss = None
         for _ in range(steps):
             a = Z[rng.integers(0, len(Z), batch)]
             b = Z[rng.integers(0, len(Z), batch)]
-            loss = self.net.train_step(self._inputs(a), (b - self.zmu) / self.zsd, lr=self.lr)
+            loss = self.net.train_step(self._inputs(a), self._whiten(b), lr=self.lr)
             self.train_steps += 1
         self.train_time += time.perf_counter() - t0
         return loss

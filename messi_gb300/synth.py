@@ -13,6 +13,9 @@ Named workloads (seeded ``numpy.random.Generator(PCG64(seed))``):
   "c2": 64 seqs x 1,000 nt, max pair span 500, 30% paired, mean branch 0.1
   "c4": 30 seqs x 9,000 nt, max pair span 800, 20% paired, mean branch 0.05
   "c2p": 64 seqs x 600 nt, max pair span 300 (profiling-sized c2)
+Batches (``make_batch``): "c3" = 256 alignments, each with L ~ U(80, 1500)
+columns, N ~ U(8, 128) sequences, W = L - 1, its own tree, structure and
+model; "c3s" = 24 alignments, L ~ U(20, 160), N ~ U(4, 24) (test-sized).
 Every workload: pi ~ Dirichlet(5,5,5,5), lambda_GC/AT/GT ~ U(1,5), exchange
 rates and site-rate shape at the reference's starting vector
 (src/MESSI.jl:1479), 5% i.i.d. gaps.
@@ -20,7 +23,6 @@ rates and site-rate shape at the reference's starting vector
 from dataclasses import dataclass
 
 import numpy as np
-from scipy.linalg import expm
 
 from . import model as M
 from .dataset import Dataset, TreeNode, to_newick
@@ -130,6 +132,20 @@ def _simulate_down(rng, ds, Pn, rootprob, ncols):
     return states
 
 
+def _pmats(Q, pi, bls):
+    """exp(Q t) for every branch length (reversible Q with stationary pi, by
+    the symmetric eigendecomposition); zero matrix for the root (index 0)."""
+    d = np.sqrt(pi)
+    S = (d[:, None] * Q) / d[None, :]
+    w, U = np.linalg.eigh(0.5 * (S + S.T))
+    t = np.asarray(bls, np.float64)
+    E = np.exp(w[None, :] * t[:, None])
+    P = np.einsum("ak,nk,dk->nad", U, E, U) * (d[None, None, :] / d[None, :, None])
+    P = np.maximum(P, 0.0)
+    P[0] = 0.0
+    return P
+
+
 def simulate(rng, ds, params15, paired, gap_rate=0.05):
     """Fill the alignment of `ds` (its tree only is used) from the model."""
     cp = M.getparams(params15, ds.branchlengths, 3, 5)
@@ -138,7 +154,7 @@ def simulate(rng, ds, params15, paired, gap_rate=0.05):
     nodes = ds.numnodes
     # unpaired model: GTR x site rate (src/Simulations.jl:99-107)
     Q4 = M.gtr(cp.q, cp.freqs)
-    P4 = np.array([[np.zeros((4, 4))] + [expm(Q4 * r * t) for t in ds.branchlengths[1:]] for r in cp.siteRates])
+    P4 = np.array([_pmats(Q4 * r, cp.freqs, ds.branchlengths) for r in cp.siteRates])
     # paired model: 45 categories with weights (src/Simulations.jl:110-128)
     museparams = M.getmusespecificparamsarray(cp)
     cats, logw = [], []
@@ -171,8 +187,11 @@ def simulate(rng, ds, params15, paired, gap_rate=0.05):
                 cp.lambdaratesGT[mp.lambdacat - 1] + 1
             Q = M.muse(lGC, lAT, lGT, cp.q, cp.freqs, cp.siteRates[a], cp.siteRates[b])
             pi16[c] = M.musefreqs(cp.freqs, lGC, lAT, lGT)
-            P16[c] = np.array([np.zeros((16, 16))] + [expm(Q * t) for t in ds.branchlengths[1:]])
-        Pn = [np.array([P16[c][v] for c in z]) for v in range(nodes)]
+            P16[c] = _pmats(Q, pi16[c], ds.branchlengths)
+        idx = {c: k for k, c in enumerate(used)}
+        stack = np.array([P16[c] for c in used])       # [used, nodes, 16, 16]
+        zi = np.array([idx[c] for c in z])
+        Pn = [stack[zi, v] for v in range(nodes)]
         rootp = np.array([pi16[c] for c in z])
         st = _simulate_down(rng, ds, Pn, rootp, len(left))
         for v in range(nodes):
@@ -205,3 +224,23 @@ def make_workload(name_or_spec, seed=1):
     fasta = "".join(f">{n}\n{s}\n" for n, s in zip(names, seqs))
     ds = Dataset.from_sequences(names, seqs, newick)
     return Synthetic(dataset=ds, params15=p15, paired=paired, W=W, fasta=fasta, newick=newick, seed=seed)
+
+
+BATCHES = {
+    "c3": dict(count=256, numcols=(80, 1500), numseqs=(8, 128), paired=0.30, mean_bl=0.10),
+    "c3s": dict(count=24, numcols=(20, 160), numseqs=(4, 24), paired=0.30, mean_bl=0.10),
+}
+
+
+def make_batch(name, seed=1):
+    """Seeded batch of independent workloads (see module docstring); the
+    band of each alignment is its full length (W = L - 1)."""
+    spec = BATCHES[name]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(spec["count"]):
+        L = int(rng.integers(spec["numcols"][0], spec["numcols"][1] + 1))
+        N = int(rng.integers(spec["numseqs"][0], spec["numseqs"][1] + 1))
+        one = dict(numseqs=max(3, N), numcols=L, W=max(1, L - 1), paired=spec["paired"], mean_bl=spec["mean_bl"])
+        out.append(make_workload(one, seed=int(rng.integers(1, 2 ** 31))))
+    return out

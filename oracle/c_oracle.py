@@ -55,9 +55,13 @@ def lib():
             L.mo_inside.argtypes = [_f64p, _f64pF, c_int, c_double, _f64pF, c_int]
             L.mo_inside_banded.argtypes = [_f64p, _f64pF, c_int, c_int, c_double, ctypes.POINTER(c_double), c_int]
             L.mo_outside.argtypes = [_f64pF, _f64p, _f64pF, c_int, _f64pF, c_int]
+            _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+            L.mo_posterior_decoding.argtypes = [_f32p, _f32p, c_int, ctypes.c_float, _f32p, _i32p]
+            L.mo_posterior_traceback.argtypes = [_i32p, c_int, _i32p]
             L.mo_basepairprobs.argtypes = [_f64pF, _f64pF, _f64p, _f64pF, c_int, _f64p, _f64pF]
             for name in ("mo_reversible_eig", "mo_transition_matrices", "mo_subcolumnrefs", "mo_pair_matrix",
-                         "mo_unpaired", "mo_inside", "mo_inside_banded", "mo_outside", "mo_basepairprobs"):
+                         "mo_unpaired", "mo_inside", "mo_inside_banded", "mo_outside", "mo_basepairprobs",
+                         "mo_posterior_decoding", "mo_posterior_traceback"):
                 getattr(L, name).restype = c_int
             _lib = L
     return _lib
@@ -211,3 +215,27 @@ def basepairprobs(ins, outs, u, p):
     _check(lib().mo_basepairprobs(np.asfortranarray(ins, np.float64), np.asfortranarray(outs, np.float64), u,
                                   np.asfortranarray(p, np.float64), L, single, pair), "basepairprobs")
     return single, pair
+
+
+def posterior_decoding(single, pair, alpha=2.0):
+    """(e, s) L x L row-major, the GPU-path semantics of
+    computeposteriordecodingcuda (FP32).  The reference kernel reads
+    pair[i*L + k] of the column-major Julia matrix, i.e. element (k, i); the
+    same element is passed here (row-normalised posteriors are symmetric only
+    to rounding)."""
+    L = len(single)
+    e = np.zeros(L * L, np.float32)
+    sm = np.zeros(L * L, np.int32)
+    buf = np.ascontiguousarray(np.asarray(pair, np.float64).T.astype(np.float32))
+    _check(lib().mo_posterior_decoding(np.ascontiguousarray(single, np.float32), buf, L, float(alpha), e, sm),
+           "posterior_decoding")
+    return e.reshape(L, L), sm.reshape(L, L)
+
+
+def posterior_traceback(s):
+    """1-based partner per column (0 = unpaired) from a row-major s."""
+    s = np.ascontiguousarray(s, np.int32)
+    L = s.shape[0]
+    paired = np.zeros(L, np.int32)
+    _check(lib().mo_posterior_traceback(s.ravel(), L, paired), "posterior_traceback")
+    return paired

@@ -772,3 +772,99 @@ int mo_inside_banded(const double* u, const double* p, int L, int W, double B, d
     free(suf);
     return MO_OK;
 }
+
+/*
+ * Posterior decoding (maximum expected accuracy structure) as
+ * computeposteriordecodingcuda runs it (src/InsideCUDA.jl:183-215 with the
+ * kernel posteriordecoding of src/cuda/inside.cu:286-321): FP32 values,
+ * e(i,i) = 0, diagonals in increasing span, and for cell (i,j)
+ *   e1 = single[i] + e(i+1,j)
+ *   e2 = alpha*pair(i,j) + e(i+1,j-1)
+ *   e3 = max_{k=i+1..j-1} alpha*pair(i,k) + e(i+1,k-1) + e(k+1,j)
+ * with ties going to e1, then e2, then the smallest k.  The alpha*x + y
+ * products are single-rounding fused multiply-adds, as the CUDA compiler
+ * contracts them.  e and s are L x L row-major (e[i*L+j]); s = -1 (i
+ * unpaired), -2 (i pairs j) or k+1 (i pairs k, 0-based k).  pair is read as
+ * pair[i*L+k], the reference kernel's indexing of the column-major matrix.
+ */
+int mo_posterior_decoding(const float* single, const float* pair, int L, float alpha, float* e, int* s)
+{
+    if (L < 1) return MO_EINVAL;
+    memset(e, 0, sizeof(float) * (size_t)L * L);
+    memset(s, 0, sizeof(int) * (size_t)L * L);
+    for (int diag = 1; diag < L; diag++) {
+        for (int i = 0; i < L - diag; i++) {
+            const int j = i + diag;
+            const float e1 = single[i] + e[(size_t)(i + 1) * L + j];
+            const float e2 = fmaf(alpha, pair[(size_t)i * L + j], e[(size_t)(i + 1) * L + j - 1]);
+            float maxe3 = -1e10f;
+            int maxk = 0;
+            for (int k = i + 1; k <= j - 1; k++) {
+                const float v = fmaf(alpha, pair[(size_t)i * L + k], e[(size_t)(i + 1) * L + k - 1]) +
+                                e[(size_t)(k + 1) * L + j];
+                if (v > maxe3) {
+                    maxe3 = v;
+                    maxk = k;
+                }
+            }
+            float maxval = e1;
+            int sv = -1;
+            if (e2 > maxval) {
+                maxval = e2;
+                sv = -2;
+            }
+            if (maxe3 > maxval) {
+                maxval = maxe3;
+                sv = maxk + 1;
+            }
+            s[(size_t)i * L + j] = sv;
+            e[(size_t)i * L + j] = maxval;
+        }
+    }
+    return MO_OK;
+}
+
+/* posteriordecodingtraceback (src/RNATools.jl:43-72) on the row-major s of
+ * mo_posterior_decoding.  paired[i] = 1-based partner of column i (0-based
+ * i), 0 when unpaired (the reference's Julia vector). */
+int mo_posterior_traceback(const int* s, int L, int* paired)
+{
+    if (L < 1) return MO_EINVAL;
+    memset(paired, 0, sizeof(int) * (size_t)L);
+    int* stack = (int*)malloc(sizeof(int) * 2 * ((size_t)L + 2));
+    if (!stack) return MO_ENOMEM;
+    int top = 0;
+    stack[top++] = 1;
+    stack[top++] = L;  /* 1-based (i, j) as the reference */
+    while (top > 0) {
+        const int j = stack[--top];
+        const int i = stack[--top];
+        const int k = s[(size_t)(i - 1) * L + (j - 1)];
+        if (k == -1) {
+            stack[top++] = i + 1;
+            stack[top++] = j;
+        } else if (k == -2) {
+            paired[i - 1] = j;
+            paired[j - 1] = i;
+            if (i + 1 < j - 1) {
+                stack[top++] = i + 1;
+                stack[top++] = j - 1;
+            }
+        } else if (k > 0) {
+            if (i < k) {
+                paired[i - 1] = k;
+                paired[k - 1] = i;
+            }
+            if (i + 1 <= k - 1) {
+                stack[top++] = i + 1;
+                stack[top++] = k - 1;
+            }
+            if (k + 1 <= j) {
+                stack[top++] = k + 1;
+                stack[top++] = j;
+            }
+        }
+    }
+    free(stack);
+    return MO_OK;
+}

@@ -189,3 +189,33 @@ def brute_force_posteriors(u, p):
                 pair[x, paired[x]] += wi
     s = single + pair.sum(axis=1)
     return single / s, pair / s[:, None]
+
+
+def decoding_score(pairs, single, pair, alpha, i, j):
+    """Objective of the posterior-decoding recursion (src/cuda/inside.cu:286-321)
+    for one nested structure on [i, j]: the segment decomposition the
+    recursion uses (first column unpaired / paired with the segment end /
+    paired inside), with e(i, i) = 0."""
+    if j <= i:
+        return 0.0
+    partner = dict(pairs)
+    partner.update({b: a for a, b in pairs})
+    k = partner.get(i)
+    if k is None or k < i:
+        return single[i] + decoding_score(pairs, single, pair, alpha, i + 1, j)
+    if k == j:
+        return alpha * pair[i][j] + decoding_score(pairs, single, pair, alpha, i + 1, j - 1)
+    return (alpha * pair[i][k] + decoding_score(pairs, single, pair, alpha, i + 1, k - 1)
+            + decoding_score(pairs, single, pair, alpha, k + 1, j))
+
+
+def brute_force_decoding(single, pair, alpha):
+    """(best score, best pair set) over every nested structure on L columns
+    (adjacent pairs allowed, as in the decoding recursion)."""
+    L = len(single)
+    best, arg = -np.inf, None
+    for s in _structures(0, L - 1, minloop=1):
+        v = decoding_score(s, single, pair, alpha, 0, L - 1)
+        if v > best:
+            best, arg = v, s
+    return best, arg

@@ -13,7 +13,9 @@ sequences of the reference's host code:
 * ``inside``: src/InsideCUDA.jl:63-181 (float sanitising :63-85,
   initialiseinside, insidealgorithm per span, insidez, 256-thread blocks);
 * ``outside``: src/InsideCUDA.jl:301-389 (outsidealgorithm per span,
-  descending, 1024-thread blocks).
+  descending, 1024-thread blocks);
+* ``posterior_decoding``: src/InsideCUDA.jl:183-215 (posteriordecoding per
+  span, 256-thread blocks, e and s zero-initialised).
 
 It is used as a parity pin for the FP64 oracle (the reference's own outputs)
 and to time the reference GPU path on the same GPU.  felsensteinhelper16 reads
@@ -40,6 +42,7 @@ K_INIT = b"_Z16initialiseinsidePfS_S_PKfi"
 K_INSIDE = b"_Z15insidealgorithmPfS_S_PKfS1_iif"
 K_INSIDEZ = b"_Z7insidezPKfPfi"
 K_OUTSIDE = b"_Z16outsidealgorithmPfPKfS1_S1_iif"
+K_DECODE = b"_Z17posteriordecodingPfPiPKfS2_iif"
 
 
 def available():
@@ -299,3 +302,23 @@ def outside(inside_tab, u, p, B=1.0):
         drv.launch("inside.cubin", K_OUTSIDE, g, bs, ("p", d_out), ("p", d_in), ("p", d_p), ("p", d_u), ("i", a),
                    ("i", L), ("f", B))
     return d_out.cpu().numpy().reshape(3, L, L).astype(np.float64)
+
+
+def posterior_decoding(single, pair, alpha=2.0):
+    """(e, s) as L x L row-major arrays (device layout: e[i*L+j]) from the
+    reference posteriordecoding kernel; single/pair are converted to FP32 as
+    src/InsideCUDA.jl:184-185 does.  pair is uploaded in Julia column-major
+    order (it is symmetric)."""
+    drv = driver()
+    torch = drv.torch
+    L = len(single)
+    d_s = torch.tensor(np.asarray(single, np.float32), device="cuda")
+    d_p = torch.tensor(np.asarray(pair, np.float32).ravel(order="F"), device="cuda")
+    e = torch.zeros(L * L, dtype=torch.float32, device="cuda")
+    sm = torch.zeros(L * L, dtype=torch.int32, device="cuda")
+    bs = 256
+    g = (L + bs - 1) // bs
+    for diag in range(1, L):
+        drv.launch("inside.cubin", K_DECODE, g, bs, ("p", e), ("p", sm), ("p", d_p), ("p", d_s), ("i", L),
+                   ("i", diag), ("f", alpha))
+    return e.cpu().numpy().reshape(L, L), sm.cpu().numpy().reshape(L, L)

@@ -83,11 +83,11 @@ def test_learned_proposal_is_exact_and_beats_the_plain_move(api):
     tgt = ToyTarget()
     theta0 = mcmc.from_z(tgt.m + 0.5 * tgt.s)
     summ = np.linspace(-1, 1, 32)
-    n, burn = 6000, 2000
+    n, burn = 20000, 6667
     plain = mcmc.run_chain(tgt, theta0, n, burn, proposal="plain", seed=1)
     learned = mcmc.LearnedProposal(summ, seed=5)
-    lrn = mcmc.run_chain(tgt, theta0, n, burn, proposal="learned", seed=2, learned=learned, fit_every=250,
-                         fit_steps=120)
+    lrn = mcmc.run_chain(tgt, theta0, n, burn, proposal="learned", seed=2, learned=learned, fit_every=333,
+                         fit_steps=60)
     for res in (plain, lrn):
         Z = np.array([mcmc.to_z(t) for t in res.samples])
         for k in range(mcmc.NFREE):

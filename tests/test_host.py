@@ -78,3 +78,17 @@ def test_synthetic_workload_shapes(name):
     # deterministic from the seed
     s2 = synth.make_workload(name, seed=3)
     assert s2.fasta == s.fasta and s2.newick == s.newick
+
+
+def test_kh99_prior_matches_oracle():
+    from messi_gb300.structures import calculateKH99prior
+    from oracle import oracle_np as onp
+    rng = np.random.default_rng(2)
+    for L in (1, 2, 5, 9, 14):
+        for s in list(onp._structures(0, L - 1))[:: max(1, len(list(onp._structures(0, L - 1))) // 7)]:
+            paired0 = -np.ones(L, dtype=int)
+            paired1 = np.zeros(L, dtype=int)
+            for a, b in s:
+                paired0[a], paired0[b] = b, a
+                paired1[a], paired1[b] = b + 1, a + 1
+            assert abs(calculateKH99prior(paired1) - onp.kh99_prior(paired0, L)) < 1e-12

@@ -67,3 +67,43 @@ def test_ess_on_ar1():
     # MCSE of the mean of an AR(1): sd * sqrt(tau / n)
     expected = math.sqrt(1 / (1 - phi ** 2)) * math.sqrt(tau / n)
     assert abs(mcmc.mcse(x) - expected) < 0.35 * expected
+
+
+class _ZeroHead:
+    """Stand-in for the proposal network: every head is zero, so the learned
+    proposal is the whitened Gaussian N(zmu, inflate^2 * Cov) of the burn-in."""
+
+    def __init__(self, K, D):
+        self.width = K + 2 * K * D
+
+    def forward(self, x):
+        return np.zeros((np.atleast_2d(x).shape[0], self.width), np.float32)
+
+    def train_step(self, x, t, lr=None):
+        return 0.0
+
+
+def test_whitened_learned_proposal_is_exact_on_a_correlated_target():
+    rng = np.random.default_rng(8)
+    D = mcmc.NFREE
+    A = rng.normal(size=(D, D))
+    cov = 0.02 * (A @ A.T / D + 0.1 * np.eye(D))
+    icov = np.linalg.inv(cov)
+    m = np.array([0.5, 1.4, 0.5, -0.7, 1.7, -0.3, -0.5, 0.0, 0.4, 0.7, -0.7])
+
+    def target(theta):
+        if not mcmc.isvalid_theta(theta) or theta[7] <= 0.0 or theta[7] >= 1.0:
+            return -math.inf
+        z = mcmc.to_z(theta)
+        d = z - m
+        return float(-0.5 * d @ icov @ d - mcmc.log_jacobian(z))
+
+    lp = mcmc.LearnedProposal(np.zeros(4), ncomp=2, net=_ZeroHead(2, D))
+    res = mcmc.run_chain(target, mcmc.from_z(m + 0.1), 15000, 5000, proposal="learned", seed=4, learned=lp,
+                         fit_every=250, fit_steps=1)
+    Z = np.array([mcmc.to_z(t) for t in res.samples])
+    assert res.accept["learned"][0] > 0.2
+    sd = np.sqrt(np.diag(cov))
+    for k in range(D):
+        assert abs(Z[:, k].mean() - m[k]) < 5 * mcmc.mcse(Z[:, k]) + 0.02 * sd[k]
+    np.testing.assert_allclose(np.cov(Z.T), cov, atol=0.25 * np.max(np.diag(cov)))

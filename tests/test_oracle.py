@@ -225,3 +225,25 @@ def test_banded_inside_equals_dense(L, W):
     Zd = co.inside(u, p)[0, 0, L - 1]
     Zb = co.inside_banded_Z(u, p, W)
     assert abs(Zd - Zb) <= 1e-12 * abs(Zd)
+
+
+@pytest.mark.parametrize("L", [1, 2, 3, 6, 9])
+def test_posterior_decoding_equals_brute_force(L):
+    rng = np.random.default_rng(40 + L)
+    p = rng.random((L, L)) ** 3
+    p = np.triu(p, 1)
+    p = p + p.T
+    p /= max(1.0, p.sum(axis=1).max()) * 1.2
+    single = 1.0 - p.sum(axis=1)
+    e, s = co.posterior_decoding(single, p, 2.0)
+    best, arg = onp.brute_force_decoding(single.astype(np.float32).astype(np.float64),
+                                         p.astype(np.float32).astype(np.float64), 2.0)
+    assert abs(float(e[0, L - 1]) - best) <= 1e-5 * max(1.0, abs(best))
+    paired = co.posterior_traceback(s)
+    got = tuple(sorted((i, paired[i] - 1) for i in range(L) if paired[i] - 1 > i))
+    val = onp.decoding_score(got, single.astype(np.float32).astype(np.float64),
+                             p.astype(np.float32).astype(np.float64), 2.0, 0, L - 1)
+    assert abs(val - best) <= 1e-5 * max(1.0, abs(best))
+    for i in range(L):
+        if paired[i]:
+            assert paired[paired[i] - 1] == i + 1
