@@ -115,6 +115,27 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws):
+    """Largest value of x over the ranks (the whole job takes as long as its
+    slowest rank).  Works on the NCCL (GPU tensor) and gloo (CPU) backends."""
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    if dist.get_backend() == "nccl":
+        t = torch.tensor([float(x)], dtype=torch.float64, device=f"cuda:{torch.cuda.current_device()}")
+    else:
+        t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, steps, max_ms, ws):
+    """Units processed by all ranks per second of the slowest rank (weak
+    scaling: every rank evaluates its own replica)."""
+    return ws * units_per_rank * steps / (max_ms / 1e3)
+
+
 def make_params(s, count, seed):
     """`count` parameter vectors around the workload's generating vector (the
     moves an MCMC chain makes); discretised on the host like getparams."""
@@ -300,14 +321,9 @@ def run_ours(args):
         t_wall = time.perf_counter() - t_wall
     barrier()
     per = [a.elapsed_time(b) for a, b in ev]
-    ms = sum(per)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(per), ws)
     ms_per_step = ms / args.steps
-    value = ws * npairs * args.steps / (ms / 1e3)
+    value = whole_job_rate(npairs, args.steps, ms, ws)
 
     # ---- kernel-level timing pass (event pairs around each pruning launch)
     ctx.profile(True)
@@ -351,7 +367,7 @@ def run_ours(args):
     model_bytes = (45 * (16 + 256 + 16) + 3 * (4 + 16 + 4) + 45 * 3 + 3 + 4 + ds.numnodes) * 8 + 45 * 16 * 4
     h2d = 2 * model_bytes + L * L * 8 + L * 8
     d2h = L * 8 + L * L * 8 + 8
-    e2e_value = ws * npairs / statistics.mean(t_e2e)
+    e2e_value = whole_job_rate(npairs, 1, 1e3 * max_over_ranks(statistics.mean(t_e2e), ws), ws)
 
     # ---- CPU baseline (rank 0, single process)
     cpu = None

@@ -152,6 +152,22 @@ int messi_basepairprobs(messi_ctx* ctx, int32_t L, const double* inside, const d
 int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,
                      double* Z, double* single, double* pairprobs);
 
+/* Likelihood of one fixed structure, integrated over site rates: the
+ * usecuda branch of computemodellikelihood (src/FARCE.jl:2480-2485) without
+ * the prior, i.e. sum(computeunpairedlikelihoods(..., paired)) +
+ * felsensteincudapaired(dataset, paired, params, museparams)
+ * (src/FelsensteinCUDA.jl:721-912).  Only the structure's pairs are pruned
+ * (subtree-pattern dedup as for the band); the reference's paired kernels
+ * stride their child arrays incorrectly for more than one pair per unique
+ * pattern (src/FelsensteinCUDA.jl:858-859), so this follows the CPU
+ * computeuncachedlikelihood (src/FARCE.jl:1257-1456) instead.
+ *   paired:   [L] 1-based partners, 0 when unpaired (symmetric);
+ *   total:    sum of unpaired-column and pair log-likelihoods;
+ *   pairll:   optional [L], the pair log-likelihood at the first column of
+ *             each pair, 0 elsewhere;
+ *   unpaired: optional [L], unpaired log-likelihoods, 0 on paired columns. */
+int messi_structure_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const int32_t* paired,
+                               double* total, double* pairll, double* unpaired);
 /* computeposteriordecodingcuda (src/InsideCUDA.jl:183-215) followed by
  * posteriordecodingtraceback (src/RNATools.jl:43-72): maximum expected
  * accuracy structure from posterior probabilities, in FP32 as the

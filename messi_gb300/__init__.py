@@ -21,7 +21,7 @@ _API_NAMES = ("felsensteincuda", "coevolutionall", "computeunpairedlikelihoods",
               "computeoutsideKH99", "computebasepairprobs", "computeposteriors",
               "computestructureintegratedlikelihood", "computestructureintegratedlikelihoods", "Batch", "Context",
               "get_context", "computeposteriordecodingcuda", "getPosteriorDecodingConsensusStructure",
-              "consensusstructure", "samplestructures")
+              "consensusstructure", "samplestructures", "felsensteincudapaired", "computemodellikelihood")
 
 
 def __getattr__(name):

@@ -192,14 +192,59 @@ def coevolutionall(dataset, params, parallel=True, keepmatrices=False, integrate
     return felsensteincuda(dataset, params, getmusespecificparamsarray(params), maxbasepairdistance, keepmatrices)
 
 
-def computeunpairedlikelihoods(dataset, params, ctx=None):
-    """src/FARCE.jl:1198-1220 (site-rate categories integrated)."""
+def computeunpairedlikelihoods(dataset, params, museparams=None, states=None, paired=None, B=1.0,
+                               conditionalRates=False, rng=None, likelihoodsOnly=True, ctx=None):
+    """src/FARCE.jl:1198-1220 (site-rate categories integrated).  With
+    `paired` (1-based partners, 0 = unpaired) the overload of
+    src/FARCE.jl:1222-1250: 0 on paired columns."""
     ctx = ctx or get_context()
-    h = ctx.dataset(dataset)
+    if paired is not None:
+        _need_cuda(not conditionalRates)
+        _, _, u = _structure_call(dataset, params, paired, ctx)
+        return u
+    h = ctx.dataset(dataset, 1)  # the unpaired pass needs the tree only: smallest pair plan
     m = ModelArgs(params)
     u = np.empty(dataset.numcols)
     ctx.check(ctx.lib.messi_unpaired(ctx.handle, h.handle, ctypes.byref(m.struct), _p(u)), "messi_unpaired")
     return u
+
+
+def _structure_call(dataset, params, paired, ctx):
+    h = ctx.dataset(dataset, 1)
+    m = ModelArgs(params)
+    pr = np.ascontiguousarray(paired, np.int32)
+    if pr.shape != (dataset.numcols,):
+        raise ValueError("paired must have one entry per column")
+    L = dataset.numcols
+    total = ctypes.c_double()
+    pairll = np.empty(L)
+    u = np.empty(L)
+    ctx.check(ctx.lib.messi_structure_likelihood(ctx.handle, h.handle, ctypes.byref(m.struct), _p(pr),
+                                                 ctypes.byref(total), _p(pairll), _p(u)),
+              "messi_structure_likelihood")
+    return total.value, pairll, u
+
+
+def felsensteincudapaired(dataset, paired, params, museparams=None, ctx=None):
+    """src/FelsensteinCUDA.jl:721-912: sum over the pairs of a fixed structure
+    (1-based partners, 0 = unpaired) of the pair log-likelihood mixed over
+    all categories."""
+    ctx = ctx or get_context()
+    if not np.any(np.asarray(paired) > 0):
+        return 0.0
+    _, pairll, _ = _structure_call(dataset, params, paired, ctx)
+    return float(pairll.sum())
+
+
+def computemodellikelihood(rng, dataset, params, paired, samplebranchlengths=False, integratesiterates=True,
+                           useprior=True, fixLambdaGT=False, usecuda=True, ctx=None):
+    """src/FARCE.jl:2439-2520 (the integratesiterates / usecuda branch):
+    prior + unpaired columns + pairs of the fixed structure."""
+    _need_cuda(usecuda and integratesiterates)
+    ctx = ctx or get_context()
+    priorll = computeprior(params, samplebranchlengths, fixLambdaGT) if useprior else 0.0
+    total, _, _ = _structure_call(dataset, params, paired, ctx)
+    return priorll + total
 
 
 def maskgapped(probs, gapfrequency, cutoff, v=0.0):

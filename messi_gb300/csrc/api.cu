@@ -292,6 +292,8 @@ int messi_ctx_create(int device, messi_ctx** out)
     {
         const char* w = std::getenv("MESSI_WAVE_CTAS");
         if (w) ctx->wave_ctas = std::max(0, std::atoi(w));
+        const char* wt = std::getenv("MESSI_WAVE_THREADS");
+        if (wt) ctx->wave_threads = std::atoi(wt);
     }
     *out = ctx;
     return MESSI_OK;
@@ -631,6 +633,72 @@ int messi_sample_structures(messi_ctx* ctx, int32_t L, const double* unpaired, c
     if ((rc = finish(ctx))) return rc;
     if (status != 0u) return fail(ctx, MESSI_ESTATE, "sample structures: a span had no derivation (check the inputs)");
     return MESSI_OK;
+}
+
+int messi_structure_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, const int32_t* paired,
+                               double* total, double* pairll, double* unpaired)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ds || !model || !paired || !total) return fail(ctx, MESSI_EINVAL, "structure likelihood: null argument");
+    const int L = ds->L;
+    std::vector<int2> pairs;
+    std::vector<int32_t> col_pair(L, -1);
+    for (int i = 0; i < L; i++) {
+        const int k = paired[i];
+        if (k < 0 || k > L || k == i + 1 || (k > 0 && paired[k - 1] != i + 1))
+            return fail(ctx, MESSI_EINVAL, "structure likelihood: paired must hold symmetric 1-based partners or 0");
+        if (k > i + 1) {
+            col_pair[i] = (int32_t)pairs.size();
+            pairs.push_back(make_int2(i, k - 1));
+        }
+    }
+    // plan of exactly the structure's pairs (subtree-pattern dedup as for the band)
+    messi_dataset* sub = nullptr;
+    std::vector<int32_t> pu;
+    if (!pairs.empty()) {
+        sub = new (std::nothrow) messi_dataset();
+        if (!sub) return fail(ctx, MESSI_ENOMEM, "structure likelihood: host allocation");
+        sub->ctx = ctx;
+        messi_alignment aln{ds->N, ds->L, ds->numnodes, ds->masks.data(), ds->children.data(), ds->seqindex.data()};
+        std::string err;
+        if ((rc = build_plan(sub, &aln, L - 1, nullptr, &err, &pairs, &pu))) {
+            messi_dataset_destroy(sub);
+            return fail(ctx, rc, err);
+        }
+    }
+    auto done = [&](int code) {
+        if (sub) messi_dataset_destroy(sub);
+        return code;
+    };
+    ModelDev md;
+    if ((rc = upload_model(ctx, ds, model, !pairs.empty(), true, nullptr, &md))) return done(rc);
+    if (sub) {
+        if ((rc = prepare_arena(ctx, sub, md.cat.C))) return done(rc);
+        if ((rc = run_pairs(ctx, sub, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false)))
+            return done(rc);
+    }
+    void *dv, *di;
+    if ((rc = ensure(ctx, kSlotVec, (2 * (size_t)L + 8) * sizeof(double), &dv))) return done(rc);
+    if ((rc = ensure(ctx, kSlotDecodeI, ((size_t)L + 8) * sizeof(int32_t), &di))) return done(rc);
+    double* d_u = (double*)dv;
+    double* d_pairll = d_u + L;
+    double* d_total = d_pairll + L;
+    int32_t* d_col = (int32_t*)di;
+    std::vector<int32_t> colu(L, -1);
+    for (int i = 0; i < L; i++) {
+        if (col_pair[i] >= 0) colu[i] = pu[col_pair[i]];
+        else if (paired[i] > 0) colu[i] = -2;
+    }
+    if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, d_u, nullptr)))
+        return done(rc);
+    if ((rc = h2d(ctx, d_col, colu.data(), (size_t)L * sizeof(int32_t)))) return done(rc);
+    if ((rc = launch_structure_sum(ctx, L, d_u, d_col, sub ? sub->d_mix : nullptr, d_total, d_pairll)))
+        return done(rc);
+    if ((rc = d2h(ctx, total, d_total, sizeof(double)))) return done(rc);
+    if (pairll && (rc = d2h(ctx, pairll, d_pairll, (size_t)L * sizeof(double)))) return done(rc);
+    if (unpaired && (rc = d2h(ctx, unpaired, d_u, (size_t)L * sizeof(double)))) return done(rc);
+    return done(finish(ctx));
 }
 
 int messi_posteriors(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan,

@@ -60,7 +60,7 @@ __global__ void to_double_kernel(const float* __restrict__ in, double* __restric
 
 // pair: L x L as uploaded from the Julia matrix (column-major); it is read as
 // pair[i*L + k], the reference kernel's indexing (the matrix is symmetric).
-__global__ void __launch_bounds__(256) decode_wave_kernel(const float* __restrict__ single,
+__global__ void __launch_bounds__(kWaveMaxThreads) decode_wave_kernel(const float* __restrict__ single,
                                                           const float* __restrict__ pair, int L, float alpha,
                                                           float* __restrict__ erow, float* __restrict__ ecol,
                                                           int* __restrict__ scol, unsigned int* sync)
@@ -316,7 +316,7 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
         int Lv = L;
         void* args[] = {(void*)&f_single, (void*)&f_pair, &Lv, (void*)&a, &erow, &ecol, &d_scol, &d_sync};
         const int grid = wave_grid(ctx, (const void*)decode_wave_kernel, L);
-        e = cudaLaunchCooperativeKernel((const void*)decode_wave_kernel, dim3(grid), dim3(256), args, 0,
+        e = cudaLaunchCooperativeKernel((const void*)decode_wave_kernel, dim3(grid), dim3(wave_threads(ctx)), args, 0,
                                         ctx->stream);
         ctx->launches++;
         if (e != cudaSuccess) return cuda_fail(ctx, e, "decode_wave_kernel");

@@ -118,8 +118,10 @@ constexpr int kProfKernels = 4;
 
 struct messi_ctx {
     int device = 0;
-    // CTAs of the persistent wavefront kernels (0 = one per SM, fewer for short sequences)
+    // CTAs of the persistent wavefront kernels (0 = one per SM, fewer for short
+    // sequences) and their size (256, 512 or 1024 threads; 0 = 1024)
     int wave_ctas = 0;
+    int wave_threads = 0;
     // per-kernel event timing (messi_ctx_profile)
     bool profiling = false;
     std::vector<messi::ProfRec> prof_pending;
@@ -201,7 +203,11 @@ void host_muse(double lGC, double lAT, double lGT, const double* q, const double
 int host_reversible_eig(int n, const double* Q, const double* pi, double* w, double* U);
 
 // ---- plan (plan.cpp) ----
-int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8_t* pairmask, std::string* err);
+// Plan of the band pairs (y - x <= W, pairmask non-zero), or with `pairs`
+// of exactly those pairs (pair_unique[p] = unique root pair of pairs[p]; no
+// band index map).
+int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8_t* pairmask, std::string* err,
+               const std::vector<int2>* pairs = nullptr, std::vector<int32_t>* pair_unique = nullptr);
 int allocate_arena(messi_dataset* ds, int C, std::string* err);
 
 // Node descriptors of one dataset whose partial rows live at `arena_f/e` +
@@ -229,6 +235,9 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
 // d_P4 with node stride `pstride` (nodes of all site categories: [s][pstride][16]).
 int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int pstride, const double* d_pi4,
                     const double* d_logw_site, int nsite, double* d_u, double* d_scratch);
+// Fixed-structure sums (prune.cu, structure_sum_kernel).
+int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const double* d_mix, double* d_total,
+                         double* d_pairll);
 int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, double* d_out);
 int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask,
                              double B);
@@ -258,8 +267,9 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
 // d_paired: [nstruct][L]; d_stack: [nstruct][3 (L + 1)] ints; d_status: 1 uint.
 int run_sample_structures(messi_ctx* ctx, const Band& t, double B, int nstruct, unsigned long long seed,
                           int* d_paired, int* d_stack, unsigned int* d_status);
-// Grid size of a persistent wavefront kernel (cooperative launch, 256 threads).
+// Grid and CTA size of a persistent wavefront kernel (cooperative launch).
 int wave_grid(messi_ctx* ctx, const void* kernel, int L);
+int wave_threads(const messi_ctx* ctx);
 int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandBatch* bb, std::string* err);
 void bandbatch_free(BandBatch* bb);
 int launch_baseline_batch(messi_ctx* ctx, const BandBatch& bb, double B);

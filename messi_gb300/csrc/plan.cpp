@@ -49,7 +49,8 @@ struct KeyMap {
 
 }  // namespace
 
-int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8_t* pairmask, std::string* err)
+int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8_t* pairmask, std::string* err,
+               const std::vector<int2>* pairs, std::vector<int32_t>* pair_unique)
 {
     const int N = aln->numseqs, L = aln->numcols, nn = aln->numnodes;
     if (N < 2 || L < 1 || nn != 2 * N - 1 || !aln->masks || !aln->children || !aln->seqindex) {
@@ -152,12 +153,35 @@ int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8
         }
     }
 
-    // ---- unique pairs at the root (band + mask), band index map
+    // ---- unique pairs at the root (band + mask, or an explicit pair list), band index map
     const int W1 = W + 1;
-    std::vector<int32_t> bandidx((size_t)L * W1, -1);
+    std::vector<int32_t> bandidx(pairs ? (size_t)1 : (size_t)L * W1, -1);
     std::vector<std::vector<int32_t>> rep(nn);  // representative (x, y) per unique pair, interleaved
     ds->nunique.assign(nn, 0);
-    {
+    if (pairs) {
+        ds->band_pairs = (int64_t)pairs->size();
+        km.reset((size_t)std::min<int64_t>(ds->band_pairs, (int64_t)npat[0] * npat[0]));
+        pair_unique->assign(pairs->size(), -1);
+        int32_t n = 0;
+        for (size_t p = 0; p < pairs->size(); p++) {
+            const int x = (*pairs)[p].x, y = (*pairs)[p].y;
+            if (x < 0 || y >= L || x >= y) {
+                *err = "structure: pairs must satisfy 0 <= x < y < numcols";
+                return MESSI_EINVAL;
+            }
+            bool ins;
+            const int64_t key = (int64_t)pid[0][x] * npat[0] + pid[0][y];
+            const int32_t u = km.get_or_insert(key, n, &ins);
+            if (ins) {
+                rep[0].push_back(x);
+                rep[0].push_back(y);
+                n++;
+            }
+            (*pair_unique)[p] = u;
+        }
+        ds->nroot = n;
+        ds->nunique[0] = n;
+    } else {
         int64_t count_band = 0;
         for (int x = 0; x < L; x++) {
             int kmax = std::min(W, L - 1 - x);

@@ -578,4 +578,44 @@ int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, c
     return MESSI_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Fixed-structure likelihood: sum of the unpaired columns and of the pairs
+// (one block, FP64, fixed reduction order).  On return u holds the unpaired
+// log-likelihood of unpaired columns and 0 on paired ones (the reference's
+// computeunpairedlikelihoods(..., paired), src/FARCE.jl:1222-1250), pairll
+// the pair log-likelihood at the first column of each pair and 0 elsewhere.
+// ---------------------------------------------------------------------------
+// colu[c]: unique root pair of the pair opened at column c (>= 0), -2 on the
+// closing column of a pair, -1 on an unpaired column.
+__global__ void __launch_bounds__(1024) structure_sum_kernel(double* __restrict__ u, const int* __restrict__ colu,
+                                                             int L, const double* __restrict__ mix,
+                                                             double* __restrict__ total, double* __restrict__ pairll)
+{
+    __shared__ double part[1024];
+    double acc = 0.0;
+    for (int c = threadIdx.x; c < L; c += blockDim.x) {
+        const int k = colu[c];
+        const double pv = (k >= 0) ? mix[k] : 0.0;
+        if (k == -1) acc += u[c];
+        else u[c] = 0.0;
+        pairll[c] = pv;
+        acc += pv;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) part[threadIdx.x] += part[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) total[0] = part[0];
+}
+
+int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const double* d_mix, double* d_total,
+                         double* d_pairll)
+{
+    structure_sum_kernel<<<1, 1024, 0, ctx->stream>>>(d_u, d_colu, L, d_mix, d_total, d_pairll);
+    LAUNCH_CHECK(ctx, "structure_sum_kernel");
+    return MESSI_OK;
+}
+
 }  // namespace messi

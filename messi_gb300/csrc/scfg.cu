@@ -413,7 +413,7 @@ __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool va
 }
 
 // All band diagonals of the inside pass (span 0 initialisation included).
-__global__ void __launch_bounds__(256) inside_wave_kernel(Band t, Rules R, double B)
+__global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
     unsigned int gen = 0;
     const int L = t.L;
@@ -461,7 +461,7 @@ __device__ __forceinline__ int batch_band(const long long* __restrict__ cumL, in
     return lo;
 }
 
-__global__ void __launch_bounds__(256) inside_wave_batch_kernel(const Band* __restrict__ bands,
+__global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(const Band* __restrict__ bands,
                                                                 const long long* __restrict__ cumL,
                                                                 const int* __restrict__ wbs, int n, Rules R,
                                                                 double B, unsigned int* sync)
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256) inside_wave_batch_kernel(const Band* __re
 }
 
 // All band diagonals of the outside pass, descending spans.
-__global__ void __launch_bounds__(256) outside_wave_kernel(Band t, Rules R)
+__global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, Rules R)
 {
     unsigned int gen = 0;
     const int L = t.L, Wb = t.Wb, RS = t.RS;
@@ -584,10 +584,17 @@ __global__ void __launch_bounds__(256) outside_wave_kernel(Band t, Rules R)
     }
 }
 
+int wave_threads(const messi_ctx* ctx)
+{
+    const int t = ctx->wave_threads;
+    return (t == 256 || t == 512 || t == 1024) ? t : kWaveMaxThreads;
+}
+
 int wave_grid(messi_ctx* ctx, const void* kernel, int L)
 {
+    const int threads = wave_threads(ctx);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     int sms = ctx->num_sms;
     if (sms <= 0) {
@@ -596,8 +603,9 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         ctx->num_sms = sms;
     }
-    // one CTA per SM at most keeps the barrier cheap; a context may cap it lower
-    const int useful = (int)std::min<long long>((long long)L * 32 / 256 + 1, (long long)per_sm * sms);
+    // one CTA per SM at most keeps the barrier cheap (the CTA is large enough
+    // to keep the split-sum loads in flight); a context may cap it lower
+    const int useful = (int)std::min<long long>((long long)L * 32 / threads + 1, (long long)per_sm * sms);
     int grid = std::max(1, std::min(useful, sms));
     if (ctx->wave_ctas > 0) grid = std::min(grid, ctx->wave_ctas);
     return grid;
@@ -607,7 +615,7 @@ static int launch_wave(messi_ctx* ctx, const void* kernel, int grid, void** args
 {
     cudaError_t e = cudaMemsetAsync(t.sync, 0, 4 * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(256), args, 0, ctx->stream);
+    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(wave_threads(ctx)), args, 0, ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, what);
     return MESSI_OK;
@@ -763,7 +771,7 @@ int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
     prof_begin(ctx, 1, cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    e = cudaLaunchCooperativeKernel((const void*)inside_wave_batch_kernel, dim3(grid), dim3(256), args, 0,
+    e = cudaLaunchCooperativeKernel((const void*)inside_wave_batch_kernel, dim3(grid), dim3(wave_threads(ctx)), args, 0,
                                     ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_wave_batch_kernel");

@@ -7,6 +7,9 @@
 
 namespace messi {
 
+// Largest CTA of the persistent wavefront kernels (their launch bounds).
+constexpr int kWaveMaxThreads = 1024;
+
 // ---------------------------------------------------------------------------
 // grid barrier with a bounded wait (wavefront kernels)
 // ---------------------------------------------------------------------------
