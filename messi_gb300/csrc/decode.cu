@@ -315,8 +315,9 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
         const float a = (float)alpha;
         int Lv = L;
         void* args[] = {(void*)&f_single, (void*)&f_pair, &Lv, (void*)&a, &erow, &ecol, &d_scol, &d_sync};
-        const int grid = wave_grid(ctx, (const void*)decode_wave_kernel, L);
-        e = cudaLaunchCooperativeKernel((const void*)decode_wave_kernel, dim3(grid), dim3(wave_threads(ctx)), args, 0,
+        const int threads = wave_threads(ctx, 0.5 * (double)L * L);
+        const int grid = wave_grid(ctx, (const void*)decode_wave_kernel, L, threads);
+        e = cudaLaunchCooperativeKernel((const void*)decode_wave_kernel, dim3(grid), dim3(threads), args, 0,
                                         ctx->stream);
         ctx->launches++;
         if (e != cudaSuccess) return cuda_fail(ctx, e, "decode_wave_kernel");

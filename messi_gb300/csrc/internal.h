@@ -119,7 +119,7 @@ constexpr int kProfKernels = 4;
 struct messi_ctx {
     int device = 0;
     // CTAs of the persistent wavefront kernels (0 = one per SM, fewer for short
-    // sequences) and their size (256, 512 or 1024 threads; 0 = 1024)
+    // sequences) and their size (256, 512 or 1024 threads; 0 = by band size)
     int wave_ctas = 0;
     int wave_threads = 0;
     // per-kernel event timing (messi_ctx_profile)
@@ -268,8 +268,8 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
 int run_sample_structures(messi_ctx* ctx, const Band& t, double B, int nstruct, unsigned long long seed,
                           int* d_paired, int* d_stack, unsigned int* d_status);
 // Grid and CTA size of a persistent wavefront kernel (cooperative launch).
-int wave_grid(messi_ctx* ctx, const void* kernel, int L);
-int wave_threads(const messi_ctx* ctx);
+int wave_threads(const messi_ctx* ctx, double band_cells);
+int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads);
 int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandBatch* bb, std::string* err);
 void bandbatch_free(BandBatch* bb);
 int launch_baseline_batch(messi_ctx* ctx, const BandBatch& bb, double B);

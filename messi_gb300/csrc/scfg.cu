@@ -584,15 +584,19 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
     }
 }
 
-int wave_threads(const messi_ctx* ctx)
+// CTA size of a persistent wavefront launch.  The split sums are bound by
+// the latency of their L2 loads: long bands need many warps per SM to keep
+// enough loads in flight, short ones pay more for the larger CTA barrier
+// than they gain (GB300: 256 threads best at L x W = 0.5e6, 1024 at 7e6).
+int wave_threads(const messi_ctx* ctx, double cells)
 {
     const int t = ctx->wave_threads;
-    return (t == 256 || t == 512 || t == 1024) ? t : kWaveMaxThreads;
+    if (t == 256 || t == 512 || t == 1024) return t;
+    return cells < 1.5e6 ? 256 : (cells < 4e6 ? 512 : kWaveMaxThreads);
 }
 
-int wave_grid(messi_ctx* ctx, const void* kernel, int L)
+int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
 {
-    const int threads = wave_threads(ctx);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
@@ -603,19 +607,20 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         ctx->num_sms = sms;
     }
-    // one CTA per SM at most keeps the barrier cheap (the CTA is large enough
-    // to keep the split-sum loads in flight); a context may cap it lower
+    // one CTA per SM at most keeps the barrier cheap; a context may cap it lower
     const int useful = (int)std::min<long long>((long long)L * 32 / threads + 1, (long long)per_sm * sms);
     int grid = std::max(1, std::min(useful, sms));
     if (ctx->wave_ctas > 0) grid = std::min(grid, ctx->wave_ctas);
     return grid;
 }
 
-static int launch_wave(messi_ctx* ctx, const void* kernel, int grid, void** args, const Band& t, const char* what)
+static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, const Band& t, const char* what)
 {
+    const int threads = wave_threads(ctx, (double)t.L * (t.Wb + 1));
+    const int grid = wave_grid(ctx, kernel, t.L, threads);
     cudaError_t e = cudaMemsetAsync(t.sync, 0, 4 * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(wave_threads(ctx)), args, 0, ctx->stream);
+    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, what);
     return MESSI_OK;
@@ -635,9 +640,8 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     Band tt = t;
     double Bv = B;
     void* args[] = {&tt, &R, &Bv};
-    const int grid = wave_grid(ctx, (const void*)inside_wave_kernel, t.L);
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc = launch_wave(ctx, (const void*)inside_wave_kernel, grid, args, t, "inside_wave_kernel");
+    int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t, "inside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
@@ -764,14 +768,18 @@ int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
     double Bv = B;
     unsigned int* sync = bb.d_sync;
     void* args[] = {&bands, &cum, &wbs, &n, &R, &Bv, &sync};
+    double cells = 0.0, band = 0.0;
+    for (const Band& t : bb.host) {
+        cells += (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0);
+        band += (double)t.L * (t.Wb + 1);
+    }
+    const int threads = wave_threads(ctx, band);
     const int grid = wave_grid(ctx, (const void*)inside_wave_batch_kernel,
-                               (int)std::min<long long>(bb.total_cols, 1 << 30));
-    double cells = 0.0;
-    for (const Band& t : bb.host) cells += (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0);
+                               (int)std::min<long long>(bb.total_cols, 1 << 30), threads);
     prof_begin(ctx, 1, cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    e = cudaLaunchCooperativeKernel((const void*)inside_wave_batch_kernel, dim3(grid), dim3(wave_threads(ctx)), args, 0,
+    e = cudaLaunchCooperativeKernel((const void*)inside_wave_batch_kernel, dim3(grid), dim3(threads), args, 0,
                                     ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_wave_batch_kernel");
@@ -843,9 +851,8 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
     }
     Band tt = t;
     void* args[] = {&tt, &R};
-    const int grid = wave_grid(ctx, (const void*)outside_wave_kernel, t.L);
     prof_begin(ctx, 3, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc = launch_wave(ctx, (const void*)outside_wave_kernel, grid, args, t, "outside_wave_kernel");
+    int rc = launch_wave(ctx, (const void*)outside_wave_kernel, args, t, "outside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     return queue_status_readback(ctx, t);
