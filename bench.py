@@ -39,9 +39,9 @@ WORKLOAD_TEXT = {"c2": "c2: 64 seqs x 1,000 nt, max pair span 500",
                  "c1": "c1: 16 seqs x 120 nt, all pairs"}
 BYTES_PER_UPDATE = 212  # algorithmic bytes of one node update (2 child rows + exps + indices in, 1 row out)
 # DRAM bytes (read + write) per node update of the pruning kernel from one ncu
-# capture of the c2-shaped profiling case, weighted over its interior-level
-# launches (profiles/prune_level_kernel_c2p.md); scaled by updates per launch.
-TRAFFIC_BYTES_PER_UPDATE = 150.0
+# capture of the c2-shaped profiling case, weighted over two interior-level
+# launches (profiles/prune_mma_kernel_c2p.md); scaled by updates per launch.
+TRAFFIC_BYTES_PER_UPDATE = 120.0
 
 
 def measured_peaks():
@@ -344,7 +344,7 @@ def run_ours(args):
         "frac": (achieved / peak) if achieved else None,
         "traffic": (TRAFFIC_BYTES_PER_UPDATE * units_per_launch) if (TRAFFIC_BYTES_PER_UPDATE and units_per_launch)
         else None,
-        "kernel": "prune_level_kernel", "peak_source": f"{peak_kind} hbm_gbs",
+        "kernel": "prune_mma_kernel", "peak_source": f"{peak_kind} hbm_gbs",
         "bytes_per_unit": BYTES_PER_UPDATE, "unit_name": "node update (pair x category x internal node)",
         "units_per_launch": units_per_launch, "launches": p_n, "avg_launch_ms": p_ms / p_n if p_n else None,
         "kernel_ms_per_step": p_ms / nprof,

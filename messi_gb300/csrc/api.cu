@@ -126,7 +126,7 @@ int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool p
                  const uint8_t* gapmask, ModelDev* md)
 {
     std::string err;
-    int rc = build_categories(m, ds->numnodes, &md->cat, &err);
+    int rc = build_categories(m, ds->numnodes, &md->cat, &err, pairs);
     if (rc) return fail(ctx, rc, err);
     Categories& c = md->cat;
     Staged st;

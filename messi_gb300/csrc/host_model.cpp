@@ -132,7 +132,7 @@ static double safe_log(double x) { return x > 0.0 ? std::log(x) : -INFINITY; }
 // Categories in the reference order: siteCat1 outer, siteCat2, lambda inner
 // (src/FelsensteinCUDA.jl:277-279), weight log(w1) + log(w2) + log(w_lambda)
 // (src/FelsensteinCUDA.jl:403-418).
-int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err)
+int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs)
 {
     if (!m || m->nsite < 1 || m->nlambda < 1 || !m->siteRates || !m->siteWeights || !m->lambdaGC ||
         !m->lambdaAT || !m->lambdaGT || !m->lambdaWeights || !m->branchlengths) {
@@ -171,26 +171,34 @@ int build_categories(const messi_model* m, int numnodes, Categories* out, std::s
     c.pi16.assign((size_t)c.C * 16, 0.f);
     c.logw.assign(c.C, 0.0);
     c.lam.assign(c.C, 0);
-    int k = 0;
-    for (int s1 = 0; s1 < m->nsite; s1++)
-        for (int s2 = 0; s2 < m->nsite; s2++)
-            for (int l = 0; l < m->nlambda; l++, k++) {
-                double Q[256], pi16[16];
-                host_muse(m->lambdaGC[l], m->lambdaAT[l], m->lambdaGT[l], m->q, m->freqs, m->siteRates[s1],
-                          m->siteRates[s2], Q);
-                host_musefreqs(m->freqs, m->lambdaGC[l], m->lambdaAT[l], m->lambdaGT[l], pi16);
-                double* e = &c.eig[(size_t)k * kEigStride];
-                if (host_reversible_eig(16, Q, pi16, e, e + 16)) {
-                    *err = "model: rate matrix is not diagonalisable";
-                    return MESSI_EINVAL;
-                }
-                for (int a = 0; a < 16; a++) {
-                    e[16 + 256 + a] = std::sqrt(pi16[a]);
-                    c.pi16[(size_t)k * 16 + a] = (float)pi16[a];
-                }
-                c.logw[k] = safe_log(m->siteWeights[s1]) + safe_log(m->siteWeights[s2]) + safe_log(m->lambdaWeights[l]);
-                c.lam[k] = l;
-            }
+    // the 16-state eigensystems are independent: one per host thread
+    std::vector<int> bad(c.C, 0);
+    const int nl = m->nlambda, ns = m->nsite;
+#pragma omp parallel for schedule(dynamic, 1) if (pairs && c.C >= 4)
+    for (int k = 0; k < c.C; k++) {
+        const int s1 = k / (ns * nl), s2 = (k / nl) % ns, l = k % nl;
+        c.logw[k] = safe_log(m->siteWeights[s1]) + safe_log(m->siteWeights[s2]) + safe_log(m->lambdaWeights[l]);
+        c.lam[k] = l;
+        if (!pairs) continue;
+        double Q[256], pi16[16];
+        host_muse(m->lambdaGC[l], m->lambdaAT[l], m->lambdaGT[l], m->q, m->freqs, m->siteRates[s1],
+                  m->siteRates[s2], Q);
+        host_musefreqs(m->freqs, m->lambdaGC[l], m->lambdaAT[l], m->lambdaGT[l], pi16);
+        double* e = &c.eig[(size_t)k * kEigStride];
+        if (host_reversible_eig(16, Q, pi16, e, e + 16)) {
+            bad[k] = 1;
+            continue;
+        }
+        for (int a = 0; a < 16; a++) {
+            e[16 + 256 + a] = std::sqrt(pi16[a]);
+            c.pi16[(size_t)k * 16 + a] = (float)pi16[a];
+        }
+    }
+    for (int k = 0; k < c.C; k++)
+        if (bad[k]) {
+            *err = "model: rate matrix is not diagonalisable";
+            return MESSI_EINVAL;
+        }
     // unpaired 4-state model per site rate: gtr(q, freqs) * rate (src/FARCE.jl:742-750)
     c.eig4.assign((size_t)m->nsite * kEig4Stride, 0.0);
     c.logw_site.assign(m->nsite, 0.0);
