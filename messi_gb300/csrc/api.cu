@@ -294,6 +294,8 @@ int messi_ctx_create(int device, messi_ctx** out)
         if (w) ctx->wave_ctas = std::max(0, std::atoi(w));
         const char* wt = std::getenv("MESSI_WAVE_THREADS");
         if (wt) ctx->wave_threads = std::atoi(wt);
+        const char* wm = std::getenv("MESSI_WAVE_MODE");
+        if (wm) ctx->wave_mode = std::strcmp(wm, "grid") == 0 ? 1 : (std::strcmp(wm, "cluster") == 0 ? 2 : 0);
     }
     *out = ctx;
     return MESSI_OK;

@@ -43,8 +43,6 @@ struct messi_batch {
     int64_t total_rows = 0;
     int chunk = 0, arena_C = 0;
     BandBatch bands;
-    double* d_unp = nullptr;  // unpaired scratch: nodes x columns x 5 doubles per alignment
-    std::vector<int64_t> unp_off;
     DevBuf stage, P16, P4;
     int64_t executed = 0, naive = 0, band_pairs = 0, nroot = 0;
 };
@@ -84,7 +82,7 @@ void destroy_batch(messi_batch* b)
     if (!b) return;
     for (messi_dataset* d : b->ds)
         if (d) messi_dataset_destroy(d);
-    void* bufs[] = {b->d_tiles, b->d_nodes, b->d_arena_f, b->d_arena_e, b->d_unp, b->stage.p, b->P16.p, b->P4.p};
+    void* bufs[] = {b->d_tiles, b->d_nodes, b->d_arena_f, b->d_arena_e, b->stage.p, b->P16.p, b->P4.p};
     for (void* p : bufs)
         if (p) cudaFree(p);
     bandbatch_free(&b->bands);
@@ -174,8 +172,6 @@ int messi_batch_create(messi_ctx* ctx, int32_t n, const messi_alignment* alns, c
     b->node_base.resize(n);
     b->col_base.resize(n);
     b->row_base.resize(n);
-    b->unp_off.resize(n);
-    int64_t unp = 0;
     for (int a = 0; a < n; a++) {
         const messi_dataset* d = b->ds[a];
         b->node_base[a] = b->total_nodes;
@@ -184,8 +180,6 @@ int messi_batch_create(messi_ctx* ctx, int32_t n, const messi_alignment* alns, c
         b->total_cols += d->L;
         b->row_base[a] = b->total_rows;
         b->total_rows += d->arena_rows;
-        b->unp_off[a] = unp;
-        unp += (int64_t)d->numnodes * d->L * 5;
         b->H = std::max(b->H, d->H);
         b->executed += d->executed;
         b->naive += d->naive;
@@ -219,7 +213,6 @@ int messi_batch_create(messi_ctx* ctx, int32_t n, const messi_alignment* alns, c
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_nodes, sizeof(NodeDev) * std::max(1, b->total_nodes));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_unp, sizeof(double) * std::max<int64_t>(unp, 1));
     if (e != cudaSuccess) {
         destroy_batch(b);
         return cuda_fail(ctx, e, "batch upload");
@@ -378,12 +371,12 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
             }
         }
     }
-    // unpaired columns, baselines, banded pair scores, batched inside
+    // unpaired columns (one scratch buffer, reused in stream order), baselines,
+    // banded pair scores, batched inside
     for (int a = 0; a < n; a++) {
         const Band& t = b->bands.host[b->bands.slot[a]];
         if ((rc = launch_unpaired(ctx, b->ds[a], (const double*)p4 + (size_t)b->node_base[a] * 16, b->total_nodes,
-                                  d_pi4 + 4 * grp[a], d_lws + (size_t)nsite * grp[a], nsite, t.u,
-                                  b->d_unp + b->unp_off[a])))
+                                  d_pi4 + 4 * grp[a], d_lws + (size_t)nsite * grp[a], nsite, t.u, nullptr)))
             return rc;
     }
     if ((rc = launch_baseline_batch(ctx, b->bands, 1.0))) return rc;

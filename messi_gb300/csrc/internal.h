@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/messi_gb300.h"
@@ -122,6 +123,9 @@ struct messi_ctx {
     // sequences) and their size (256, 512 or 1024 threads; 0 = by band size)
     int wave_ctas = 0;
     int wave_threads = 0;
+    // 0 = choose per pass, 1 = grid barrier, 2 = one thread-block cluster
+    int wave_mode = 0;
+    std::vector<std::pair<const void*, int>> cluster_sizes;  // kernel -> cluster size (0: none)
     // per-kernel event timing (messi_ctx_profile)
     bool profiling = false;
     std::vector<messi::ProfRec> prof_pending;
@@ -234,6 +238,8 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
               const int* d_lam, int C, int nlam, bool per_lambda);
 // Unpaired column likelihoods of one tree whose transition matrices start at
 // d_P4 with node stride `pstride` (nodes of all site categories: [s][pstride][16]).
+// d_scratch: nsite * (numnodes * L * 5 + L) doubles, or nullptr for the
+// context's buffer (reused in stream order).
 int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int pstride, const double* d_pi4,
                     const double* d_logw_site, int nsite, double* d_u, double* d_scratch);
 // Fixed-structure sums (prune.cu, structure_sum_kernel).

@@ -435,65 +435,79 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
 }
 
 // ---------------------------------------------------------------------------
-// Unpaired columns: one thread per column, nodes in post-order, partials of
-// every node kept in a [numnodes][L][4] scratch table (FP64).
+// Unpaired columns: one thread per (column, site-rate category), nodes in
+// post-order, partials of every node kept in a [nsite][numnodes][L][4]
+// scratch table (FP64; the FP64 pipe is narrow on this part, so the work is
+// spread over many small blocks); then the mixture over site rates in the
+// reference's order.
 // ---------------------------------------------------------------------------
-__global__ void unpaired_kernel(const uint8_t* __restrict__ masks, const int* __restrict__ tree,
-                                const int* __restrict__ post, int nn, int L, const double* __restrict__ P4,
-                                int pstride, const double* __restrict__ pi4, const double* __restrict__ logw_site,
-                                int nsite, double* __restrict__ part, double* __restrict__ lmv,
-                                double* __restrict__ u)
+__global__ void __launch_bounds__(32) unpaired_site_kernel(const uint8_t* __restrict__ masks,
+                                                           const int* __restrict__ tree, const int* __restrict__ post,
+                                                           int nn, int L, const double* __restrict__ P4, int pstride,
+                                                           const double* __restrict__ pi4, double* __restrict__ part,
+                                                           double* __restrict__ lmv, double* __restrict__ ll)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (x >= L) return;
+    const double* Ps = P4 + (size_t)s * pstride * 16;
+    double* ps = part + (size_t)s * nn * L * 4;
+    double* ls = lmv + (size_t)s * nn * L;
+    for (int t = 0; t < nn; t++) {
+        const int v = post[t];
+        const int c0 = tree[4 * v], c1 = tree[4 * v + 1];
+        double* pv = ps + ((size_t)v * L + x) * 4;
+        if (c0 < 0) {
+            const int m = masks[(size_t)tree[4 * v + 2] * L + x];
+#pragma unroll
+            for (int a = 0; a < 4; a++) pv[a] = (double)((m >> a) & 1);
+            ls[(size_t)v * L + x] = 0.0;
+            continue;
+        }
+        const double* p0 = ps + ((size_t)c0 * L + x) * 4;
+        const double* p1 = ps + ((size_t)c1 * L + x) * 4;
+        const double* P0 = Ps + (size_t)c0 * 16;
+        const double* P1 = Ps + (size_t)c1 * 16;
+        double l[4], r[4], o[4], m = -INFINITY;
+#pragma unroll
+        for (int a = 0; a < 4; a++) { l[a] = p0[a]; r[a] = p1[a]; }
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            double sl = 0.0, sr = 0.0;
+#pragma unroll
+            for (int d = 0; d < 4; d++) {
+                sl += __ldg(P0 + a * 4 + d) * l[d];
+                sr += __ldg(P1 + a * 4 + d) * r[d];
+            }
+            o[a] = sl * sr;
+            m = fmax(m, o[a]);
+        }
+        double lm = ls[(size_t)c0 * L + x] + ls[(size_t)c1 * L + x];
+        if (m < 1e-20) {  // src/FARCE.jl:2226-2238
+#pragma unroll
+            for (int a = 0; a < 4; a++) o[a] /= m;
+            lm += log(m);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) pv[a] = o[a];
+        ls[(size_t)v * L + x] = lm;
+    }
+    const double* pr = ps + (size_t)x * 4;  // root = node 0
+    double tot = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) tot += pi4[a] * pr[a];
+    ll[(size_t)s * L + x] = log(tot) + ls[x];
+}
+
+__global__ void unpaired_mix_kernel(const double* __restrict__ ll, const double* __restrict__ logw_site, int nsite,
+                                    int L, double* __restrict__ u)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= L) return;
     double acc = -INFINITY;
     for (int s = 0; s < nsite; s++) {
-        const double* Ps = P4 + (size_t)s * pstride * 16;
-        for (int t = 0; t < nn; t++) {
-            const int v = post[t];
-            const int c0 = tree[4 * v], c1 = tree[4 * v + 1];
-            double* pv = part + ((size_t)v * L + x) * 4;
-            if (c0 < 0) {
-                const int m = masks[(size_t)tree[4 * v + 2] * L + x];
-#pragma unroll
-                for (int a = 0; a < 4; a++) pv[a] = (double)((m >> a) & 1);
-                lmv[(size_t)v * L + x] = 0.0;
-                continue;
-            }
-            const double* p0 = part + ((size_t)c0 * L + x) * 4;
-            const double* p1 = part + ((size_t)c1 * L + x) * 4;
-            const double* P0 = Ps + (size_t)c0 * 16;
-            const double* P1 = Ps + (size_t)c1 * 16;
-            double l[4], r[4], o[4], m = -INFINITY;
-#pragma unroll
-            for (int a = 0; a < 4; a++) { l[a] = p0[a]; r[a] = p1[a]; }
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-                double sl = 0.0, sr = 0.0;
-#pragma unroll
-                for (int d = 0; d < 4; d++) {
-                    sl += P0[a * 4 + d] * l[d];
-                    sr += P1[a * 4 + d] * r[d];
-                }
-                o[a] = sl * sr;
-                m = fmax(m, o[a]);
-            }
-            double lm = lmv[(size_t)c0 * L + x] + lmv[(size_t)c1 * L + x];
-            if (m < 1e-20) {  // src/FARCE.jl:2226-2238
-#pragma unroll
-                for (int a = 0; a < 4; a++) o[a] /= m;
-                lm += log(m);
-            }
-#pragma unroll
-            for (int a = 0; a < 4; a++) pv[a] = o[a];
-            lmv[(size_t)v * L + x] = lm;
-        }
-        const double* pr = part + (size_t)x * 4;  // root = node 0
-        double tot = 0.0;
-#pragma unroll
-        for (int a = 0; a < 4; a++) tot += pi4[a] * pr[a];
-        const double ll = log(tot) + lmv[x] + logw_site[s];
-        acc = (s == 0) ? ll : lse_d(acc, ll);
+        const double v = ll[(size_t)s * L + x] + logw_site[s];
+        acc = (s == 0) ? v : lse_d(acc, v);
     }
     u[x] = acc;
 }
@@ -501,21 +515,23 @@ __global__ void unpaired_kernel(const uint8_t* __restrict__ masks, const int* __
 int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int pstride, const double* d_pi4,
                     const double* d_logw_site, int nsite, double* d_u, double* d_scratch)
 {
-    // d_scratch: numnodes * L * 5 doubles, or nullptr for the context's buffer
+    // d_scratch: nsite * (numnodes * L * 5 + L) doubles, or nullptr for the context's buffer
     const size_t n = (size_t)ds->numnodes * ds->L;
     if (!d_scratch) {
         void* scratch;
-        int rc = ensure(ctx, 20, n * 5 * sizeof(double), &scratch);
+        int rc = ensure(ctx, 20, ((size_t)nsite * (n * 5 + ds->L)) * sizeof(double), &scratch);
         if (rc) return rc;
         d_scratch = (double*)scratch;
     }
     double* part = d_scratch;
-    double* lmv = part + n * 4;
-    const int bs = 128;
-    unpaired_kernel<<<(ds->L + bs - 1) / bs, bs, 0, ctx->stream>>>(ds->d_masks, ds->d_tree, ds->d_post,
-                                                                   ds->numnodes, ds->L, d_P4, pstride, d_pi4,
-                                                                   d_logw_site, nsite, part, lmv, d_u);
-    LAUNCH_CHECK(ctx, "unpaired_kernel");
+    double* lmv = part + (size_t)nsite * n * 4;
+    double* ll = lmv + (size_t)nsite * n;
+    const int bs = 32;
+    unpaired_site_kernel<<<dim3((ds->L + bs - 1) / bs, nsite), bs, 0, ctx->stream>>>(
+        ds->d_masks, ds->d_tree, ds->d_post, ds->numnodes, ds->L, d_P4, pstride, d_pi4, part, lmv, ll);
+    LAUNCH_CHECK(ctx, "unpaired_site_kernel");
+    unpaired_mix_kernel<<<(ds->L + 127) / 128, 128, 0, ctx->stream>>>(ll, d_logw_site, nsite, ds->L, d_u);
+    LAUNCH_CHECK(ctx, "unpaired_mix_kernel");
     return MESSI_OK;
 }
 

@@ -413,12 +413,13 @@ __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool va
 }
 
 // All band diagonals of the inside pass (span 0 initialisation included).
+template <int MODE>
 __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
     unsigned int gen = 0;
     const int L = t.L;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
-    if (!grid_sync(t.sync, gen)) return;
+    if (!wave_sync<MODE>(t.sync, gen)) return;
     for (int d = 1; d <= t.Wb; d++) {
         const int G = group_width(d);
         const int gpb = blockDim.x / G;
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
             const int i = base + gid0;
             inside_cell(t, i, d, i < ncell, lane, G, R);
         }
-        if (!grid_sync(t.sync, gen)) return;
+        if (!wave_sync<MODE>(t.sync, gen)) return;
     }
 }
 
@@ -496,6 +497,7 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
 }
 
 // All band diagonals of the outside pass, descending spans.
+template <int MODE>
 __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, Rules R)
 {
     unsigned int gen = 0;
@@ -580,7 +582,7 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
                 if (j == L - 1) t.Osuf[i] = oS;
             }
         }
-        if (!grid_sync(t.sync, gen)) return;
+        if (!wave_sync<MODE>(t.sync, gen)) return;
     }
 }
 
@@ -614,16 +616,84 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
     return grid;
 }
 
-static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, const Band& t, const char* what)
+// Cluster mode: one thread-block cluster runs the whole wavefront and
+// synchronises with the hardware cluster barrier.  It wins while a diagonal
+// holds little work (the grid barrier costs ~5 us per diagonal); long bands
+// need the whole GPU.  Returns the cluster size to use, 0 for grid mode.
+static int probe_cluster_size(const void* kernel, int threads)
 {
-    const int threads = wave_threads(ctx, (double)t.L * (t.Wb + 1));
-    const int grid = wave_grid(ctx, kernel, t.L, threads);
-    cudaError_t e = cudaMemsetAsync(t.sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    for (int cl : {16, 8}) {
+        if (cl > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cl);
+        cfg.blockDim = dim3(threads);
+        cudaLaunchAttribute at;
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = cl;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        cfg.attrs = &at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, kernel, &cfg) == cudaSuccess && nclusters >= 1) return cl;
+        cudaGetLastError();
+    }
+    return 0;
+}
+
+static int wave_cluster_size(messi_ctx* ctx, const void* kernel, int threads, double terms_per_diag)
+{
+    if (ctx->wave_mode == 1) return 0;
+    if (ctx->wave_mode != 2 && terms_per_diag > 1.0e6) return 0;
+    // the largest cluster the device runs for this kernel, found once per context
+    for (const auto& kv : ctx->cluster_sizes)
+        if (kv.first == kernel) return kv.second;
+    const int cl = probe_cluster_size(kernel, threads);
+    ctx->cluster_sizes.push_back({kernel, cl});
+    return cl;
+}
+
+// Launch a wavefront kernel pair (grid-barrier and cluster-barrier builds).
+static int launch_wave2(messi_ctx* ctx, const void* grid_kernel, const void* cluster_kernel, void** args,
+                        unsigned int* sync, int L, double band_cells, double terms_per_diag, const char* what)
+{
+    int threads = wave_threads(ctx, band_cells);
+    const int cl = wave_cluster_size(ctx, cluster_kernel, kWaveMaxThreads, terms_per_diag);
+    cudaError_t e = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
+    if (cl > 0) {
+        threads = kWaveMaxThreads;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cl);
+        cfg.blockDim = dim3(threads);
+        cfg.stream = ctx->stream;
+        cudaLaunchAttribute at;
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = cl;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        cfg.attrs = &at;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelExC(&cfg, cluster_kernel, args);
+    } else {
+        const int grid = wave_grid(ctx, grid_kernel, L, threads);
+        e = cudaLaunchCooperativeKernel(grid_kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
+    }
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, what);
     return MESSI_OK;
+}
+
+// split terms per diagonal of a band pass, averaged over its diagonals
+static double band_terms_per_diag(int L, int Wb)
+{
+    if (Wb < 1) return 0.0;
+    double terms = 0.0;
+    for (int d = 1; d <= Wb; d++) terms += (double)(L - d) * d;
+    return terms / Wb;
 }
 
 int queue_status_readback(messi_ctx* ctx, const Band& t)
@@ -641,7 +711,8 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     double Bv = B;
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t, "inside_wave_kernel");
+    int rc = launch_wave2(ctx, (const void*)inside_wave_kernel<kGrid>, (const void*)inside_wave_kernel<kCluster>, args,
+                          t.sync, t.L, (double)t.L * (t.Wb + 1), band_terms_per_diag(t.L, t.Wb), "inside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
@@ -852,7 +923,9 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
     Band tt = t;
     void* args[] = {&tt, &R};
     prof_begin(ctx, 3, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc = launch_wave(ctx, (const void*)outside_wave_kernel, args, t, "outside_wave_kernel");
+    int rc = launch_wave2(ctx, (const void*)outside_wave_kernel<kGrid>, (const void*)outside_wave_kernel<kCluster>,
+                          args, t.sync, t.L, (double)t.L * (t.Wb + 1), 2.0 * band_terms_per_diag(t.L, t.Wb),
+                          "outside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     return queue_status_readback(ctx, t);

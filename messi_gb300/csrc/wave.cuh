@@ -58,6 +58,23 @@ static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
     return s_ok != 0;
 }
 
+// Synchronisation of the wavefront kernels.  kGrid: the bounded grid
+// barrier above (any grid of co-resident CTAs); kCluster: the hardware
+// barrier of one thread-block cluster (the whole launch is one cluster), a
+// release/acquire at cluster scope.  Cells written by other CTAs of the
+// cluster are read through L2 (__ldcg) as in grid mode.
+enum WaveSync { kGrid = 0, kCluster = 1 };
+
+template <int MODE>
+static __device__ __forceinline__ bool wave_sync(unsigned int* sync, unsigned int& gen)
+{
+    if (MODE == kCluster) {
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+        return true;
+    }
+    return grid_sync(sync, gen);
+}
+
 static __device__ __forceinline__ int group_width(int nterms)
 {
     return nterms <= 8 ? 1 : (nterms <= 32 ? 4 : (nterms <= 96 ? 8 : (nterms <= 256 ? 16 : 32)));
