@@ -547,6 +547,70 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_structures(args):
+    """Structure outputs on the c2 alignment: posterior decoding (ours vs the
+    reference's posteriordecoding kernel replayed on the same GPU), the
+    device-resident consensus chain, stochastic sampling and the
+    fixed-structure likelihood.  Prints its own JSON line (wall times of the
+    host-facing calls, medians over --steps)."""
+    import numpy as np
+    import torch
+
+    from messi_gb300 import api, synth
+    from messi_gb300 import model as M
+    s = synth.make_workload(args.workload, seed=1)
+    ds = s.dataset
+    L, W = ds.numcols, s.W
+    prm = M.getparams(s.params15, ds.branchlengths)
+    ctx = api.get_context(0)
+    u = api.computeunpairedlikelihoods(ds, prm, ctx=ctx)
+    mat, _ = api.felsensteincuda(ds, prm, None, W, ctx=ctx)
+    api.maskgapped(mat, ds.gapfrequency, 1.0, -np.inf)
+    _, single, pair = api.computeposteriors(u, mat, ctx=ctx)
+    paired1 = np.where(s.paired >= 0, s.paired + 1, 0)
+
+    def timed(fn, n):
+        out, ts = None, []
+        for k in range(args.warmup + n):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                ts.append(1e3 * (time.perf_counter() - t0))
+        return out, statistics.median(ts)
+
+    nsamp = 1000
+    (e, sm), t_dec = timed(lambda: api.computeposteriordecodingcuda(single, pair, 2.0, ctx=ctx), args.steps)
+    cons, t_cons = timed(lambda: api.consensusstructure(u, mat, ctx=ctx), args.steps)
+    post, t_post = timed(lambda: api.computeposteriors(u, mat, ctx=ctx), args.steps)
+    (S, pri), t_samp = timed(lambda: api.samplestructures(u, mat, nsamp, seed=3, ctx=ctx), args.steps)
+    fx, t_fix = timed(lambda: api._structure_call(ds, prm, paired1, ctx), args.steps)
+    band, t_band = timed(lambda: api.computestructureintegratedlikelihood(ds, prm, W, ctx=ctx), args.steps)
+    ref = None
+    try:
+        from oracle import ref_kernels as rk
+        if rk.available():
+            (er, sr), t_ref = timed(lambda: rk.posterior_decoding(single, pair, 2.0), max(1, min(args.steps, 3)))
+            ref = {"ms": t_ref, "bit_identical_e": bool(np.array_equal(e, er.astype(np.float64))),
+                   "bit_identical_s": bool(np.array_equal(sm, sr)),
+                   "kind": "reference posteriordecoding kernel (src/cuda/inside.cu) compiled unmodified, one "
+                           "launch per span as src/InsideCUDA.jl:202-204"}
+    except Exception as exc:
+        ref = {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
+    npairs_struct = int(np.count_nonzero(paired1) // 2)
+    line = {"metric": "structure outputs (ms per call)", "workload": WORKLOAD_TEXT[args.workload],
+            "steps": args.steps, "warmup": args.warmup,
+            "posterior_decoding_ms": t_dec, "decoding_cells": L * (L - 1) // 2,
+            "reference_decoding": ref,
+            "posteriors_ms": t_post, "consensus_chain_ms": t_cons,
+            "consensus_pairs": int(np.count_nonzero(cons) // 2),
+            "sampling_ms": t_samp, "structures_per_s": nsamp / (t_samp / 1e3), "samples": nsamp,
+            "fixed_structure_ms": t_fix, "fixed_structure_pairs": npairs_struct,
+            "band_likelihood_ms": t_band}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -558,6 +622,8 @@ def main():
     ap.add_argument("--mcmc", action="store_true", help="run the MCMC comparison (config 5) instead")
     ap.add_argument("--mcmc-iters", type=int, default=20000)
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT))
+    ap.add_argument("--structures", action="store_true",
+                    help="time the structure outputs (decoding, consensus, sampling, fixed structure)")
     ap.add_argument("--batch", choices=["c3", "c3s"], default=None,
                     help="time the batched evaluation of a batch workload instead (own JSON line)")
     ap.add_argument("--profile-only", action="store_true",
@@ -569,6 +635,8 @@ def main():
         run_mcmc(args)
     elif args.batch:
         run_batch(args)
+    elif args.structures:
+        run_structures(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

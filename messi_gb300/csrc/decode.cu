@@ -83,7 +83,23 @@ __global__ void __launch_bounds__(kWaveMaxThreads) decode_wave_kernel(const floa
                 const float* prow = pair + (size_t)i * L;
                 const float* er = erow + (size_t)(i + 1) * L;  // e(i+1, k-1)
                 const float* ec = ecol + (size_t)j * L;        // e(k+1, j)
-                for (int k = i + 1 + lane; k <= j - 1; k += G) {
+                int k = i + 1 + lane;
+                // four splits per step, loads issued together, compared in ascending k
+                for (; k + 3 * G <= j - 1; k += 4 * G) {
+                    float v[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int kq = k + q * G;
+                        v[q] = __fmaf_rn(alpha, __ldg(prow + kq), __ldcg(er + kq - 1)) + __ldcg(ec + kq + 1);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (v[q] > bv) {
+                            bv = v[q];
+                            bk = k + q * G;
+                        }
+                }
+                for (; k <= j - 1; k += G) {
                     const float v = __fmaf_rn(alpha, __ldg(prow + k), __ldcg(er + k - 1)) + __ldcg(ec + k + 1);
                     if (v > bv) {
                         bv = v;

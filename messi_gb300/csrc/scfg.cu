@@ -67,6 +67,26 @@ __device__ __forceinline__ void lse_add4(float& m, float& s, float x0, float x1,
     s += (__expf(x0 - m) + __expf(x1 - m)) + (__expf(x2 - m) + __expf(x3 - m));
 }
 
+// Eight terms at once (sixteen independent loads in flight per lane).
+__device__ __forceinline__ void lse_add8(float& m, float& s, const float (&x)[8])
+{
+    float mx = x[0];
+#pragma unroll
+    for (int q = 1; q < 8; q++) mx = fmaxf(mx, x[q]);
+    if (mx == -INFINITY) return;
+    if (mx > m) {
+        s *= __expf(m - mx);
+        m = mx;
+    }
+    float a = 0.f, b = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; q += 2) {
+        a += __expf(x[q] - m);
+        b += __expf(x[q + 1] - m);
+    }
+    s += a + b;
+}
+
 __device__ __forceinline__ void lse_merge(float& m, float& s, float m2, float s2)
 {
     if (m2 > m) {
@@ -389,6 +409,12 @@ __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool va
         const float* lrow = t.Lrow + (size_t)i * RS;
         const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
         int k = lane;
+        for (; k + 7 * G < d; k += 8 * G) {
+            float x[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) x[q] = __ldcg(lrow + k + q * G) + __ldcg(scol - k - q * G);
+            lse_add8(m, s, x);
+        }
         for (; k + 3 * G < d; k += 4 * G)
             lse_add4(m, s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
                      __ldcg(lrow + k + 2 * G) + __ldcg(scol - k - 2 * G),
@@ -616,10 +642,9 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
     return grid;
 }
 
-// Cluster mode: one thread-block cluster runs the whole wavefront and
-// synchronises with the hardware cluster barrier.  It wins while a diagonal
-// holds little work (the grid barrier costs ~5 us per diagonal); long bands
-// need the whole GPU.  Returns the cluster size to use, 0 for grid mode.
+// Cluster mode (MESSI_WAVE_MODE=cluster): one thread-block cluster runs the
+// whole wavefront and synchronises with the hardware cluster barrier.
+// Returns the cluster size to use, 0 for grid mode.
 static int probe_cluster_size(const void* kernel, int threads)
 {
     for (int cl : {16, 8}) {
@@ -646,8 +671,11 @@ static int probe_cluster_size(const void* kernel, int threads)
 
 static int wave_cluster_size(messi_ctx* ctx, const void* kernel, int threads, double terms_per_diag)
 {
-    if (ctx->wave_mode == 1) return 0;
-    if (ctx->wave_mode != 2 && terms_per_diag > 1.0e6) return 0;
+    // measured on GB300: the grid barrier is as fast as the cluster barrier for
+    // these passes (the per-diagonal cost is the L2 latency chain of the split
+    // sums) and the grid has 10x the SMs, so the cluster build runs only on request
+    (void)terms_per_diag;
+    if (ctx->wave_mode != 2) return 0;
     // the largest cluster the device runs for this kernel, found once per context
     for (const auto& kv : ctx->cluster_sizes)
         if (kv.first == kernel) return kv.second;

@@ -75,9 +75,12 @@ static __device__ __forceinline__ bool wave_sync(unsigned int* sync, unsigned in
     return grid_sync(sync, gen);
 }
 
+// Lanes per cell for a split sum of `nterms` terms: at most 8 terms per lane
+// up to 256 terms, so a lane's loads are issued together and the sum costs
+// one L2 round trip; longer sums use the whole warp.
 static __device__ __forceinline__ int group_width(int nterms)
 {
-    return nterms <= 8 ? 1 : (nterms <= 32 ? 4 : (nterms <= 96 ? 8 : (nterms <= 256 ? 16 : 32)));
+    return nterms <= 8 ? 1 : (nterms <= 16 ? 2 : (nterms <= 32 ? 4 : (nterms <= 64 ? 8 : (nterms <= 128 ? 16 : 32))));
 }
 
 }  // namespace messi
