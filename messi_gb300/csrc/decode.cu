@@ -202,7 +202,8 @@ __device__ __forceinline__ float option_weight(const Band& t, const Rules& R, in
         const float lv = __ldg(t.Lrow + (size_t)x * t.RS + (h - x));
         const int span = y - h - 1;
         float sv;
-        if (span <= t.Wb) sv = __ldg(t.Srow + (size_t)(h + 1) * t.RS + span);
+        // column layout: consecutive h of a warp read consecutive addresses
+        if (span <= t.Wb) sv = __ldg(t.Scol + (size_t)y * t.RS + span);
         else if (y == t.L - 1) sv = __ldg(t.Ssuf + h + 1);
         else sv = -INFINITY;
         return ((P == 0) ? R.r[0] : R.r[4]) + lv + sv;
@@ -213,6 +214,8 @@ __device__ __forceinline__ float option_weight(const Band& t, const Rules& R, in
     const float fv = __ldg(t.Frow + (size_t)(x + 1) * t.RS + (span - 2));
     return ((P == 0) ? R.r[2] : (P == 1 ? R.r[3] : R.r[6])) + pv + fv;
 }
+
+constexpr int kCachedRounds = 32;  // options of a span kept in registers: 32 per lane
 
 // One warp per structure.  stack: [nstruct][3 * (L + 1)] ints;
 // paired: [nstruct][L] (1-based partners, 0 = unpaired).
@@ -242,27 +245,46 @@ __global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R,
         const int P = stk[3 * top], x = stk[3 * top + 1], y = stk[3 * top + 2];
         __syncwarp();
         if (x >= y) continue;
-        // bifurcations x..h | h+1..y with L(x, h) in the band; then the pair
+        // bifurcations x..h | h+1..y with L(x, h) in the band; then the pair.
+        // Up to kCached options per span keep their weights in registers (one
+        // pass of loads); longer option lists are re-read per pass.
         const int nsplit = (P == 2) ? 0 : min(y - x, t.Wb + 1);
         const int nopt = nsplit + 1;
+        const bool cached = nopt <= 32 * kCachedRounds;
+        float wv[kCachedRounds];
         float m = -INFINITY;
-        for (int o = lane; o < nopt; o += 32) m = fmaxf(m, option_weight(t, R, P, x, y, o, nsplit));
+        if (cached) {
+#pragma unroll
+            for (int q = 0; q < kCachedRounds; q++) {
+                const int o = lane + 32 * q;
+                wv[q] = (o < nopt) ? option_weight(t, R, P, x, y, o, nsplit) : -INFINITY;
+                m = fmaxf(m, wv[q]);
+            }
+        } else {
+            for (int o = lane; o < nopt; o += 32) m = fmaxf(m, option_weight(t, R, P, x, y, o, nsplit));
+        }
         for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
         if (m == -INFINITY) {
             if (lane == 0) atomicOr(status, 2u);  // a span with no derivation: the tables are inconsistent
             break;
         }
         double tot = 0.0;
-        for (int o = lane; o < nopt; o += 32) tot += (double)__expf(option_weight(t, R, P, x, y, o, nsplit) - m);
+        if (cached) {
+#pragma unroll
+            for (int q = 0; q < kCachedRounds; q++) tot += (double)__expf(wv[q] - m);
+        } else {
+            for (int o = lane; o < nopt; o += 32) tot += (double)__expf(option_weight(t, R, P, x, y, o, nsplit) - m);
+        }
         for (int off = 16; off > 0; off >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, off);
         const double target = uniform01(seed, (unsigned long long)warp, draw++) * tot;
         // inverse CDF in rounds of 32 options; if rounding leaves the target
         // past the last cumulative sum, the last option of non-zero weight
         int pick = -1, last = -1;
         double run = 0.0;
-        for (int r0 = 0; r0 < nopt; r0 += 32) {
+        // one round of 32 options: returns true once the pick is found
+        auto round = [&](int r0, float wo) {
             const int o = r0 + lane;
-            double w = (o < nopt) ? (double)__expf(option_weight(t, R, P, x, y, o, nsplit) - m) : 0.0;
+            const double w = (o < nopt) ? (double)__expf(wo - m) : 0.0;
             double inc = w;
             for (int off = 1; off < 32; off <<= 1) {
                 const double n = __shfl_up_sync(0xffffffffu, inc, off);
@@ -273,9 +295,19 @@ __global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R,
             const unsigned int ball = __ballot_sync(0xffffffffu, (w > 0.0) && (run + inc > target));
             if (ball) {
                 pick = r0 + __ffs(ball) - 1;
-                break;
+                return true;
             }
             run += __shfl_sync(0xffffffffu, inc, 31);
+            return false;
+        };
+        if (cached) {
+            bool found = false;
+#pragma unroll
+            for (int q = 0; q < kCachedRounds; q++)
+                if (!found && 32 * q < nopt) found = round(32 * q, wv[q]);
+        } else {
+            for (int r0 = 0; r0 < nopt; r0 += 32)
+                if (round(r0, (r0 + lane < nopt) ? option_weight(t, R, P, x, y, r0 + lane, nsplit) : -INFINITY)) break;
         }
         if (pick < 0) pick = last;
         const int npush = (pick < nsplit) ? 2 : 1;
