@@ -119,6 +119,16 @@ int messi_dataset_stats(messi_dataset* ds, int64_t* out, int32_t n);
 int messi_felsenstein_pairs(messi_ctx* ctx, messi_dataset* ds, const messi_model* model,
                             double* pairedlogprobs, double* museconditionals);
 
+/* felsensteinposteriorsiterateconditionalscuda (src/FelsensteinCUDA.jl:
+ * 518-717): per column and site-rate category s, the log-sum-exp of
+ * log w_s + log singleprobs[x] + (unpaired log-likelihood of x under s) and,
+ * over the evaluated partners y of x, log pairprobs + log w_c + (pair
+ * log-likelihood of category c) for the categories whose rate at x is s.
+ *   singleprobs: [L], pairprobs: [L x L] posteriors;
+ *   conditionals: [nsite x L] output (column-major, as the reference's
+ *                 siteCats x numcols array). */
+int messi_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const messi_model* model,
+                                const double* singleprobs, const double* pairprobs, double* conditionals);
 /* computeunpairedlikelihoods(dataset, params) (src/FARCE.jl:1198-1220):
  * per-column log-likelihood mixed over site-rate categories.  [L] output. */
 int messi_unpaired(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, double* unpairedlogprobs);
@@ -188,10 +198,13 @@ int messi_consensus_structure(messi_ctx* ctx, int32_t L, const double* unpaired,
 /* samplestructure (src/InsideOutsideAlgorithm.jl:570-635, B = 1 as every
  * caller uses it): nstruct structures drawn independently from the KH99
  * posterior given the scores.  structures: [nstruct][L] 1-based partners, 0
- * when unpaired.  Random numbers: SplitMix64 streams keyed by (seed, index),
- * so a (seed, nstruct) pair always gives the same structures. */
+ * when unpaired.  logprior: optional [nstruct], the log KH99 prior of each
+ * structure (calculateKH99prior, src/InsideOutsideAlgorithm.jl:86-144, which
+ * samplestructure returns), summed over the sampled derivation.  Random
+ * numbers: SplitMix64 streams keyed by (seed, index), so a seed always gives
+ * the same structures. */
 int messi_sample_structures(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired,
-                            int32_t maxspan, int32_t nstruct, uint64_t seed, int32_t* structures);
+                            int32_t maxspan, int32_t nstruct, uint64_t seed, int32_t* structures, double* logprior);
 /* computestructureintegratedlikelihood without the prior
  * (src/FARCE.jl:2322-2345, with maskgapped! as at src/MESSI.jl:310): unpaired
  * likelihoods, pair pruning, gap masking and the inside pass, all on the

@@ -21,7 +21,8 @@ _API_NAMES = ("felsensteincuda", "coevolutionall", "computeunpairedlikelihoods",
               "computeoutsideKH99", "computebasepairprobs", "computeposteriors",
               "computestructureintegratedlikelihood", "computestructureintegratedlikelihoods", "Batch", "Context",
               "get_context", "computeposteriordecodingcuda", "getPosteriorDecodingConsensusStructure",
-              "consensusstructure", "samplestructures", "felsensteincudapaired", "computemodellikelihood")
+              "consensusstructure", "samplestructures", "felsensteincudapaired", "computemodellikelihood",
+              "felsensteinposteriorsiterateconditionalscuda")
 
 
 def __getattr__(name):

@@ -70,6 +70,8 @@ _SIGS = {
                                         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "messi_likelihood": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Model), ctypes.c_void_p,
                                         ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "messi_siterate_conditionals": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Model),
+                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "messi_structure_likelihood": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Model),
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "messi_posterior_decoding": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
@@ -77,7 +79,8 @@ _SIGS = {
     "messi_consensus_structure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_int32, ctypes.c_double, ctypes.c_void_p]),
     "messi_sample_structures": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
-                                               ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_void_p]),
+                                               ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
     "messi_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.POINTER(ctypes.c_void_p)]),
     "messi_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),

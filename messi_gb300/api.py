@@ -185,6 +185,20 @@ def felsensteincuda(dataset, params, museparams=None, maxbasepairdistance=100000
     return mat, ret
 
 
+def felsensteinposteriorsiterateconditionalscuda(singleprobs, pairprobs, dataset, params, museparams=None,
+                                                  maxbasepairdistance=1000000, keepmuseconditionals=False, ctx=None):
+    """src/FelsensteinCUDA.jl:518-717: siteCats x numcols log conditionals of
+    each column's site-rate category given the structure posteriors."""
+    ctx = ctx or get_context()
+    h = ctx.dataset(dataset, maxbasepairdistance)
+    m = ModelArgs(params, museparams)
+    L = dataset.numcols
+    out = np.empty((len(m.sr), L), order="F")
+    ctx.check(ctx.lib.messi_siterate_conditionals(ctx.handle, h.handle, ctypes.byref(m.struct), _p(_f64c(singleprobs)),
+                                                  _p(_f64f(pairprobs)), _p(out)), "messi_siterate_conditionals")
+    return out
+
+
 def coevolutionall(dataset, params, parallel=True, keepmatrices=False, integratesiterates=True,
                    maxbasepairdistance=1000000, usecuda=True):
     """src/FARCE.jl:1736-1741 (the GPU branch)."""
@@ -366,15 +380,14 @@ def samplestructures(unpairedlogprobs, pairedlogprobs, count, seed=1, maxspan=-1
     """samplestructure (src/InsideOutsideAlgorithm.jl:570-635), `count`
     independent draws on the device.  Returns (structures [count, L] as
     1-based partners / 0, log KH99 prior of each)."""
-    from .structures import calculateKH99prior
     ctx = ctx or get_context()
     u = _f64c(unpairedlogprobs)
     L = len(u)
     out = np.empty((int(count), L), np.int32)
+    priors = np.empty(int(count))
     ctx.check(ctx.lib.messi_sample_structures(ctx.handle, L, _p(u), _p(_f64f(pairedlogprobs)), int(maxspan),
-                                              int(count), int(seed) & 0xFFFFFFFFFFFFFFFF, _p(out)),
+                                              int(count), int(seed) & 0xFFFFFFFFFFFFFFFF, _p(out), _p(priors)),
               "messi_sample_structures")
-    priors = np.array([calculateKH99prior(row) for row in out])
     return out.astype(np.int64), priors
 
 

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstddef>
 #include <cstring>
 #include <new>
 
@@ -105,7 +106,7 @@ namespace {
 // Scratch slots (grow-only, per context).  0..14 belong to the band tables.
 enum Slot {
     kSlotStage = 15, kSlotP16 = 16, kSlotDense = 17, kSlotVec = 18, kSlotTable = 19, kSlotP4 = 21,
-    kSlotDecodeF = 22, kSlotDecodeI = 23
+    kSlotDecodeF = 22, kSlotDecodeI = 23, kSlotCatLL = 24, kSlotCond = 25
 };
 
 struct ModelDev {
@@ -428,6 +429,50 @@ int messi_felsenstein_pairs(messi_ctx* ctx, messi_dataset* ds, const messi_model
     return finish(ctx);
 }
 
+int messi_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const messi_model* model,
+                                const double* singleprobs, const double* pairprobs, double* conditionals)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ds || !model || !singleprobs || !pairprobs || !conditionals)
+        return fail(ctx, MESSI_EINVAL, "site-rate conditionals: null argument");
+    ModelDev md;
+    if ((rc = upload_model(ctx, ds, model, true, true, nullptr, &md))) return rc;
+    if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
+    const int L = ds->L, C = md.cat.C, ns = md.cat.nsite;
+    void *pc, *pv;
+    if ((rc = ensure(ctx, kSlotCatLL, (size_t)C * std::max<int64_t>(ds->nroot, 1) * sizeof(double), &pc))) return rc;
+    if ((rc = ensure(ctx, kSlotCond, ((size_t)L * L + (size_t)L * (ns + 1)) * sizeof(double), &pv))) return rc;
+    double* d_catll = (double*)pc;
+    double* d_pair = (double*)pv;
+    double* d_single = d_pair + (size_t)L * L;
+    double* d_out = d_single + L;
+    // the root descriptor writes per-category values for this call only
+    double* on = d_catll;
+    double* off = nullptr;
+    const size_t field = offsetof(NodeDev, catll);
+    cudaError_t e = cudaMemcpyAsync((char*)ds->d_nodes + field, &on, sizeof(double*), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "root descriptor");
+    rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, C, md.cat.nlam, false);
+    e = cudaMemcpyAsync((char*)ds->d_nodes + field, &off, sizeof(double*), cudaMemcpyHostToDevice, ctx->stream);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "root descriptor");
+    void* pu;
+    if ((rc = ensure(ctx, kSlotVec, (size_t)L * sizeof(double), &pu))) return rc;
+    if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, ns, (double*)pu, nullptr)))
+        return rc;
+    // per-site unpaired log-likelihoods: the last block of the unpaired scratch
+    const size_t n = (size_t)ds->numnodes * L;
+    const double* d_ull = (const double*)ctx->scratch[20].p + (size_t)ns * n * 5;
+    if ((rc = h2d(ctx, d_pair, pairprobs, (size_t)L * L * sizeof(double)))) return rc;
+    if ((rc = h2d(ctx, d_single, singleprobs, (size_t)L * sizeof(double)))) return rc;
+    if ((rc = launch_siterate_conditionals(ctx, ds, d_catll, md.logw, ns, md.cat.nlam, d_single, d_pair, d_ull,
+                                           md.logw_site, d_out)))
+        return rc;
+    if ((rc = d2h(ctx, conditionals, d_out, (size_t)L * ns * sizeof(double)))) return rc;
+    return finish(ctx);
+}
+
 int messi_unpaired(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, double* unpairedlogprobs)
 {
     int rc = begin(ctx);
@@ -612,7 +657,7 @@ int messi_consensus_structure(messi_ctx* ctx, int32_t L, const double* unpaired,
 }
 
 int messi_sample_structures(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired,
-                            int32_t maxspan, int32_t nstruct, uint64_t seed, int32_t* structures)
+                            int32_t maxspan, int32_t nstruct, uint64_t seed, int32_t* structures, double* logprior)
 {
     int rc = begin(ctx);
     if (rc) return rc;
@@ -627,10 +672,18 @@ int messi_sample_structures(messi_ctx* ctx, int32_t L, const double* unpaired, c
     int* d_out = (int*)ints;
     int* d_stack = d_out + (size_t)L * nstruct;
     unsigned int* d_status = (unsigned int*)(d_stack + 3 * ((size_t)L + 1) * nstruct);
-    if ((rc = run_sample_structures(ctx, t, 1.0, nstruct, (unsigned long long)seed, d_out, d_stack, d_status)))
+    double* d_prior = nullptr;
+    if (logprior) {
+        void* pp;
+        if ((rc = ensure(ctx, kSlotCond, (size_t)nstruct * sizeof(double), &pp))) return rc;
+        d_prior = (double*)pp;
+    }
+    if ((rc = run_sample_structures(ctx, t, 1.0, nstruct, (unsigned long long)seed, d_out, d_stack, d_prior,
+                                    d_status)))
         return rc;
     unsigned int status = 0;
     if ((rc = d2h(ctx, structures, d_out, (size_t)L * nstruct * sizeof(int32_t)))) return rc;
+    if (logprior && (rc = d2h(ctx, logprior, d_prior, (size_t)nstruct * sizeof(double)))) return rc;
     if ((rc = d2h(ctx, &status, d_status, sizeof(unsigned int)))) return rc;
     if ((rc = finish(ctx))) return rc;
     if (status != 0u) return fail(ctx, MESSI_ESTATE, "sample structures: a span had no derivation (check the inputs)");

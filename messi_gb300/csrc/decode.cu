@@ -28,6 +28,7 @@
 // Random numbers: SplitMix64 (Steele, Lea and Flood, OOPSLA 2014) over
 // (seed, structure, draw).
 #include <climits>
+#include <cmath>
 
 #include "internal.h"
 #include "wave.cuh"
@@ -219,8 +220,16 @@ constexpr int kCachedRounds = 32;  // options of a span kept in registers: 32 pe
 
 // One warp per structure.  stack: [nstruct][3 * (L + 1)] ints;
 // paired: [nstruct][L] (1-based partners, 0 = unpaired).
-__global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R, int nstruct, unsigned long long seed,
-                                                                int* __restrict__ paired, int* __restrict__ stack,
+// KH99 log rule probabilities in FP64 (the prior of a sampled structure is
+// the sum over its derivation: src/InsideOutsideAlgorithm.jl:86-144 parses
+// the same rules, unfolded).
+struct PriorRules {
+    double r[7];
+};
+
+__global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R, PriorRules PR, int nstruct,
+                                                                unsigned long long seed, int* __restrict__ paired,
+                                                                int* __restrict__ stack, double* __restrict__ prior,
                                                                 unsigned int* __restrict__ status)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -239,11 +248,13 @@ __global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R,
     }
     top = 1;
     unsigned long long draw = 0;
+    double lp = 0.0;  // log prior of the derivation (lane 0's copy is the result)
     while (top > 0) {
         __syncwarp();
         top--;
         const int P = stk[3 * top], x = stk[3 * top + 1], y = stk[3 * top + 2];
         __syncwarp();
+        if (x == y) lp += (P == 0) ? PR.r[1] : (P == 2 ? PR.r[5] : -INFINITY);  // S -> s, L -> s
         if (x >= y) continue;
         // bifurcations x..h | h+1..y with L(x, h) in the band; then the pair.
         // Up to kCached options per span keep their weights in registers (one
@@ -315,6 +326,8 @@ __global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R,
             if (lane == 0) atomicOr(status, 4u);
             break;
         }
+        if (pick < nsplit) lp += (P == 0) ? PR.r[0] : PR.r[4];                   // S -> LS, F -> LS
+        else lp += (P == 0) ? PR.r[2] : (P == 1 ? PR.r[3] : PR.r[6]);            // pair rules
         if (lane == 0) {
             if (pick < nsplit) {
                 const int h = x + pick;
@@ -335,6 +348,7 @@ __global__ void __launch_bounds__(128) sample_structures_kernel(Band t, Rules R,
         }
         top += npush;
     }
+    if (lane == 0 && prior) prior[warp] = lp;
 }
 
 // ---------------------------------------------------------------------------
@@ -387,15 +401,17 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
 }
 
 int run_sample_structures(messi_ctx* ctx, const Band& t, double B, int nstruct, unsigned long long seed,
-                          int* d_paired, int* d_stack, unsigned int* d_status)
+                          int* d_paired, int* d_stack, double* d_prior, unsigned int* d_status)
 {
     Rules R = make_rules(B);
+    PriorRules PR;
+    for (int k = 0; k < 7; k++) PR.r[k] = std::log(kKH99Prob[k]);
     cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "sampler status reset");
     const int warps_per_block = 4;
     const int blocks = (nstruct + warps_per_block - 1) / warps_per_block;
-    sample_structures_kernel<<<blocks, 32 * warps_per_block, 0, ctx->stream>>>(t, R, nstruct, seed, d_paired,
-                                                                                d_stack, d_status);
+    sample_structures_kernel<<<blocks, 32 * warps_per_block, 0, ctx->stream>>>(t, R, PR, nstruct, seed, d_paired,
+                                                                                d_stack, d_prior, d_status);
     LAUNCH_CHECK(ctx, "sample_structures_kernel");
     return MESSI_OK;
 }

@@ -56,6 +56,7 @@ struct NodeDev {
     long long ocs;
     double* mix;       // root only: [n] category mixture per unique root pair
     double* mixlam;    // root only: [kMaxLambda][n] per-lambda mixtures (nullable)
+    double* catll;     // root only: [C][n] per-category log-likelihoods (nullable)
     int n;             // unique pairs at this node
     int left;          // child node ids (index of their transition matrices)
     int right;
@@ -101,6 +102,10 @@ struct BandBatch {
     size_t bytes = 0;
 };
 
+// KH99 rule probabilities (src/InsideOutsideAlgorithm.jl:40-53):
+// S->LS, S->s, S->dFd, F->dFd, F->LS, L->s, L->dFd.
+constexpr double kKH99Prob[7] = {0.868534, 0.117609877998, 0.013856122002, 0.787640, 0.21236, 0.894603, 0.105397};
+
 // Rule log-probabilities times B (index 0..6 = r1..r7).
 struct Rules {
     float r[7];
@@ -138,7 +143,7 @@ struct messi_ctx {
     std::string last_error;
     int num_sms = 0;
     // scratch buffers (grow-only)
-    messi::DevBuf scratch[24];
+    messi::DevBuf scratch[32];
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
     unsigned int* status_host = nullptr;  // pinned word: wavefront barrier status of the last call
@@ -242,6 +247,12 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
 // context's buffer (reused in stream order).
 int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int pstride, const double* d_pi4,
                     const double* d_logw_site, int nsite, double* d_u, double* d_scratch);
+// Site-rate conditionals (prune.cu): catll [C][nroot] per-category root
+// log-likelihoods, ull [nsite][L] per-site unpaired log-likelihoods, single
+// [L] and pair [L x L] (column-major) posteriors; out [nsite x L] column-major.
+int launch_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const double* d_catll, const double* d_logw,
+                                 int nsite, int nlam, const double* d_single, const double* d_pair,
+                                 const double* d_ull, const double* d_logw_site, double* d_out);
 // Fixed-structure sums (prune.cu, structure_sum_kernel).
 int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const double* d_mix, double* d_total,
                          double* d_pairll);
@@ -271,9 +282,10 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
                            float* d_work, int* d_scol, unsigned int* d_sync, int* d_paired, int* d_stack,
                            double* d_eout);
 // Structure sampling through the inside band tables of t (computed with B).
-// d_paired: [nstruct][L]; d_stack: [nstruct][3 (L + 1)] ints; d_status: 1 uint.
+// d_paired: [nstruct][L]; d_stack: [nstruct][3 (L + 1)] ints; d_prior
+// (nullable): [nstruct] log KH99 prior of each structure; d_status: 1 uint.
 int run_sample_structures(messi_ctx* ctx, const Band& t, double B, int nstruct, unsigned long long seed,
-                          int* d_paired, int* d_stack, unsigned int* d_status);
+                          int* d_paired, int* d_stack, double* d_prior, unsigned int* d_status);
 // Grid and CTA size of a persistent wavefront kernel (cooperative launch).
 int wave_threads(const messi_ctx* ctx, double band_cells);
 int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads);

@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
             }
             const float dot = dots[0] * (t == 0) + dots[1] * (t == 1) + dots[2] * (t == 2) + dots[3] * (t == 3);
             const double ll = (dot > 0.f) ? (double)logf(dot) + (double)e * 0.69314718055994530942 : -INFINITY;
+            if (nd.catll && myvalid) nd.catll[(size_t)(c0 + cc) * n + myu] = ll;
             const double tt = __ldg(logw + (size_t)nd.grp * C + c0 + cc) + ll;
             if (tt > mm) {
                 ss = ss * __expf((float)(mm - tt)) + 1.f;
@@ -601,6 +602,75 @@ int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, c
 // computeunpairedlikelihoods(..., paired), src/FARCE.jl:1222-1250), pairll
 // the pair log-likelihood at the first column of each pair and 0 elsewhere.
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Site-rate conditionals (felsensteinposteriorsiterateconditionalscuda,
+// src/FelsensteinCUDA.jl:518-717): for column x and site-rate category s,
+//   LSE( log w_s + log single[x] + u_s[x],
+//        over band partners y > x, categories with s1 = s:
+//            log pair[x,y] + log w_c + ll_c(x, y),
+//        over band partners y < x, categories with s2 = s:
+//            log pair[y,x] + log w_c + ll_c(y, x) )
+// One thread per (column, category); categories in the order s1, s2, lambda.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double lse_acc(double a, double b)
+{
+    if (b == -INFINITY) return a;
+    if (a == -INFINITY) return b;
+    return (a < b) ? b + log1p(exp(a - b)) : a + log1p(exp(b - a));
+}
+
+__global__ void siterate_cond_kernel(const int* __restrict__ bandidx, int L, int W, const double* __restrict__ catll,
+                                     int nroot, const double* __restrict__ logw, int ns, int nl,
+                                     const double* __restrict__ single, const double* __restrict__ pair,
+                                     const double* __restrict__ ull, const double* __restrict__ logw_site,
+                                     double* __restrict__ out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (x >= L) return;
+    double acc = -INFINITY;
+    const double us = ull[(size_t)s * L + x];
+    if (us != -INFINITY) acc = lse_acc(acc, logw_site[s] + log(single[x]) + us);
+    for (int k = 1; k <= W && x + k < L; k++) {
+        const int b = bandidx[(size_t)x * (W + 1) + k];
+        if (b < 0) continue;
+        const double pp = pair[(size_t)x + (size_t)(x + k) * L];
+        if (!(pp > 0.0)) continue;
+        const double lp = log(pp);
+        for (int s2 = 0; s2 < ns; s2++)
+            for (int l = 0; l < nl; l++) {
+                const int c = (s * ns + s2) * nl + l;
+                acc = lse_acc(acc, lp + logw[c] + catll[(size_t)c * nroot + b]);
+            }
+    }
+    for (int k = 1; k <= W && k <= x; k++) {
+        const int y = x - k;
+        const int b = bandidx[(size_t)y * (W + 1) + k];
+        if (b < 0) continue;
+        const double pp = pair[(size_t)y + (size_t)x * L];
+        if (!(pp > 0.0)) continue;
+        const double lp = log(pp);
+        for (int s1 = 0; s1 < ns; s1++)
+            for (int l = 0; l < nl; l++) {
+                const int c = (s1 * ns + s) * nl + l;
+                acc = lse_acc(acc, lp + logw[c] + catll[(size_t)c * nroot + b]);
+            }
+    }
+    out[(size_t)s + (size_t)x * ns] = acc;
+}
+
+int launch_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const double* d_catll, const double* d_logw,
+                                 int nsite, int nlam, const double* d_single, const double* d_pair,
+                                 const double* d_ull, const double* d_logw_site, double* d_out)
+{
+    const int bs = 64;
+    siterate_cond_kernel<<<dim3((ds->L + bs - 1) / bs, nsite), bs, 0, ctx->stream>>>(
+        ds->d_bandidx, ds->L, ds->W, d_catll, (int)ds->nroot, d_logw, nsite, nlam, d_single, d_pair, d_ull,
+        d_logw_site, d_out);
+    LAUNCH_CHECK(ctx, "siterate_cond_kernel");
+    return MESSI_OK;
+}
+
 // colu[c]: unique root pair of the pair opened at column c (>= 0), -2 on the
 // closing column of a pair, -1 on an unpaired column.
 __global__ void __launch_bounds__(1024) structure_sum_kernel(double* __restrict__ u, const int* __restrict__ colu,

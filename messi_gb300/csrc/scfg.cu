@@ -162,9 +162,8 @@ int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
 
 Rules make_rules(double B)
 {
-    static const double p[7] = {0.868534, 0.117609877998, 0.013856122002, 0.787640, 0.21236, 0.894603, 0.105397};
     Rules r;
-    for (int k = 0; k < 7; k++) r.r[k] = (float)(B * std::log(p[k]));
+    for (int k = 0; k < 7; k++) r.r[k] = (float)(B * std::log(kKH99Prob[k]));
     return r;
 }
 

@@ -152,3 +152,36 @@ def structure_integrated_likelihood(tree, masks, gapfreq, p15, W, gapcutoff=1.0,
     ins = c_oracle.inside(u, p, 1.0, nthreads=nthreads)
     Z = ins[0, 0, len(u) - 1]
     return computeprior(rp) + Z, dict(u=u, p=p, inside=ins, Z=Z, params=rp)
+
+
+def siterate_conditionals(tree, masks, rp, W, single, pair, pairmask=None):
+    """felsensteinposteriorsiterateconditionalscuda (src/FelsensteinCUDA.jl:
+    518-717) in FP64: per site-rate category s and column x, the log-sum-exp
+    of log w_s + log single[x] + u_s[x] and, over evaluated partners, of
+    log pair + log w_c + ll_c for the categories whose rate at x is s
+    (first column: siteCat1, second column: siteCat2)."""
+    import numpy as np
+    P, pi16, logw, lam, l1, s1, s2 = pair_categories(rp)
+    C = P.shape[0]
+    L = masks.shape[1]
+    ns = len(rp.siteRates)
+    _, ubs = unpaired_loglik(tree, masks, rp)
+    out = np.full((ns, L), -np.inf)
+
+    def lse(a, b):
+        return np.logaddexp(a, b)
+    for s in range(ns):
+        for x in range(L):
+            if np.isfinite(ubs[s, x]) and single[x] > 0:
+                out[s, x] = np.log(rp.siteWeights[s]) + np.log(single[x]) + ubs[s, x]
+    for c in range(C):
+        llc, _ = c_oracle.pair_matrix(tree["children"], tree["seqindex"], masks, P[c:c + 1], pi16[c:c + 1],
+                                      np.zeros(1), W, pairmask=pairmask)
+        for x in range(L):
+            for y in range(x + 1, min(L, x + W + 1)):
+                if not np.isfinite(llc[x, y]) or not (pair[x, y] > 0):
+                    continue
+                v = np.log(pair[x, y]) + logw[c] + llc[x, y]
+                out[s1[c], x] = lse(out[s1[c], x], v)
+                out[s2[c], y] = lse(out[s2[c], y], v)
+    return out

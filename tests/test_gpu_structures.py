@@ -95,6 +95,10 @@ def test_sampled_structures_follow_the_posterior(api, L, W):
     tol = 5.0 * np.sqrt(pair * (1.0 - pair) / n) + 2e-3
     assert np.all(np.abs(freq - pair) <= tol), float(np.max(np.abs(freq - pair) - tol))
     np.testing.assert_allclose(1.0 - freq.sum(axis=1), single, atol=5.0 * np.sqrt(0.25 / n) + 2e-3)
+    # the device's prior of each structure equals the host parse (calculateKH99prior)
+    from messi_gb300.structures import calculateKH99prior
+    for row, pr in zip(S[:200], priors[:200]):
+        assert abs(pr - calculateKH99prior(row)) <= 1e-9 * abs(pr)
     # the same seed gives the same structures
     S2, _ = api.samplestructures(u, p, 64, seed=7)
     np.testing.assert_array_equal(S2, S[:64])
