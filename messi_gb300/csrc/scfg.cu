@@ -302,9 +302,11 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R)
     const int T = t.L - 1 - t.Wb;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ float known[32];
+    __shared__ float tri[32][33];  // Lrow[i0 - l][k], k < 32: the in-block terms, read by the serial warp
     for (int i0 = T - 1; i0 >= 0; i0 -= 32) {
         const int lo = max(0, i0 - 31);
         const int i = i0 - w;
+        tri[w][lane] = (i >= lo && lane <= t.Wb) ? t.Lrow[(size_t)i * t.RS + lane] : -INFINITY;
         if (i >= lo) {
             float m = -INFINITY, s = 0.f;
             const float* lrow = t.Lrow + (size_t)i * t.RS;
@@ -321,15 +323,14 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R)
             const int nb = i0 - lo + 1;
             float mine = -INFINITY;  // lane l holds Ssuf[i0 - l] once computed
             for (int l = 0; l < nb; l++) {
-                const int ic = i0 - l;
                 const int k = l - lane - 1;
                 float x = -INFINITY;
-                if (lane < l && k <= t.Wb) x = t.Lrow[(size_t)ic * t.RS + k] + mine;
+                if (lane < l && k <= t.Wb) x = tri[l][k] + mine;
                 float m = x, s = (x == -INFINITY) ? 0.f : 1.f;
                 group_reduce<32>(m, s);
                 const float sv = R.r[0] + lse2f(known[l], lse_val(m, s));
                 if (lane == l) mine = sv;
-                if (lane == 0) t.Ssuf[ic] = sv;
+                if (lane == 0) t.Ssuf[i0 - l] = sv;
             }
         }
         __syncthreads();
@@ -903,9 +904,11 @@ __global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
     const int T = t.L - 1 - t.Wb;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ float known[32];
+    __shared__ float tri[32][33];  // Lcol[i0 + l - 1][k], k < 32: the in-block terms
     for (int i0 = 0; i0 < T; i0 += 32) {
         const int hi = min(T - 1, i0 + 31);
         const int i = i0 + w;
+        tri[w][lane] = (i <= hi && i >= 1 && lane <= t.Wb) ? t.Lcol[(size_t)(i - 1) * t.RS + lane] : -INFINITY;
         if (i <= hi) {
             float m = -INFINITY, s = 0.f;
             if (i >= 1) {
@@ -928,7 +931,7 @@ __global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
                 const int ic = i0 + l;
                 const int k = l - lane - 1;
                 float x = -INFINITY;
-                if (lane < l && k <= t.Wb && ic >= 1) x = t.Lcol[(size_t)(ic - 1) * t.RS + k] + mine;
+                if (lane < l && k <= t.Wb && ic >= 1) x = tri[l][k] + mine;
                 float m = x, s = (x == -INFINITY) ? 0.f : 1.f;
                 group_reduce<32>(m, s);
                 const float sv = (ic == 0) ? 0.f : R.r[0] + lse2f(known[l], lse_val(m, s));
