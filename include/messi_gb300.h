@@ -103,6 +103,11 @@ int messi_ctx_profile_read(messi_ctx* ctx, int kernel, double* total_ms, int64_t
 int messi_dataset_create(messi_ctx* ctx, const messi_alignment* aln, int32_t maxbasepairdistance,
                          const uint8_t* pairmask, messi_dataset** ds);
 int messi_dataset_destroy(messi_dataset* ds);
+/* Dataset.subcolumnrefs (src/Dataset.jl:180-196) computed on the device:
+ * for every tree node v and column x, the first column whose subtree
+ * pattern at v equals x's.  Output: [numnodes x L] column-major with 1-based
+ * values (the reference's Julia matrix). */
+int messi_subcolumnrefs(messi_ctx* ctx, messi_dataset* ds, int32_t* subcolumnrefs);
 /* Plan statistics: out[0] pairs in band, [1] unique root pairs, [2] node
  * updates per category executed (sum over internal nodes of unique pairs),
  * [3] naive node updates per category (pairs x internal nodes), [4] tree

@@ -22,7 +22,7 @@ _API_NAMES = ("felsensteincuda", "coevolutionall", "computeunpairedlikelihoods",
               "computestructureintegratedlikelihood", "computestructureintegratedlikelihoods", "Batch", "Context",
               "get_context", "computeposteriordecodingcuda", "getPosteriorDecodingConsensusStructure",
               "consensusstructure", "samplestructures", "felsensteincudapaired", "computemodellikelihood",
-              "felsensteinposteriorsiterateconditionalscuda")
+              "felsensteinposteriorsiterateconditionalscuda", "subcolumnrefs")
 
 
 def __getattr__(name):

@@ -185,6 +185,16 @@ def felsensteincuda(dataset, params, museparams=None, maxbasepairdistance=100000
     return mat, ret
 
 
+def subcolumnrefs(dataset, ctx=None):
+    """Dataset.subcolumnrefs (src/Dataset.jl:180-196) on the device:
+    numnodes x numcols, 1-based first column with the same subtree pattern."""
+    ctx = ctx or get_context()
+    h = ctx.dataset(dataset, 1)
+    out = np.empty((dataset.numnodes, dataset.numcols), dtype=np.int32, order="F")
+    ctx.check(ctx.lib.messi_subcolumnrefs(ctx.handle, h.handle, _p(out)), "messi_subcolumnrefs")
+    return out.astype(np.int64)
+
+
 def felsensteinposteriorsiterateconditionalscuda(singleprobs, pairprobs, dataset, params, museparams=None,
                                                   maxbasepairdistance=1000000, keepmuseconditionals=False, ctx=None):
     """src/FelsensteinCUDA.jl:518-717: siteCats x numcols log conditionals of

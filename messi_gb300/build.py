@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmessi_gb300.so")
-SOURCES = ["api.cu", "prune.cu", "scfg.cu", "batch.cu", "decode.cu", "noalloc.cu", "mlp.cu", "host_model.cpp", "plan.cpp"]
+SOURCES = ["api.cu", "prune.cu", "scfg.cu", "batch.cu", "decode.cu", "ingest.cu", "noalloc.cu", "mlp.cu", "host_model.cpp", "plan.cpp"]
 HEADERS = [os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "wave.cuh"),
            os.path.join(ROOT, "include", "messi_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

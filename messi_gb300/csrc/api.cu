@@ -473,6 +473,23 @@ int messi_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const messi_m
     return finish(ctx);
 }
 
+int messi_subcolumnrefs(messi_ctx* ctx, messi_dataset* ds, int32_t* subcolumnrefs)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ds || !subcolumnrefs) return fail(ctx, MESSI_EINVAL, "subcolumnrefs: null argument");
+    const size_t n = (size_t)ds->numnodes * ds->L;
+    const size_t work = subcolumnrefs_work_bytes(ds);
+    void *pr, *pw;
+    if ((rc = ensure(ctx, kSlotCond, 2 * n * sizeof(int32_t), &pr))) return rc;
+    if ((rc = ensure(ctx, kSlotCatLL, work, &pw))) return rc;
+    int* d_refs = (int*)pr;
+    int* d_out = d_refs + n;
+    if ((rc = run_subcolumnrefs(ctx, ds, d_refs, d_out, pw, work))) return rc;
+    if ((rc = d2h(ctx, subcolumnrefs, d_out, n * sizeof(int32_t)))) return rc;
+    return finish(ctx);
+}
+
 int messi_unpaired(messi_ctx* ctx, messi_dataset* ds, const messi_model* model, double* unpairedlogprobs)
 {
     int rc = begin(ctx);

@@ -260,6 +260,13 @@ int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals
 int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask,
                              double B);
 
+// ---- column patterns on the device (ingest.cu) ----
+// d_refs: [numnodes][L] first-column pattern ids; d_out_julia (nullable):
+// [numnodes x L] column-major, 1-based (the reference's subcolumnrefs).
+int run_subcolumnrefs(messi_ctx* ctx, messi_dataset* ds, int* d_refs, int* d_out_julia, void* d_work,
+                      size_t work_bytes);
+size_t subcolumnrefs_work_bytes(const messi_dataset* ds);
+
 // ---- SCFG kernels (scfg.cu) ----
 int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t);
 int launch_baseline(messi_ctx* ctx, const Band& t, double B);
