@@ -203,7 +203,9 @@ __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
     }
 }
 
-constexpr int kStages = 3;  // categories in flight per warp (cp.async pipeline)
+// Pipeline shapes: STAGES categories in flight per warp (cp.async), MINB CTAs
+// per SM.  3 stages x 2 CTAs (128 registers, 104 KB) or 2 stages x 3 CTAs
+// (80 registers, 70 KB): deeper per-warp pipelining against more warps.
 
 // Per-warp staging of one category: 8 float4 per lane (child rows) + 2 exponents.
 struct WarpStage {
@@ -211,8 +213,8 @@ struct WarpStage {
     int e[2][32];
 };
 
-template <bool ROOT>
-__global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
+template <bool ROOT, int STAGES, int MINB>
+__global__ void __launch_bounds__(kTile, ROOT ? 1 : MINB) prune_mma_kernel(
     const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ PT, int numnodes,
     int c0, int nc, int C, const float* __restrict__ pi16, const double* __restrict__ logw,
     const int* __restrict__ lam, int per_lambda)
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     const int g = lane >> 2, t = lane & 3;
     const int base = tile.y + warp * 32;  // first pair of this warp
     if (base >= n) return;                // whole warp idle (warp-uniform)
-    WarpStage* stage = reinterpret_cast<WarpStage*>(smem_raw) + (size_t)warp * kStages;
+    WarpStage* stage = reinterpret_cast<WarpStage*>(smem_raw) + (size_t)warp * STAGES;
     // child rows of pairs g + 8k (clamped to a valid row past the end)
     int li[4], ri[4];
 #pragma unroll
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     const long long lcs = nd.lcs, rcs = nd.rcs;
     // issue the copies of category cc into its stage (each lane copies what it later reads)
     auto issue = [&](int cc) {
-        WarpStage& st = stage[cc % kStages];
+        WarpStage& st = stage[cc % STAGES];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             cp_async16(&st.x[k][lane], lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
         if (re) cp_async4(&st.e[1][lane], re + (size_t)cc * rcs + myr);
     };
 #pragma unroll
-    for (int s0 = 0; s0 < kStages - 1; s0++) {
+    for (int s0 = 0; s0 < STAGES - 1; s0++) {
         if (s0 < nc) issue(s0);
         cp_async_commit();
     }
@@ -269,10 +271,10 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
         for (int q = 0; q < kMaxLambda; q++) { lm[q] = -INFINITY; ls[q] = 0.f; }
     }
     for (int cc = 0; cc < nc; cc++) {
-        if (cc + kStages - 1 < nc) issue(cc + kStages - 1);
+        if (cc + STAGES - 1 < nc) issue(cc + STAGES - 1);
         cp_async_commit();
-        cp_async_wait<kStages - 1>();
-        const WarpStage& st = stage[cc % kStages];
+        cp_async_wait<STAGES - 1>();
+        const WarpStage& st = stage[cc % STAGES];
         float4 XL[4], XR[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -386,28 +388,42 @@ __global__ void __launch_bounds__(kTile, ROOT ? 1 : 2) prune_mma_kernel(
     }
 }
 
+template <int STAGES, int MINB>
+static int launch_prune_shape(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
+                              const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
+                              const double* d_logw, const int* d_lam, bool per_lambda)
+{
+    static thread_local int smem_set_device = -1;
+    const size_t smem = (size_t)(kTile / 32) * STAGES * sizeof(WarpStage);
+    if (smem_set_device != ctx->device) {
+        cudaFuncSetAttribute(prune_mma_kernel<false, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        cudaFuncSetAttribute(prune_mma_kernel<true, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        smem_set_device = ctx->device;
+    }
+    if (root) {
+        prune_mma_kernel<true, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
+            d_nodes, d_tiles, d_PT, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
+        LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
+    } else {
+        prune_mma_kernel<false, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
+            d_nodes, d_tiles, d_PT, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
+        LAUNCH_CHECK(ctx, "prune_mma_kernel");
+    }
+    return MESSI_OK;
+}
+
 int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
                        const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
                        const double* d_logw, const int* d_lam, bool per_lambda)
 {
-    static thread_local int smem_set_device = -1;
-    const size_t smem = (size_t)(kTile / 32) * kStages * sizeof(WarpStage);
-    if (smem_set_device != ctx->device) {
-        cudaFuncSetAttribute(prune_mma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(prune_mma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        smem_set_device = ctx->device;
-    }
     if (nt <= 0) return MESSI_OK;
-    if (root) {
-        prune_mma_kernel<true><<<nt, kTile, smem, ctx->stream>>>(d_nodes, d_tiles, d_PT, numnodes, c0, nc, C, d_pi16,
-                                                                 d_logw, d_lam, per_lambda ? 1 : 0);
-        LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
-    } else {
-        prune_mma_kernel<false><<<nt, kTile, smem, ctx->stream>>>(d_nodes, d_tiles, d_PT, numnodes, c0, nc, C,
-                                                                  d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
-        LAUNCH_CHECK(ctx, "prune_mma_kernel");
-    }
-    return MESSI_OK;
+    if (ctx->prune_shape == 1)
+        return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
+                                        d_lam, per_lambda);
+    return launch_prune_shape<3, 2>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
+                                    d_lam, per_lambda);
 }
 
 int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
