@@ -130,7 +130,7 @@ struct messi_ctx {
     int wave_threads = 0;
     // 0 = choose per pass, 1 = grid barrier, 2 = one thread-block cluster
     int wave_mode = 0;
-    // pair node-update pipeline: 0 = 3 stages x 2 CTAs/SM, 1 = 2 stages x 3 CTAs/SM
+    // pair node-update pipeline: 0 = 2 stages x 3 CTAs/SM, 1 = 3 stages x 2 CTAs/SM
     int prune_shape = 0;
     std::vector<std::pair<const void*, int>> cluster_sizes;  // kernel -> cluster size (0: none)
     // per-kernel event timing (messi_ctx_profile)

@@ -419,10 +419,11 @@ int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_til
                        const double* d_logw, const int* d_lam, bool per_lambda)
 {
     if (nt <= 0) return MESSI_OK;
+    // measured on GB300: 2 stages x 3 CTAs is 2-5% faster (c4, c2)
     if (ctx->prune_shape == 1)
-        return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
+        return launch_prune_shape<3, 2>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
                                         d_lam, per_lambda);
-    return launch_prune_shape<3, 2>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
+    return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
                                     d_lam, per_lambda);
 }
 

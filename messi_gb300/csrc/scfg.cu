@@ -320,17 +320,15 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R)
         }
         __syncthreads();
         if (w == 0) {
+            // column-oriented substitution: lane q owns cell i0 - q; once cell l
+            // is final it is broadcast and every later cell adds its term
             const int nb = i0 - lo + 1;
-            float mine = -INFINITY;  // lane l holds Ssuf[i0 - l] once computed
+            float am = (lane < nb) ? known[lane] : -INFINITY, as = (am == -INFINITY) ? 0.f : 1.f;
             for (int l = 0; l < nb; l++) {
-                const int k = l - lane - 1;
-                float x = -INFINITY;
-                if (lane < l && k <= t.Wb) x = tri[l][k] + mine;
-                float m = x, s = (x == -INFINITY) ? 0.f : 1.f;
-                group_reduce<32>(m, s);
-                const float sv = R.r[0] + lse2f(known[l], lse_val(m, s));
-                if (lane == l) mine = sv;
+                const float sv = __shfl_sync(0xffffffffu, R.r[0] + lse_val(am, as), l);
                 if (lane == 0) t.Ssuf[i0 - l] = sv;
+                const int k = lane - l - 1;
+                if (lane > l && lane < nb && k <= t.Wb) lse_add(am, as, tri[lane][k] + sv);
             }
         }
         __syncthreads();
@@ -925,18 +923,16 @@ __global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
         }
         __syncthreads();
         if (w == 0) {
+            // column-oriented substitution (lane q owns cell i0 + q); Osuf[0] = 0
             const int nb = hi - i0 + 1;
-            float mine = -INFINITY;  // lane l holds Osuf[i0 + l]
+            float am = (lane < nb) ? known[lane] : -INFINITY, as = (am == -INFINITY) ? 0.f : 1.f;
             for (int l = 0; l < nb; l++) {
                 const int ic = i0 + l;
-                const int k = l - lane - 1;
-                float x = -INFINITY;
-                if (lane < l && k <= t.Wb && ic >= 1) x = tri[l][k] + mine;
-                float m = x, s = (x == -INFINITY) ? 0.f : 1.f;
-                group_reduce<32>(m, s);
-                const float sv = (ic == 0) ? 0.f : R.r[0] + lse2f(known[l], lse_val(m, s));
-                if (lane == l) mine = sv;
+                const float fin = (ic == 0) ? 0.f : R.r[0] + lse_val(am, as);
+                const float sv = __shfl_sync(0xffffffffu, fin, l);
                 if (lane == 0) t.Osuf[ic] = sv;
+                const int k = lane - l - 1;
+                if (lane > l && lane < nb && k <= t.Wb && i0 + lane >= 1) lse_add(am, as, tri[lane][k] + sv);
             }
         }
         __syncthreads();
