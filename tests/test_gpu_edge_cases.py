@@ -1,0 +1,99 @@
+"""Edge cases through the C ABI against the FP64 oracle: the smallest
+alignments and trees, ambiguity codes, all-gap columns, a band of one,
+constant columns, and invalid inputs that must be rejected with a status
+(relative 1e-6 on every log-likelihood)."""
+import numpy as np
+import pytest
+
+from oracle import c_oracle as co
+from oracle import model_ref as mr
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-6
+
+
+def _params(p15, ds):
+    from messi_gb300 import model as M
+    return M.getparams(p15, ds.branchlengths)
+
+
+def _check_likelihood(ds, p15, W):
+    from messi_gb300 import api
+    total = api.computestructureintegratedlikelihood(ds, _params(p15, ds), W)
+    ref, _ = mr.structure_integrated_likelihood(ds.tree_arrays(), ds.masks, ds.gapfrequency, p15, W)
+    assert abs(total - ref) <= REL * abs(ref), (total, ref)
+    return total
+
+
+@pytest.fixture(scope="module")
+def p15():
+    from messi_gb300 import model as M
+    return M.DEFAULT_PARAMS15.copy()
+
+
+def test_one_column_and_two_columns(p15):
+    from messi_gb300.dataset import Dataset
+    newick = "(a:0.1,b:0.2,c:0.3);"
+    one = Dataset.from_sequences(["a", "b", "c"], ["A", "G", "A"], newick)
+    _check_likelihood(one, p15, 1)
+    two = Dataset.from_sequences(["a", "b", "c"], ["AU", "GC", "AU"], newick)
+    _check_likelihood(two, p15, 1)
+
+
+def test_three_sequences_ambiguity_codes_and_gaps(p15):
+    from messi_gb300.dataset import Dataset
+    seqs = ["ACGURYN-ACGUAC", "RYKMSWBDHVN-GA", "acgu-ACGUACGUU"]
+    ds = Dataset.from_sequences(["a", "b", "c"], seqs, "(a:0.1,b:0.2,c:0.3);")
+    for W in (1, 5, 13):
+        _check_likelihood(ds, p15, W)
+
+
+def test_all_gap_and_constant_columns(p15):
+    from messi_gb300.dataset import Dataset
+    seqs = ["A-GGGCCC-UA", "A-GGACCC-UA", "A-GGGCCU-UA", "A-GAGCCC-UA"]
+    ds = Dataset.from_sequences(["a", "b", "c", "d"], seqs, "(a:0.1,b:0.2,(c:0.05,d:0.07):0.1);")
+    assert ds.gapfrequency[1] == 1.0 and ds.gapfrequency[8] == 1.0
+    _check_likelihood(ds, p15, 10)
+
+
+def test_zero_branch_lengths_and_caterpillar_tree(p15):
+    from messi_gb300.dataset import Dataset
+    newick = "(a:0.0,(b:0.1,(c:0.0,(d:0.2,(e:0.05,f:0.3):0.0):0.1):0.2):0.0,g:0.4);"
+    rng = np.random.default_rng(3)
+    seqs = ["".join(rng.choice(list("ACGU"), 24)) for _ in range(7)]
+    ds = Dataset.from_sequences(list("abcdefg"), seqs, newick)
+    _check_likelihood(ds, p15, 23)
+
+
+def test_inside_degenerate_scores():
+    from messi_gb300 import api
+    L = 6
+    u = np.full(L, -5.0)
+    p = np.full((L, L), -np.inf)
+    # no pair possible: closed form of the grammar
+    r = co.kh99_logprobs()
+    Z = api.computeinsideKH99(u, p)
+    assert abs(Z - (u.sum() + (L - 1) * (r[0] + r[5]) + r[1])) <= REL * abs(Z)
+    # a single possible pair
+    p[0, 5] = p[5, 0] = -3.0
+    Z = api.computeinsideKH99(u, p)
+    Zref = co.inside(u, p)[0, 0, L - 1]
+    assert abs(Z - Zref) <= REL * abs(Zref)
+
+
+def test_invalid_inputs_are_rejected(c1, p15):
+    from messi_gb300 import api
+    from messi_gb300._lib import MessiError
+    ds = c1.dataset
+    prm = _params(p15, ds)
+    prm.branchlengths = prm.branchlengths.copy()
+    prm.branchlengths[3] = -1.0
+    with pytest.raises(MessiError):
+        api.felsensteincuda(ds, prm, None, 10)
+    with pytest.raises(MessiError):
+        api.computeposteriordecodingcuda(np.zeros(0), np.zeros((0, 0)))
+    bad = np.zeros(ds.numcols, np.int64)
+    bad[0] = ds.numcols + 5
+    with pytest.raises(MessiError):
+        api.felsensteincudapaired(ds, bad, _params(p15, ds))
