@@ -295,8 +295,6 @@ int messi_ctx_create(int device, messi_ctx** out)
         if (w) ctx->wave_ctas = std::max(0, std::atoi(w));
         const char* wt = std::getenv("MESSI_WAVE_THREADS");
         if (wt) ctx->wave_threads = std::atoi(wt);
-        const char* it = std::getenv("MESSI_INSIDE_TILED");
-        if (it) ctx->inside_tiled = std::atoi(it) != 0;
         const char* ps = std::getenv("MESSI_PRUNE_SHAPE");
         if (ps) ctx->prune_shape = std::atoi(ps) == 1 ? 1 : 0;
         const char* wm = std::getenv("MESSI_WAVE_MODE");

@@ -84,7 +84,6 @@ struct Band {
     double *b, *cb, *u, *Zd;
     int* maxspan;
     unsigned int* sync;  // grid barrier of the wavefront kernels: count, generation, error flag, spare
-    float* ext = nullptr;  // [L][RS] external split sums of the tiled inside pass (nullptr: diagonal pass)
 };
 
 // Band tables of a batch of alignments for the batched inside pass.  Bands
@@ -133,8 +132,6 @@ struct messi_ctx {
     int wave_mode = 0;
     // pair node-update pipeline: 0 = 2 stages x 3 CTAs/SM, 1 = 3 stages x 2 CTAs/SM
     int prune_shape = 0;
-    // inside pass: 1 = tiled (32 x 32 tiles), 0 = one diagonal per grid barrier
-    int inside_tiled = 1;
     std::vector<std::pair<const void*, int>> cluster_sizes;  // kernel -> cluster size (0: none)
     // per-kernel event timing (messi_ctx_profile)
     bool profiling = false;

@@ -135,8 +135,6 @@ int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
         if ((rc = ensure(ctx, k, tab, &p))) return rc;
         *in_tabs[k] = (float*)p;
     }
-    if ((rc = ensure(ctx, 26, tab, &p))) return rc;
-    t->ext = (float*)p;
     if ((rc = ensure(ctx, 6, (size_t)(L + 1) * sizeof(float) * 2, &p))) return rc;
     t->Ssuf = (float*)p;
     t->Osuf = t->Ssuf + (L + 1);
@@ -461,164 +459,6 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
     }
 }
 
-// ---------------------------------------------------------------------------
-// Tiled inside pass: the band is cut into 32 x 32 tiles (rows I*32.., columns
-// J*32..); the tiles of one tile diagonal D = J - I are independent.  For each
-// D the whole grid first sums every cell's split terms whose factors lie in
-// finished tiles (split points k in [I*32 + 31, J*32 - 1]: the "external"
-// part, stored per cell in t.ext), then one CTA per tile finishes its cells
-// in an in-tile wavefront over local diagonals b - a, with the tile, the two
-// diagonal tiles it needs and its boundary F values in shared memory.  Grid
-// barriers: about 2 W / 32 instead of W.
-// ---------------------------------------------------------------------------
-constexpr int kTileW = 32;
-
-struct TileSmem {
-    float LT[kTileW][kTileW + 1], ST[kTileW][kTileW + 1], FT[kTileW][kTileW + 1];  // this tile
-    float LD[kTileW][kTileW + 1];  // L of diagonal tile (I, I)
-    float SD[kTileW][kTileW + 1];  // S of diagonal tile (J, J)
-    float PB[kTileW][kTileW + 1], EX[kTileW][kTileW + 1];
-    float FBr[kTileW];  // F(I*32 + 32, J*32 + b - 1): cells of the last tile row
-    float FBc[kTileW];  // F(I*32 + a + 1, J*32 - 1): cells of the first tile column
-};
-
-__device__ __forceinline__ float band_at(const float* tab, const Band& t, int i, int j)
-{
-    const int d = j - i;
-    return (i >= 0 && j < t.L && d >= 0 && d <= t.Wb) ? __ldcg(tab + (size_t)i * t.RS + d) : -INFINITY;
-}
-
-// External split sums of every cell of tile diagonal D (D >= 1).
-__device__ void tiled_external(const Band& t, int D, int nT)
-{
-    constexpr int T = kTileW;
-    const int E = (D - 1) * T + 1;
-    const int G = group_width(E);
-    const int gpb = blockDim.x / G;
-    const int lane = threadIdx.x & (G - 1);
-    const long long ncell = (long long)(nT - D) * T * T;
-    const long long total = (long long)gridDim.x * gpb;
-    for (long long base = 0; base < ncell; base += total) {
-        const long long it = base + (long long)blockIdx.x * gpb + threadIdx.x / G;
-        bool valid = it < ncell;
-        int i = 0, j = 0, k0 = 0;
-        if (valid) {
-            const int I = (int)(it / (T * T)), r = (int)(it % (T * T));
-            i = I * T + r / T;
-            j = (I + D) * T + r % T;
-            k0 = I * T + T - 1;
-            valid = i < t.L && j < t.L && j - i <= t.Wb;
-        }
-        float m = -INFINITY, s = 0.f;
-        if (valid) {
-            const float* lrow = t.Lrow + (size_t)i * t.RS + (k0 - i);
-            const float* scol = t.Scol + (size_t)j * t.RS + (j - k0 - 1);
-            int q = lane;
-            for (; q + 7 * G < E; q += 8 * G) {
-                float x[8];
-#pragma unroll
-                for (int u = 0; u < 8; u++) x[u] = __ldcg(lrow + q + u * G) + __ldcg(scol - q - u * G);
-                lse_add8(m, s, x);
-            }
-            for (; q + 3 * G < E; q += 4 * G)
-                lse_add4(m, s, __ldcg(lrow + q) + __ldcg(scol - q), __ldcg(lrow + q + G) + __ldcg(scol - q - G),
-                         __ldcg(lrow + q + 2 * G) + __ldcg(scol - q - 2 * G),
-                         __ldcg(lrow + q + 3 * G) + __ldcg(scol - q - 3 * G));
-            for (; q < E; q += G) lse_add(m, s, __ldcg(lrow + q) + __ldcg(scol - q));
-        }
-        group_reduce_rt(m, s, G);
-        if (valid && lane == 0) t.ext[(size_t)i * t.RS + (j - i)] = lse_val(m, s);
-    }
-}
-
-// Tile (I, J) of tile diagonal D by one CTA of 32 warps.
-__device__ void tiled_tile(const Band& t, const Rules& R, int I, int J, int D, TileSmem& sm)
-{
-    constexpr int T = kTileW;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    {
-        const int a = w, b = lane;
-        const int i = I * T + a, j = J * T + b;
-        const bool cell = i < t.L && j < t.L && j - i >= 0 && j - i <= t.Wb;
-        sm.PB[a][b] = (cell && j > i) ? __ldcg(t.pb + (size_t)i * t.RS + (j - i)) : -INFINITY;
-        sm.EX[a][b] = (cell && D >= 1) ? __ldcg(t.ext + (size_t)i * t.RS + (j - i)) : -INFINITY;
-        sm.LD[a][b] = (D >= 1) ? band_at(t.Lrow, t, I * T + a, I * T + b) : -INFINITY;
-        sm.SD[a][b] = (D >= 1) ? band_at(t.Srow, t, J * T + a, J * T + b) : -INFINITY;
-        // span-0 cells of a diagonal tile were written by the initialisation
-        const bool diag0 = (D == 0 && a == b && i < t.L);
-        sm.LT[a][b] = diag0 ? __ldcg(t.Lrow + (size_t)i * t.RS) : -INFINITY;
-        sm.ST[a][b] = diag0 ? __ldcg(t.Srow + (size_t)i * t.RS) : -INFINITY;
-        sm.FT[a][b] = -INFINITY;
-        if (w == 0) {
-            sm.FBr[b] = band_at(t.Frow, t, I * T + T, J * T + b - 1);
-            sm.FBc[b] = band_at(t.Frow, t, I * T + b + 1, J * T - 1);
-        }
-    }
-    __syncthreads();
-    for (int delta = (D == 0) ? 1 : -(T - 1); delta <= T - 1; delta++) {
-        const int a0 = max(0, -delta);
-        const int a = a0 + w, b = a + delta;
-        const int i = I * T + a, j = J * T + b;
-        const bool valid = b < T && a < T && i < t.L && j < t.L && j - i >= 1 && j - i <= t.Wb;
-        float m = -INFINITY, s = 0.f;
-        if (valid) {
-            if (D == 0) {
-                const int c = a + lane;  // split points i .. j - 1, all in this tile
-                if (c < b) lse_add(m, s, sm.LT[a][c] + sm.ST[c + 1][b]);
-            } else {
-                const int c1 = a + lane;  // split in row tile I: L from tile (I, I), S from this tile
-                if (c1 <= T - 2) lse_add(m, s, sm.LD[a][c1] + sm.ST[c1 + 1][b]);
-                if (lane < b) lse_add(m, s, sm.LT[a][lane] + sm.SD[lane + 1][b]);  // split in column tile J
-                if (lane == 0) lse_add(m, s, sm.EX[a][b]);
-            }
-        }
-        group_reduce<32>(m, s);
-        if (valid && lane == 0) {
-            const int d = j - i;
-            const float tmp = lse_val(m, s);
-            float fin = -INFINITY;
-            if (d >= 2) fin = (a + 1 <= T - 1 && b >= 1) ? sm.FT[a + 1][b - 1] : (a == T - 1 ? sm.FBr[b] : sm.FBc[a]);
-            const float v = sm.PB[a][b] + fin;
-            const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
-            const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
-            const float Lv = R.r[6] + v;
-            sm.LT[a][b] = Lv;
-            sm.ST[a][b] = S;
-            sm.FT[a][b] = F;
-            t.Lrow[(size_t)i * t.RS + d] = Lv;
-            t.Lcol[(size_t)j * t.RS + d] = Lv;
-            t.Srow[(size_t)i * t.RS + d] = S;
-            t.Scol[(size_t)j * t.RS + d] = S;
-            t.Frow[(size_t)i * t.RS + d] = F;
-            if (j == t.L - 1) t.Ssuf[i] = S;
-        }
-        __syncthreads();
-    }
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(kWaveMaxThreads) inside_tiled_kernel(Band t, Rules R, double B)
-{
-    __shared__ TileSmem sm;
-    unsigned int gen = 0;
-    const int L = t.L;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
-    if (!wave_sync<MODE>(t.sync, gen)) return;
-    const int nT = (L + kTileW - 1) / kTileW;
-    const int Dmax = min(nT - 1, (t.Wb + kTileW - 1) / kTileW);
-    for (int D = 0; D <= Dmax; D++) {
-        if (D >= 1) {
-            tiled_external(t, D, nT);
-            if (!wave_sync<MODE>(t.sync, gen)) return;
-        }
-        for (int tile = blockIdx.x; tile < nT - D; tile += gridDim.x) {
-            tiled_tile(t, R, tile, tile + D, D, sm);
-            __syncthreads();
-        }
-        if (!wave_sync<MODE>(t.sync, gen)) return;
-    }
-}
-
 // Batched inside over n alignments in one persistent launch: diagonal d of
 // every alignment whose band reaches it is one step of the wavefront.  Bands
 // are sorted by band width, descending, so the alignments active at span d
@@ -897,26 +737,8 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     double Bv = B;
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc;
-    if (t.ext && ctx->inside_tiled) {
-        // tiled pass: 1,024 threads per CTA (one warp per cell of a tile diagonal), one CTA per SM
-        const int threads = kWaveMaxThreads;
-        const int nT = (t.L + kTileW - 1) / kTileW;
-        // the external sums use the whole GPU; short sequences need fewer CTAs
-        int grid = wave_grid(ctx, (const void*)inside_tiled_kernel<kGrid>, 1 << 30, threads);
-        grid = std::min(grid, std::max(8, 4 * nT));
-        cudaError_t e = cudaMemsetAsync(t.sync, 0, 4 * sizeof(unsigned int), ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-        e = cudaLaunchCooperativeKernel((const void*)inside_tiled_kernel<kGrid>, dim3(grid), dim3(threads), args, 0,
-                                        ctx->stream);
-        ctx->launches++;
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_tiled_kernel");
-        rc = MESSI_OK;
-    } else {
-        rc = launch_wave2(ctx, (const void*)inside_wave_kernel<kGrid>, (const void*)inside_wave_kernel<kCluster>, args,
-                          t.sync, t.L, (double)t.L * (t.Wb + 1), band_terms_per_diag(t.L, t.Wb),
-                          "inside_wave_kernel");
-    }
+    int rc = launch_wave2(ctx, (const void*)inside_wave_kernel<kGrid>, (const void*)inside_wave_kernel<kCluster>, args,
+                          t.sync, t.L, (double)t.L * (t.Wb + 1), band_terms_per_diag(t.L, t.Wb), "inside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
