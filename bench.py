@@ -3,9 +3,11 @@
 
 One step = one structure-integrated likelihood evaluation (what every NLopt
 objective and every MCMC proposal of the reference runs,
-src/FARCE.jl:2322-2345): unpaired column likelihoods, 16-state pair pruning
-over every column pair within the span limit for all 45 categories, gap
-masking and the banded KH99 inside pass to Z.  Workload: seeded synthetic
+src/FARCE.jl:2322-2345): unpaired column likelihoods, pair likelihoods of
+every column pair within the span limit mixed over 45 categories (16-state
+pruning for the 36 with lambda != 1; the 9 with lambda = 1 are the product of
+the unpaired columns, as in the reference's CPU path, src/FARCE.jl:1891-1901),
+gap masking and the banded KH99 inside pass to Z.  Workload: seeded synthetic
 alignment of 64 sequences x 1,000 nt, max pair span 500 (374,750 pairs).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -154,19 +156,22 @@ def make_params(s, count, seed):
 
 def cpu_oracle_rate(s, rows, nthreads):
     """FP64 CPU restatement timed on a bounded sample: pair pruning for a block
-    of rows, plus the full unpaired and inside passes pro-rated to the sample."""
+    of rows, plus the full unpaired and inside passes pro-rated to the sample.
+    The lambda = 1 categories take the product of the unpaired columns, as the
+    reference's CPU path does (src/FARCE.jl:1891-1901)."""
     import numpy as np
 
     from oracle import c_oracle as co
     from oracle import model_ref as mr
     ds = s.dataset
     rp = mr.getparams(s.params15, ds.branchlengths)
-    P, pi16, logw, *_ = mr.pair_categories(rp)
+    P, pi16, logw, _, l1, s1, s2 = mr.pair_categories(rp)
     t0 = time.perf_counter()
-    u, _ = mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
+    u, ubs = mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
     t_unp = time.perf_counter() - t0
     t0 = time.perf_counter()
-    p, _ = co.pair_matrix(ds.children, ds.seqindex, ds.masks, P, pi16, logw, s.W, rows=rows, nthreads=nthreads)
+    p, _ = co.pair_matrix(ds.children, ds.seqindex, ds.masks, P, pi16, logw, s.W, rows=rows, nthreads=nthreads,
+                          lambda1_cat=l1, u_by_site=ubs, site1=s1, site2=s2)
     t_pairs = time.perf_counter() - t0
     sample = int(np.isfinite(p[np.triu_indices(ds.numcols, 1)]).sum())
     return u, t_unp, t_pairs, sample
@@ -246,7 +251,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories",
+        "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories (lambda = 1 factorised, as the "
+                               "reference's CPU path does)",
                    "pairs_per_full_step": npairs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": f"{rows_per_step} alignment rows of pairs per step (~{int(statistics.mean(samples))} "
@@ -364,8 +370,12 @@ def run_ours(args):
         api.maskgapped(mat, ds.gapfrequency, 1.0, -np.inf)
         api.computeinsideKH99(u, mat, ctx=ctx)
         t_e2e.append(time.perf_counter() - t0)
-    model_bytes = (45 * (16 + 256 + 16) + 3 * (4 + 16 + 4) + 45 * 3 + 3 + 4 + ds.numnodes) * 8 + 45 * 16 * 4
-    h2d = 2 * model_bytes + L * L * 8 + L * 8
+    # staged model uploads (eigensystems, branch lengths, pi16, weights, lambda
+    # indices, unpaired eigensystems, pi4, site weights): one per call
+    Cp = api.ModelArgs(params[0]).pruned_categories()
+    unpaired_bytes = (ds.numnodes + 3 * (4 + 16 + 4) + 4 + 3) * 8
+    pair_bytes = Cp * ((16 + 256 + 16) * 8 + 16 * 4 + 8 + 4)
+    h2d = 2 * unpaired_bytes + pair_bytes + L * L * 8 + L * 8
     d2h = L * 8 + L * L * 8 + 8
     e2e_value = whole_job_rate(npairs, 1, 1e3 * max_over_ranks(statistics.mean(t_e2e), ws), ws)
 
@@ -391,7 +401,8 @@ def run_ours(args):
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
         "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories "
-                               "(3 x 3 site rates x 5 lambda), synthetic from seed, 5% gaps",
+                               "(3 x 3 site rates x 5 lambda; the 9 with lambda = 1 factorised into unpaired "
+                               "columns), synthetic from seed, 5% gaps",
                    "pairs_per_step": npairs, "step": "unpaired + pair pruning + gap mask + banded inside -> Z",
                    "l2": "flushed between steps (256 MB write outside the timed events)",
                    "parallelism": f"replicas x{ws}", "plan": stats},

@@ -157,6 +157,15 @@ class ModelArgs:
         m.lambdaWeights = _p(self.lw)
         self.struct = m
 
+    def pruned_categories(self):
+        """Categories the library prunes with 16 states in a likelihood call:
+        the lambda categories with all three lambdas equal to 1 are
+        factorised into unpaired columns (src/FARCE.jl:1891-1901) unless
+        every lambda category is such a one."""
+        one = (self.lGC == 1.0) & (self.lAT == 1.0) & (self.lGT == 1.0)
+        kept = len(self.lw) if one.all() else int((~one).sum())
+        return len(self.sr) ** 2 * kept
+
 
 def _need_cuda(flag):
     if not flag:

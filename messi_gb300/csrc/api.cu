@@ -123,11 +123,13 @@ struct ModelDev {
 
 // Builds categories on the host, uploads them in one copy and assembles the
 // transition matrices on the device.
+// factorise: leave the lambda = 1 categories out of the 16-state pruning (the
+// caller then adds md->cat.logwF + u[x] + u[y] to every pair mixture).
 int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool pairs, bool unpaired,
-                 const uint8_t* gapmask, ModelDev* md)
+                 const uint8_t* gapmask, ModelDev* md, bool factorise = false)
 {
     std::string err;
-    int rc = build_categories(m, ds->numnodes, &md->cat, &err, pairs);
+    int rc = build_categories(m, ds->numnodes, &md->cat, &err, pairs, factorise && pairs && unpaired);
     if (rc) return fail(ctx, rc, err);
     Categories& c = md->cat;
     Staged st;
@@ -410,21 +412,31 @@ int messi_felsenstein_pairs(messi_ctx* ctx, messi_dataset* ds, const messi_model
     if (rc) return rc;
     if (!ds || !model || !pairedlogprobs) return fail(ctx, MESSI_EINVAL, "felsenstein_pairs: null argument");
     ModelDev md;
-    if ((rc = upload_model(ctx, ds, model, true, false, nullptr, &md))) return rc;
+    if ((rc = upload_model(ctx, ds, model, true, true, nullptr, &md, true))) return rc;
     if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
     if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, museconditionals != nullptr)))
         return rc;
-    void* p;
+    void *p, *pu;
     const size_t LL = (size_t)ds->L * ds->L;
     if ((rc = ensure(ctx, kSlotDense, LL * sizeof(double), &p))) return rc;
     double* d_dense = (double*)p;
-    if ((rc = launch_scatter_dense(ctx, ds, ds->d_mix, d_dense))) return rc;
+    double* d_u = nullptr;
+    if (md.cat.lamF) {  // unpaired columns for the factorised lambda categories
+        if ((rc = ensure(ctx, kSlotVec, (size_t)ds->L * sizeof(double), &pu))) return rc;
+        d_u = (double*)pu;
+        if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, d_u, nullptr)))
+            return rc;
+    }
+    if ((rc = launch_scatter_dense(ctx, ds, ds->d_mix, d_u, md.cat.logwF, d_dense))) return rc;
     if ((rc = d2h(ctx, pairedlogprobs, d_dense, LL * sizeof(double)))) return rc;
     if (museconditionals) {
         // one L x L matrix per lambda category; the copy of the previous one
         // must finish before the buffer is reused (same stream: ordered)
         for (int l = 0; l < md.cat.nlam; l++) {
-            if ((rc = launch_scatter_dense(ctx, ds, ds->d_mixlam + (size_t)l * ds->nroot, d_dense))) return rc;
+            const bool fl = (md.cat.lamF >> l) & 1u;
+            if ((rc = launch_scatter_dense(ctx, ds, fl ? nullptr : ds->d_mixlam + (size_t)l * ds->nroot, d_u,
+                                           fl ? md.cat.logw_lam[l] : -INFINITY, d_dense)))
+                return rc;
             if ((rc = d2h(ctx, museconditionals + (size_t)l * LL, d_dense, LL * sizeof(double)))) return rc;
         }
     }
@@ -518,7 +530,7 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
         for (int i = 0; i < ds->L; i++) gm[i] = (gapfrequency[i] >= gapcutoff) ? 1 : 0;
     }
     ModelDev md;
-    if ((rc = upload_model(ctx, ds, model, true, true, gapfrequency ? gm.data() : nullptr, &md))) return rc;
+    if ((rc = upload_model(ctx, ds, model, true, true, gapfrequency ? gm.data() : nullptr, &md, true))) return rc;
     if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
     if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
     Band t;
@@ -526,7 +538,7 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     if ((rc = band_alloc(ctx, ds->L, Wb, false, &t))) return rc;
     if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, t.u, nullptr))) return rc;
     if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
-    if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0))) return rc;
+    if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0, md.cat.logwF))) return rc;
     if ((rc = run_inside(ctx, t, 1.0))) return rc;
     if ((rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;
     if (unpaired && (rc = d2h(ctx, unpaired, t.u, (size_t)ds->L * sizeof(double)))) return rc;
@@ -746,7 +758,7 @@ int messi_structure_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_mo
         return code;
     };
     ModelDev md;
-    if ((rc = upload_model(ctx, ds, model, !pairs.empty(), true, nullptr, &md))) return done(rc);
+    if ((rc = upload_model(ctx, ds, model, !pairs.empty(), true, nullptr, &md, true))) return done(rc);
     if (sub) {
         if ((rc = prepare_arena(ctx, sub, md.cat.C))) return done(rc);
         if ((rc = run_pairs(ctx, sub, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false)))
@@ -754,20 +766,22 @@ int messi_structure_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_mo
     }
     void *dv, *di;
     if ((rc = ensure(ctx, kSlotVec, (2 * (size_t)L + 8) * sizeof(double), &dv))) return done(rc);
-    if ((rc = ensure(ctx, kSlotDecodeI, ((size_t)L + 8) * sizeof(int32_t), &di))) return done(rc);
+    if ((rc = ensure(ctx, kSlotDecodeI, (2 * (size_t)L + 8) * sizeof(int32_t), &di))) return done(rc);
     double* d_u = (double*)dv;
     double* d_pairll = d_u + L;
     double* d_total = d_pairll + L;
     int32_t* d_col = (int32_t*)di;
-    std::vector<int32_t> colu(L, -1);
+    std::vector<int32_t> colu(2 * (size_t)L, -1);  // root pair ids, then 0-based partners
     for (int i = 0; i < L; i++) {
         if (col_pair[i] >= 0) colu[i] = pu[col_pair[i]];
         else if (paired[i] > 0) colu[i] = -2;
+        colu[(size_t)L + i] = paired[i] - 1;
     }
     if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, d_u, nullptr)))
         return done(rc);
-    if ((rc = h2d(ctx, d_col, colu.data(), (size_t)L * sizeof(int32_t)))) return done(rc);
-    if ((rc = launch_structure_sum(ctx, L, d_u, d_col, sub ? sub->d_mix : nullptr, d_total, d_pairll)))
+    if ((rc = h2d(ctx, d_col, colu.data(), 2 * (size_t)L * sizeof(int32_t)))) return done(rc);
+    if ((rc = launch_structure_sum(ctx, L, d_u, d_col, d_col + L, sub ? sub->d_mix : nullptr, md.cat.logwF, d_total,
+                                   d_pairll)))
         return done(rc);
     if ((rc = d2h(ctx, total, d_total, sizeof(double)))) return done(rc);
     if (pairll && (rc = d2h(ctx, pairll, d_pairll, (size_t)L * sizeof(double)))) return done(rc);

@@ -274,12 +274,22 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     const int G = (int)reps.size();
     std::vector<Categories> cats(G);
     std::string err;
-    for (int g = 0; g < G; g++) {
-        const int a = reps[g];
-        if ((rc = build_categories(&models[a], b->ds[a]->numnodes, &cats[g], &err))) return fail(ctx, rc, err);
+    // lambda = 1 categories are factorised when every model group leaves out
+    // the same ones (the merged launches share one category list)
+    for (int pass = 0; pass < 2; pass++) {
+        const bool factorise = (pass == 0);
+        bool same = true;
+        for (int g = 0; g < G; g++) {
+            const int a = reps[g];
+            if ((rc = build_categories(&models[a], b->ds[a]->numnodes, &cats[g], &err, true, factorise)))
+                return fail(ctx, rc, err);
+            same = same && cats[g].lamF == cats[0].lamF;
+        }
+        if (same) break;
+    }
+    for (int g = 0; g < G; g++)
         if (cats[g].C != cats[0].C || cats[g].nsite != cats[0].nsite)
             return fail(ctx, MESSI_EINVAL, "batch likelihood: models must have the same category counts");
-    }
     for (int a = 0; a < n; a++)
         for (int v = 0; v < b->ds[a]->numnodes; v++)
             if (!models[a].branchlengths || !(models[a].branchlengths[v] >= 0.0) ||
@@ -382,7 +392,8 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     if ((rc = launch_baseline_batch(ctx, b->bands, 1.0))) return rc;
     for (int a = 0; a < n; a++) {
         const Band& t = b->bands.host[b->bands.slot[a]];
-        if ((rc = launch_bandprep_from_mix(ctx, b->ds[a], t, d_gap ? d_gap + b->col_base[a] : nullptr, 1.0)))
+        if ((rc = launch_bandprep_from_mix(ctx, b->ds[a], t, d_gap ? d_gap + b->col_base[a] : nullptr, 1.0,
+                                           cats[grp[a]].logwF)))
             return rc;
     }
     if ((rc = run_inside_batch(ctx, b->bands, 1.0))) return rc;

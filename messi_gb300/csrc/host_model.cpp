@@ -132,7 +132,18 @@ static double safe_log(double x) { return x > 0.0 ? std::log(x) : -INFINITY; }
 // Categories in the reference order: siteCat1 outer, siteCat2, lambda inner
 // (src/FelsensteinCUDA.jl:277-279), weight log(w1) + log(w2) + log(w_lambda)
 // (src/FelsensteinCUDA.jl:403-418).
-int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs)
+//
+// With factorise, the lambda categories whose three lambdas are exactly 1
+// (the first category of getparams: rate 0, src/FARCE.jl:1566-1583) are left
+// out, as long as another lambda category remains.  At lambda = 1 the paired
+// rate matrix is the sum of two independent single-site GTR processes with
+// rates r1 and r2 and pi16 = pi x pi, so the pair likelihood of category
+// (s1, s2, l) is L4(x; r_s1) * L4(y; r_s2); summed over the site rates with
+// their weights this is exp(u[x] + u[y]) times w_l, u being the unpaired
+// log-likelihood.  The reference's CPU path takes the same shortcut
+// (src/FARCE.jl:1891-1901).
+int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs,
+                     bool factorise)
 {
     if (!m || m->nsite < 1 || m->nlambda < 1 || !m->siteRates || !m->siteWeights || !m->lambdaGC ||
         !m->lambdaAT || !m->lambdaGT || !m->lambdaWeights || !m->branchlengths) {
@@ -166,17 +177,34 @@ int build_categories(const messi_model* m, int numnodes, Categories* out, std::s
     Categories& c = *out;
     c.nsite = m->nsite;
     c.nlam = m->nlambda;
-    c.C = m->nsite * m->nsite * m->nlambda;
-    c.eig.assign((size_t)c.C * kEigStride, 0.0);
-    c.pi16.assign((size_t)c.C * 16, 0.f);
+    const int nl = m->nlambda, ns = m->nsite;
+    c.lamF = 0;
+    c.logwF = -INFINITY;
+    c.logw_lam.assign(nl, 0.0);
+    double wF = 0.0;
+    for (int l = 0; l < nl; l++) {
+        c.logw_lam[l] = safe_log(m->lambdaWeights[l]);
+        if (factorise && m->lambdaGC[l] == 1.0 && m->lambdaAT[l] == 1.0 && m->lambdaGT[l] == 1.0) {
+            c.lamF |= 1u << l;
+            wF += m->lambdaWeights[l];
+        }
+    }
+    if (c.lamF == (1u << nl) - 1u) c.lamF = 0;  // nothing left to prune: keep every category
+    if (c.lamF) c.logwF = safe_log(wF);
+    std::vector<int> kept;  // lambda categories pruned with 16 states
+    for (int l = 0; l < nl; l++)
+        if (!(c.lamF >> l & 1u)) kept.push_back(l);
+    const int nk = (int)kept.size();
+    c.C = ns * ns * nk;
+    c.eig.assign(pairs ? (size_t)c.C * kEigStride : 0, 0.0);  // nothing to upload for unpaired-only calls
+    c.pi16.assign(pairs ? (size_t)c.C * 16 : 0, 0.f);
     c.logw.assign(c.C, 0.0);
     c.lam.assign(c.C, 0);
     // the 16-state eigensystems are independent: one per host thread
     std::vector<int> bad(c.C, 0);
-    const int nl = m->nlambda, ns = m->nsite;
 #pragma omp parallel for schedule(dynamic, 1) if (pairs && c.C >= 4)
     for (int k = 0; k < c.C; k++) {
-        const int s1 = k / (ns * nl), s2 = (k / nl) % ns, l = k % nl;
+        const int s1 = k / (ns * nk), s2 = (k / nk) % ns, l = kept[k % nk];
         c.logw[k] = safe_log(m->siteWeights[s1]) + safe_log(m->siteWeights[s2]) + safe_log(m->lambdaWeights[l]);
         c.lam[k] = l;
         if (!pairs) continue;

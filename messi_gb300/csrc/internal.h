@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -65,11 +66,18 @@ struct NodeDev {
 
 // Discretised model categories built on the host for one call.
 struct Categories {
-    int C = 0, nsite = 0, nlam = 0;
+    int C = 0, nsite = 0, nlam = 0;  // C = categories pruned with 16 states
     std::vector<double> eig;      // [C][kEigStride]
     std::vector<float> pi16;      // [C][16]
     std::vector<double> logw;     // [C]
     std::vector<int> lam;         // [C] lambda category of each category
+    // Lambda categories with lambda_GC = lambda_AT = lambda_GT = 1 left out of
+    // the 16-state pruning when factorising: their pair likelihood is the
+    // product of the two unpaired columns, so over the site rates they add
+    // log(sum of their weights) + u[x] + u[y] to the mixture.
+    uint32_t lamF = 0;             // bit l: lambda category l is factorised
+    double logwF = -INFINITY;      // log of the summed weights of those categories
+    std::vector<double> logw_lam;  // [nlam] log lambda weight
     std::vector<double> eig4;     // [nsite][kEig4Stride]
     std::vector<double> logw_site;  // [nsite]
     double pi4[4];
@@ -207,7 +215,8 @@ void prof_end(messi_ctx* ctx);
 
 // ---- host model (host_model.cpp) ----
 // pairs = false skips the 16-state eigensystems (unpaired-only calls).
-int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs = true);
+int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs = true,
+                     bool factorise = false);
 void host_gtr(const double* q, const double* piv, double* Q);
 void host_musefreqs(const double* pi4, double lGC, double lAT, double lGT, double* out16);
 void host_muse(double lGC, double lAT, double lGT, const double* q, const double* pi4, double sr1, double sr2,
@@ -255,12 +264,18 @@ int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int p
 int launch_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const double* d_catll, const double* d_logw,
                                  int nsite, int nlam, const double* d_single, const double* d_pair,
                                  const double* d_ull, const double* d_logw_site, double* d_out);
-// Fixed-structure sums (prune.cu, structure_sum_kernel).
-int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const double* d_mix, double* d_total,
-                         double* d_pairll);
-int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, double* d_out);
+// Fixed-structure sums (prune.cu, structure_sum_kernel); d_partner[c] is the
+// 0-based partner of column c (or -1), logwF the factorised lambda weight.
+int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const int* d_partner,
+                         const double* d_mix, double logwF, double* d_total, double* d_pairll);
+// Dense L x L pair matrix: vals (nullable) of the unique root pairs, mixed with
+// addw + u[x] + u[y] when addw is finite (the factorised lambda categories).
+int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, const double* d_u, double addw,
+                         double* d_out);
+// Banded pair scores from the root mixtures of ds, with the factorised term
+// logwF + u[i] + u[j] (u = t.u) when logwF is finite.
 int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask,
-                             double B);
+                             double B, double logwF);
 
 // ---- column patterns on the device (ingest.cu) ----
 // d_refs: [numnodes][L] first-column pattern ids; d_out_julia (nullable):

@@ -556,7 +556,8 @@ int launch_unpaired(messi_ctx* ctx, messi_dataset* ds, const double* d_P4, int p
 // ---------------------------------------------------------------------------
 // Output layouts
 // ---------------------------------------------------------------------------
-__global__ void scatter_dense_kernel(const int* __restrict__ bandidx, const double* __restrict__ vals, int L, int W,
+__global__ void scatter_dense_kernel(const int* __restrict__ bandidx, const double* __restrict__ vals,
+                                     const double* __restrict__ u, double addw, int L, int W,
                                      double* __restrict__ out)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -567,25 +568,32 @@ __global__ void scatter_dense_kernel(const int* __restrict__ bandidx, const doub
     double val = -INFINITY;
     if (k >= 1 && k <= W) {
         const int b = bandidx[(size_t)i * (W + 1) + k];
-        if (b >= 0) val = vals[b];
+        if (b >= 0) {
+            if (vals) val = vals[b];
+            if (addw != -INFINITY) val = lse_d(val, addw + u[i] + u[i + k]);
+        }
     }
     out[idx] = val;
 }
 
-int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, double* d_out)
+int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, const double* d_u, double addw,
+                         double* d_out)
 {
     const long long n = (long long)ds->L * ds->L;
     const int bs = 256;
-    scatter_dense_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, ctx->stream>>>(ds->d_bandidx, d_vals, ds->L, ds->W,
-                                                                                d_out);
+    if (addw != -INFINITY && !d_u) return fail(ctx, MESSI_EINVAL, "scatter: factorised term without unpaired values");
+    scatter_dense_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, ctx->stream>>>(ds->d_bandidx, d_vals, d_u, addw,
+                                                                                ds->L, ds->W, d_out);
     LAUNCH_CHECK(ctx, "scatter_dense_kernel");
     return MESSI_OK;
 }
 
 // Banded log-odds pair scores from the root mixtures (device-resident path),
 // with maskgapped! (src/RNATools.jl:441-451) folded in.
+// The factorised lambda categories add logwF + u[i] + u[j] to the mixture.
 __global__ void bandprep_from_mix_kernel(const int* __restrict__ bandidx, const double* __restrict__ mix, int L, int W,
                                          int Wb, int RS, const uint8_t* __restrict__ gapmask,
+                                         const double* __restrict__ u, double logwF,
                                          const double* __restrict__ b, double B, float* __restrict__ pb)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -595,19 +603,21 @@ __global__ void bandprep_from_mix_kernel(const int* __restrict__ bandidx, const 
     if (k >= 1 && k <= Wb && i + k < L && k <= W) {
         const int bi = bandidx[(size_t)i * (W + 1) + k];
         if (bi >= 0 && !(gapmask && (gapmask[i] || gapmask[i + k]))) {
-            const double p = mix[bi];
+            double p = mix[bi];
+            if (logwF != -INFINITY) p = lse_d(p, logwF + u[i] + u[i + k]);
             if (p != -INFINITY) out = (float)(B * p - b[i] - b[i + k]);
         }
     }
     pb[idx] = out;
 }
 
-int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask, double B)
+int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask, double B,
+                             double logwF)
 {
     const long long n = (long long)t.L * t.RS;
     const int bs = 256;
     bandprep_from_mix_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, ctx->stream>>>(
-        ds->d_bandidx, ds->d_mix, ds->L, ds->W, t.Wb, t.RS, d_gapmask, t.b, B, t.pb);
+        ds->d_bandidx, ds->d_mix, ds->L, ds->W, t.Wb, t.RS, d_gapmask, t.u, logwF, t.b, B, t.pb);
     LAUNCH_CHECK(ctx, "bandprep_from_mix_kernel");
     return MESSI_OK;
 }
@@ -689,21 +699,31 @@ int launch_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const double
 }
 
 // colu[c]: unique root pair of the pair opened at column c (>= 0), -2 on the
-// closing column of a pair, -1 on an unpaired column.
+// closing column of a pair, -1 on an unpaired column; partner[c] the other
+// column of the pair opened at c.  The factorised lambda categories add
+// logwF + u[c] + u[partner] to each pair, so the unpaired values of paired
+// columns are read before they are cleared.
 __global__ void __launch_bounds__(1024) structure_sum_kernel(double* __restrict__ u, const int* __restrict__ colu,
-                                                             int L, const double* __restrict__ mix,
+                                                             const int* __restrict__ partner, int L,
+                                                             const double* __restrict__ mix, double logwF,
                                                              double* __restrict__ total, double* __restrict__ pairll)
 {
     __shared__ double part[1024];
     double acc = 0.0;
     for (int c = threadIdx.x; c < L; c += blockDim.x) {
         const int k = colu[c];
-        const double pv = (k >= 0) ? mix[k] : 0.0;
+        double pv = 0.0;
+        if (k >= 0) {
+            pv = mix[k];
+            if (logwF != -INFINITY) pv = lse_d(pv, logwF + u[c] + u[partner[c]]);
+        }
         if (k == -1) acc += u[c];
-        else u[c] = 0.0;
         pairll[c] = pv;
         acc += pv;
     }
+    __syncthreads();
+    for (int c = threadIdx.x; c < L; c += blockDim.x)
+        if (colu[c] != -1) u[c] = 0.0;
     part[threadIdx.x] = acc;
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
@@ -713,10 +733,10 @@ __global__ void __launch_bounds__(1024) structure_sum_kernel(double* __restrict_
     if (threadIdx.x == 0) total[0] = part[0];
 }
 
-int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const double* d_mix, double* d_total,
-                         double* d_pairll)
+int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const int* d_partner,
+                         const double* d_mix, double logwF, double* d_total, double* d_pairll)
 {
-    structure_sum_kernel<<<1, 1024, 0, ctx->stream>>>(d_u, d_colu, L, d_mix, d_total, d_pairll);
+    structure_sum_kernel<<<1, 1024, 0, ctx->stream>>>(d_u, d_colu, d_partner, L, d_mix, logwF, d_total, d_pairll);
     LAUNCH_CHECK(ctx, "structure_sum_kernel");
     return MESSI_OK;
 }

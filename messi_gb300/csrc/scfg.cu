@@ -545,6 +545,16 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
                 if (j + 1 <= L - 1) {
                     const float* srw = t.Srow + (size_t)(j + 1) * RS;
                     int q = lane;
+                    for (; q + 3 * G < nL; q += 4 * G) {
+                        float x[8];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const float sib = srw[q + u * G];
+                            x[2 * u] = R.r[0] + __ldcg(osr + q + u * G) + sib;
+                            x[2 * u + 1] = R.r[4] + __ldcg(ofr + q + u * G) + sib;
+                        }
+                        lse_add8(mL, sL, x);
+                    }
                     for (; q + G < nL; q += 2 * G) {
                         const float sib0 = srw[q], sib1 = srw[q + G];
                         lse_add4(mL, sL, R.r[0] + __ldcg(osr + q) + sib0, R.r[4] + __ldcg(ofr + q) + sib0,
@@ -564,6 +574,16 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
                     const float* osc = t.OScol + (size_t)j * RS + d + 1;
                     const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
                     int q = lane;
+                    for (; q + 3 * G < nS; q += 4 * G) {
+                        float x[8];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const float lft = lcol[q + u * G];
+                            x[2 * u] = R.r[0] + __ldcg(osc + q + u * G) + lft;
+                            x[2 * u + 1] = R.r[4] + __ldcg(ofc + q + u * G) + lft;
+                        }
+                        lse_add8(mS, sS, x);
+                    }
                     for (; q + G < nS; q += 2 * G) {
                         const float l0 = lcol[q], l1 = lcol[q + G];
                         lse_add4(mS, sS, R.r[0] + __ldcg(osc + q) + l0, R.r[4] + __ldcg(ofc + q) + l0,

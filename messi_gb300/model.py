@@ -31,6 +31,8 @@ def discretizegamma(shape, scale, numcategories):
     """Gamma quantiles at the category mid-points (src/FARCE.jl:1531-1540)."""
     if numcategories == 1:
         return np.array([1.0])
+    if numcategories == 0:  # Julia's empty comprehension (lambdaCats = 1)
+        return np.zeros(0)
     w = 1.0 / numcategories
     return _gamma.ppf(np.array([w / 2.0 + i * w for i in range(numcategories)]), shape, scale=scale)
 
@@ -38,7 +40,8 @@ def discretizegamma(shape, scale, numcategories):
 def discretizegamma3(lambdazeroweight, meanGC, meanAT, meanGT, gammavar, numcategories):
     """Lambda categories: rate 0 plus Gamma quantiles (src/FARCE.jl:1566-1583)."""
     rates = np.concatenate([[0.0], discretizegamma(gammavar, 1.0 / gammavar, numcategories)])
-    weights = np.ones(numcategories + 1) / numcategories * (1.0 - lambdazeroweight)
+    # with no Gamma categories only the rate-0 category remains, weighted w0
+    weights = np.ones(numcategories + 1) / max(numcategories, 1) * (1.0 - lambdazeroweight)
     weights[0] = lambdazeroweight
     return (weights, rates * (meanGC - 1.0), weights.copy(), rates * (meanAT - 1.0), weights.copy(),
             rates * (meanGT - 1.0))

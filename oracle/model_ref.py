@@ -30,6 +30,8 @@ DEFAULT_PARAMS15 = np.array([2.0, 2.0, 2.0, 1.7487740904105369, 4.46407440297485
 def discretizegamma(shape, scale, numcategories):
     if numcategories == 1:
         return np.array([1.0])
+    if numcategories == 0:  # Julia's empty comprehension (lambdaCats = 1)
+        return np.zeros(0)
     w = 1.0 / numcategories
     vs = np.array([w / 2.0 + i * w for i in range(numcategories)])
     return _gamma.ppf(vs, shape, scale=scale)
@@ -37,7 +39,8 @@ def discretizegamma(shape, scale, numcategories):
 
 def discretizegamma3(lambdazeroweight, meanGC, meanAT, meanGT, gammavar, numcategories):
     rates = np.concatenate([[0.0], discretizegamma(gammavar, 1.0 / gammavar, numcategories)])
-    weights = np.ones(numcategories + 1) / numcategories * (1.0 - lambdazeroweight)
+    # with no Gamma categories only the rate-0 category remains, weighted w0
+    weights = np.ones(numcategories + 1) / max(numcategories, 1) * (1.0 - lambdazeroweight)
     weights[0] = lambdazeroweight
     return weights, rates * (meanGC - 1.0), rates * (meanAT - 1.0), rates * (meanGT - 1.0)
 

@@ -51,6 +51,27 @@ def test_getparams_matches_oracle_restatement():
     assert len(mps) == 5 and mps[0].lambdarate == 0.0 and abs(mps[0].prob - 0.5) < 1e-15
 
 
+def test_single_lambda_category_and_factorised_count():
+    """lambdaCats = 1 (src/FARCE.jl:609-657): one category with lambda = the
+    lambda itself, weight 1; the library prunes categories with lambda != 1
+    and factorises the rest unless nothing would be left."""
+    from messi_gb300.api import ModelArgs
+    bl = np.linspace(0, 1, 7)
+    p = M.DEFAULT_PARAMS15.copy()
+    p[:3] = [3.0, 2.5, 1.5]
+    cp = M.getparams(p, bl, lambdaCats=1)
+    rp = mr.getparams(p, bl, 3, 1)
+    np.testing.assert_allclose(cp.lambdaratesGC, [2.0])
+    np.testing.assert_allclose(cp.lambdaratesGT, [0.5])
+    np.testing.assert_allclose(cp.lambdaweightsGC, [1.0])
+    np.testing.assert_allclose(rp.lambdaratesAT, [1.5])
+    np.testing.assert_allclose(rp.lambdaweights, [1.0])
+    assert ModelArgs(cp).pruned_categories() == 9
+    assert ModelArgs(M.getparams(p, bl)).pruned_categories() == 36
+    p[:3] = 1.0
+    assert ModelArgs(M.getparams(p, bl)).pruned_categories() == 45
+
+
 def test_numpy_rate_matrices_match_oracle():
     from oracle import c_oracle as co
     pi = np.array([0.2, 0.3, 0.1, 0.4])
