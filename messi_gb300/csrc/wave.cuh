@@ -24,12 +24,23 @@ static __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int
     return v;
 }
 
+// Error bit of the arrival counter: a CTA that gives up waiting adds it, which
+// ends every other CTA's wait (the count then exceeds any target) and tells it,
+// from the same load, that the launch failed.
+constexpr unsigned int kBarrierError = 1u << 30;
+
+static __device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // sync[0] = arrivals, monotonic within a launch (barrier g completes when it
 // reaches g * gridDim.x, so the last arrival's add is the release itself);
-// sync[2] = error flag.  Returns false (in every thread of the CTA) once any
-// CTA has given up waiting.  The CTA barrier orders every thread's cells
-// before thread 0's fence and arrival (the cooperative-groups grid barrier
-// pattern).  Cells written by other CTAs before the barrier are read with
+// sync[2] = error flag for the host.  Returns false (in every thread of the
+// CTA) once any CTA has given up waiting.  The CTA barrier orders every
+// thread's cells before thread 0's release-add; thread 0's acquire poll and
+// the second CTA barrier order the other CTAs' cells before the CTA's next
+// reads.  Cells written by other CTAs before the barrier are read with
 // __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
 // those tables.
 static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
@@ -37,22 +48,20 @@ static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int ok = 1;
         const unsigned int target = (gen + 1) * gridDim.x;
-        __threadfence();
-        atomicAdd(&sync[0], 1u);
-        unsigned int spins = 0;
-        while (ld_acquire_u32(&sync[0]) < target) {
-            if ((++spins & 63u) == 0u && (ld_acquire_u32(&sync[2]) != 0u || spins > kSpinLimit)) {
+        red_release_add_u32(&sync[0], 1u);
+        unsigned int v, spins = 0;
+        while ((v = ld_acquire_u32(&sync[0])) < target) {
+            if (++spins > kSpinLimit) {
                 atomicExch(&sync[2], 1u);
-                ok = 0;
+                red_release_add_u32(&sync[0], kBarrierError);
+                v = kBarrierError;
                 break;
             }
             __nanosleep(32);
         }
-        __threadfence();
         gen++;
-        s_ok = ok && (ld_acquire_u32(&sync[2]) == 0u);
+        s_ok = (v & kBarrierError) == 0u;
     }
     __syncthreads();
     return s_ok != 0;
