@@ -43,7 +43,7 @@ BYTES_PER_UPDATE = 212  # algorithmic bytes of one node update (2 child rows + e
 # DRAM bytes (read + write) per node update of the pruning kernel from one ncu
 # capture of the c2-shaped profiling case, weighted over two interior-level
 # launches (profiles/prune_mma_kernel_c2p.md); scaled by updates per launch.
-TRAFFIC_BYTES_PER_UPDATE = 120.0
+TRAFFIC_BYTES_PER_UPDATE = 118.0
 
 
 def measured_peaks():

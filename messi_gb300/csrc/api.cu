@@ -298,7 +298,10 @@ int messi_ctx_create(int device, messi_ctx** out)
         const char* wt = std::getenv("MESSI_WAVE_THREADS");
         if (wt) ctx->wave_threads = std::atoi(wt);
         const char* ps = std::getenv("MESSI_PRUNE_SHAPE");
-        if (ps) ctx->prune_shape = std::atoi(ps) == 1 ? 1 : 0;
+        if (ps) {
+            const int v = std::atoi(ps);
+            ctx->prune_shape = (v >= 0 && v <= 2) ? v : 0;
+        }
         const char* wm = std::getenv("MESSI_WAVE_MODE");
         if (wm) ctx->wave_mode = std::strcmp(wm, "grid") == 0 ? 1 : (std::strcmp(wm, "cluster") == 0 ? 2 : 0);
     }

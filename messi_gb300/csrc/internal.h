@@ -14,7 +14,7 @@
 
 namespace messi {
 
-constexpr int kTile = 256;          // unique pairs per CTA in the pruning kernels
+constexpr int kTile = 128;          // unique pairs per CTA in the pruning kernels
 constexpr int kMaxLambda = 8;       // per-lambda conditionals kept in registers
 constexpr int kMaxStack = 512;      // tree height limit of the unpaired kernel
 constexpr int kEigStride = 16 + 256 + 16;  // eigenvalues, U (row-major), sqrt(pi)

@@ -9,7 +9,7 @@
 //     3xTF32 hi/lo split;
 //   * prune_mma_kernel: one launch per tree level and category pass; a warp
 //     owns 32 unique pairs of one node, gathers the child rows with cp.async
-//     (three categories in flight) and does both child mat-vecs on the tensor
+//     (two categories in flight) and does both child mat-vecs on the tensor
 //     cores (3xTF32 mma.sync).  Rows are rescaled by an exact power of two
 //     (exponent kept as an int), which computes the same likelihood as the
 //     reference's divide-by-max (felsenstein.cu:193-198);
@@ -186,6 +186,8 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+
+
 // Exact power-of-two rescale of a row max m > 0: m * 2^-ex in [0.5, 1).
 __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
 {
@@ -204,8 +206,12 @@ __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
 }
 
 // Pipeline shapes: STAGES categories in flight per warp (cp.async), MINB CTAs
-// per SM.  3 stages x 2 CTAs (128 registers, 104 KB) or 2 stages x 3 CTAs
-// (80 registers, 70 KB): deeper per-warp pipelining against more warps.
+// of kTile = 128 threads per SM.  The default, 2 stages x 4 CTAs (16 warps,
+// 128 registers, 136 KB of stages per SM), leaves ~90 KB of the SM's L1 to
+// cache the gathered child rows, which parent pairs share heavily: on GB300
+// it prunes c2 in 9.2 ms against 11.4 ms for 3 CTAs of 8 warps (24 warps, 80
+// registers with spills, 204 KB of stages) and 20.3 ms with the row copies
+// bypassing L1.
 
 // Per-warp staging of one category: 8 float4 per lane (child rows) + 2 exponents.
 struct WarpStage {
@@ -400,6 +406,7 @@ static int launch_prune_shape(messi_ctx* ctx, const NodeDev* d_nodes, const int2
                              (int)smem);
         cudaFuncSetAttribute(prune_mma_kernel<true, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
+
         smem_set_device = ctx->device;
     }
     if (root) {
@@ -420,11 +427,16 @@ int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_til
 {
     if (nt <= 0) return MESSI_OK;
     // measured on GB300: 2 stages x 3 CTAs is 2-5% faster (c4, c2)
-    if (ctx->prune_shape == 1)
-        return launch_prune_shape<3, 2>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
-                                        d_lam, per_lambda);
-    return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16, d_logw,
-                                    d_lam, per_lambda);
+    // MESSI_PRUNE_SHAPE=1 / 2: 3 stages x 3 CTAs, 2 stages x 3 CTAs (measured
+    // 6% and 5% slower on c2 and c4)
+    switch (ctx->prune_shape) {
+        case 1: return launch_prune_shape<3, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16,
+                                                d_logw, d_lam, per_lambda);
+        case 2: return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16,
+                                                d_logw, d_lam, per_lambda);
+        default: return launch_prune_shape<2, 4>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16,
+                                                 d_logw, d_lam, per_lambda);
+    }
 }
 
 int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
