@@ -220,7 +220,7 @@ struct WarpStage {
 };
 
 template <bool ROOT, int STAGES, int MINB>
-__global__ void __launch_bounds__(kTile, ROOT ? 1 : MINB) prune_mma_kernel(
+__global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
     const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ PT, int numnodes,
     int c0, int nc, int C, const float* __restrict__ pi16, const double* __restrict__ logw,
     const int* __restrict__ lam, int per_lambda)
