@@ -83,6 +83,13 @@ int messi_ctx_stream(messi_ctx* ctx, void** stream);
 int messi_ctx_last_launches(messi_ctx* ctx, int64_t* launches);
 /* Text of the last error recorded on this context. */
 const char* messi_ctx_last_error(messi_ctx* ctx);
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * launches a two-CTA grid barrier that one CTA never reaches; the other
+ * CTA's wait gives up after a few milliseconds and raises the error flag.
+ * *status receives the status such a wait produces (MESSI_ETIMEOUT when the
+ * mechanism works); the call itself returns MESSI_OK and leaves the context
+ * usable. */
+int messi_selftest_bounded_wait(messi_ctx* ctx, int32_t* status);
 
 /* Per-kernel timing (instrumentation; no counterpart in the reference).
  * enable != 0 records a CUDA event pair around each launch of the timed

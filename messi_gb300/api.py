@@ -60,6 +60,14 @@ class Context:
         _lib.check(self.lib.messi_ctx_last_launches(self.handle, ctypes.byref(n)), "messi_ctx_last_launches")
         return n.value
 
+    def selftest_bounded_wait(self):
+        """Status produced by a device wait that cannot complete (a grid
+        barrier one CTA never reaches): MESSI_ETIMEOUT when the bounded wait
+        gives up as designed.  The context stays usable."""
+        st = ctypes.c_int32()
+        self.check(self.lib.messi_selftest_bounded_wait(self.handle, ctypes.byref(st)), "messi_selftest_bounded_wait")
+        return st.value
+
     def profile(self, enable=True):
         """Enable (and reset) per-kernel CUDA-event timing."""
         self.check(self.lib.messi_ctx_profile(self.handle, 1 if enable else 0), "messi_ctx_profile")

@@ -222,6 +222,31 @@ int d2h(messi_ctx* ctx, void* dst, const void* src, size_t bytes)
     return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "device to host copy");
 }
 
+// Work on the side stream: fork() makes the side stream wait for everything
+// queued on the main stream so far; while a SideLaunches is alive the launch
+// helpers (which use ctx->stream) queue on the side stream; join() makes the
+// main stream wait for the side stream's work.
+int fork_side(messi_ctx* ctx)
+{
+    cudaError_t e = cudaEventRecord(ctx->fork_ev, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "side stream fork");
+}
+
+int join_side(messi_ctx* ctx)
+{
+    cudaError_t e = cudaEventRecord(ctx->join_ev, ctx->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0);
+    return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "side stream join");
+}
+
+struct SideLaunches {
+    messi_ctx* ctx;
+    cudaStream_t main;
+    explicit SideLaunches(messi_ctx* c) : ctx(c), main(c->stream) { ctx->stream = ctx->side; }
+    ~SideLaunches() { ctx->stream = main; }
+};
+
 // Upload a dense L x L pair matrix, pick the band width, prepare the band.
 int dense_pairs_to_band(messi_ctx* ctx, int L, const double* unpaired, const double* paired, int maxspan,
                         double B, bool outside, Band* t)
@@ -286,7 +311,19 @@ int messi_ctx_create(int device, messi_ctx** out)
         return MESSI_ECUDA;
     }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+        if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+        if (ctx->side) cudaStreamDestroy(ctx->side);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return MESSI_ECUDA;
+    }
     if (cudaMallocHost((void**)&ctx->status_host, 64) != cudaSuccess) {
+        cudaEventDestroy(ctx->fork_ev);
+        cudaEventDestroy(ctx->join_ev);
+        cudaStreamDestroy(ctx->side);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
         return MESSI_ENOMEM;
@@ -344,6 +381,10 @@ int messi_ctx_destroy(messi_ctx* ctx)
         if (b.p) cudaFree(b.p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->status_host) cudaFreeHost(ctx->status_host);
+    cudaStreamSynchronize(ctx->side);
+    cudaEventDestroy(ctx->fork_ev);
+    cudaEventDestroy(ctx->join_ev);
+    cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MESSI_OK;
@@ -353,6 +394,21 @@ int messi_ctx_stream(messi_ctx* ctx, void** stream)
 {
     if (!ctx || !stream) return MESSI_EINVAL;
     *stream = (void*)ctx->stream;
+    return MESSI_OK;
+}
+
+int messi_selftest_bounded_wait(messi_ctx* ctx, int32_t* status)
+{
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!status) return fail(ctx, MESSI_EINVAL, "bounded-wait self-test: null argument");
+    void* p;
+    if ((rc = ensure(ctx, kSlotVec, 64, &p))) return rc;
+    unsigned int flag = 0;
+    if ((rc = launch_barrier_selftest(ctx, (unsigned int*)p))) return rc;
+    if ((rc = d2h(ctx, &flag, (unsigned int*)p + 2, sizeof(unsigned int)))) return rc;
+    if ((rc = finish(ctx))) return rc;
+    *status = flag ? MESSI_ETIMEOUT : MESSI_OK;
     return MESSI_OK;
 }
 
@@ -535,12 +591,20 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     ModelDev md;
     if ((rc = upload_model(ctx, ds, model, true, true, gapfrequency ? gm.data() : nullptr, &md, true))) return rc;
     if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
-    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
     Band t;
     const int Wb = std::max(0, std::min(ds->W, ds->L - 1));
     if ((rc = band_alloc(ctx, ds->L, Wb, false, &t))) return rc;
-    if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, t.u, nullptr))) return rc;
-    if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
+    // the unpaired columns and the baselines do not need the pairs: they run
+    // on the side stream under the pruning
+    if ((rc = fork_side(ctx))) return rc;
+    {
+        SideLaunches side(ctx);
+        if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, t.u, nullptr)))
+            return rc;
+        if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
+    }
+    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
+    if ((rc = join_side(ctx))) return rc;
     if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0, md.cat.logwF))) return rc;
     if ((rc = run_inside(ctx, t, 1.0))) return rc;
     if ((rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;

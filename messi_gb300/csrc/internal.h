@@ -138,7 +138,8 @@ struct messi_ctx {
     int wave_threads = 0;
     // 0 = choose per pass, 1 = grid barrier, 2 = one thread-block cluster
     int wave_mode = 0;
-    // pair node-update pipeline: 0 = 2 stages x 3 CTAs/SM, 1 = 3 stages x 2 CTAs/SM
+    // pair node-update pipeline (128-pair tiles): 0 = 2 stages x 4 CTAs/SM,
+    // 1 = 3 stages x 3 CTAs/SM, 2 = 2 stages x 3 CTAs/SM
     int prune_shape = 0;
     std::vector<std::pair<const void*, int>> cluster_sizes;  // kernel -> cluster size (0: none)
     // per-kernel event timing (messi_ctx_profile)
@@ -149,6 +150,10 @@ struct messi_ctx {
     int64_t prof_count[messi::kProfKernels] = {0, 0, 0, 0};
     double prof_units[messi::kProfKernels] = {0, 0, 0, 0};
     cudaStream_t stream = nullptr;
+    // second stream for work independent of the pair pruning (unpaired
+    // columns, baselines), forked from and joined back to `stream` by events
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int64_t launches = 0;
     std::string last_error;
     int num_sms = 0;
@@ -268,6 +273,9 @@ int launch_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const double
 // 0-based partner of column c (or -1), logwF the factorised lambda weight.
 int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const int* d_partner,
                          const double* d_mix, double logwF, double* d_total, double* d_pairll);
+// Bounded-wait self-test (scfg.cu): a two-CTA grid barrier that one CTA never
+// reaches; d_sync[2] becomes 1 when the other CTA's wait gives up.
+int launch_barrier_selftest(messi_ctx* ctx, unsigned int* d_sync);
 // Dense L x L pair matrix: vals (nullable) of the unique root pairs, mixed with
 // addw + u[x] + u[y] when addw is finite (the factorised lambda categories).
 int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, const double* d_u, double addw,

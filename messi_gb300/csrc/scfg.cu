@@ -742,6 +742,25 @@ static double band_terms_per_diag(int L, int Wb)
     return terms / Wb;
 }
 
+// Self-test of the bounded grid barrier: CTA 1 never arrives, so CTA 0's wait
+// gives up after `limit` polls, raises the error flag (sync[2]) and returns.
+// Nothing faults and nothing waits unboundedly; the context stays usable.
+__global__ void barrier_selftest_kernel(unsigned int* sync, unsigned int limit)
+{
+    if (blockIdx.x != 0) return;
+    unsigned int gen = 0;
+    grid_sync(sync, gen, limit);
+}
+
+int launch_barrier_selftest(messi_ctx* ctx, unsigned int* d_sync)
+{
+    cudaError_t e = cudaMemsetAsync(d_sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier self-test reset");
+    barrier_selftest_kernel<<<2, 32, 0, ctx->stream>>>(d_sync, 1u << 12);
+    LAUNCH_CHECK(ctx, "barrier_selftest_kernel");
+    return MESSI_OK;
+}
+
 int queue_status_readback(messi_ctx* ctx, const Band& t)
 {
     if (!ctx->status_host) return MESSI_OK;

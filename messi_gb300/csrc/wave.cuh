@@ -43,7 +43,7 @@ static __device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsi
 // reads.  Cells written by other CTAs before the barrier are read with
 // __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
 // those tables.
-static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
+static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen, unsigned int spin_limit = kSpinLimit)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -52,7 +52,7 @@ static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen)
         red_release_add_u32(&sync[0], 1u);
         unsigned int v, spins = 0;
         while ((v = ld_acquire_u32(&sync[0])) < target) {
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 atomicExch(&sync[2], 1u);
                 red_release_add_u32(&sync[0], kBarrierError);
                 v = kBarrierError;

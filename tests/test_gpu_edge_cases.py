@@ -97,3 +97,21 @@ def test_invalid_inputs_are_rejected(c1, p15):
     bad[0] = ds.numcols + 5
     with pytest.raises(MessiError):
         api.felsensteincudapaired(ds, bad, _params(p15, ds))
+
+
+def test_bounded_wait_gives_up_and_context_stays_usable():
+    """A grid barrier that one CTA never reaches: the waiting CTA gives up
+    after a bounded spin, the host reads MESSI_ETIMEOUT, and the context
+    keeps working (no fault, no unbounded wait)."""
+    from messi_gb300 import api
+    from messi_gb300._lib import MESSI_ETIMEOUT
+    ctx = api.get_context()
+    assert ctx.selftest_bounded_wait() == MESSI_ETIMEOUT
+    L = 12
+    u = np.full(L, -5.0)
+    p = np.full((L, L), -np.inf)
+    p[0, 11] = p[11, 0] = -3.0
+    Z = api.computeinsideKH99(u, p, ctx=ctx)
+    Zref = co.inside(u, p)[0, 0, L - 1]
+    assert abs(Z - Zref) <= REL * abs(Zref)
+    assert ctx.selftest_bounded_wait() == MESSI_ETIMEOUT
