@@ -403,7 +403,7 @@ int messi_selftest_bounded_wait(messi_ctx* ctx, int32_t* status)
     if (rc) return rc;
     if (!status) return fail(ctx, MESSI_EINVAL, "bounded-wait self-test: null argument");
     void* p;
-    if ((rc = ensure(ctx, kSlotVec, 64, &p))) return rc;
+    if ((rc = ensure(ctx, kSlotVec, kSyncWords * sizeof(unsigned int), &p))) return rc;
     unsigned int flag = 0;
     if ((rc = launch_barrier_selftest(ctx, (unsigned int*)p))) return rc;
     if ((rc = d2h(ctx, &flag, (unsigned int*)p + 2, sizeof(unsigned int)))) return rc;
@@ -690,7 +690,7 @@ int decode_device(messi_ctx* ctx, int L, const double* d_single, const double* d
     void *work, *ints;
     const size_t LL = (size_t)L * L;
     if ((rc = ensure(ctx, kSlotDecodeF, ((size_t)L + 3 * LL) * sizeof(float), &work))) return rc;
-    if ((rc = ensure(ctx, kSlotDecodeI, (LL + 3 * (size_t)L + 16) * sizeof(int), &ints))) return rc;
+    if ((rc = ensure(ctx, kSlotDecodeI, (LL + 3 * (size_t)L + 16 + kSyncWords) * sizeof(int), &ints))) return rc;
     int* scol = (int*)ints;
     int* stack = scol + LL;
     int* d_paired = stack + 2 * ((size_t)L + 1);

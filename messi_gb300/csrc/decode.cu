@@ -371,7 +371,7 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
     LAUNCH_CHECK(ctx, "to_float_kernel");
     cudaError_t e = cudaMemsetAsync(erow, 0, sizeof(float) * 2 * LL, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_scol, 0, sizeof(int) * LL, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "decoding tables reset");
     if (L > 1) {
         const float a = (float)alpha;

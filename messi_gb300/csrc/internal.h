@@ -15,6 +15,9 @@
 namespace messi {
 
 constexpr int kTile = 128;          // unique pairs per CTA in the pruning kernels
+// Grid-barrier words of the wavefront kernels: [0] = arrivals, [2] =
+// host-visible error flag (wave.cuh).
+constexpr int kSyncWords = 4;
 constexpr int kMaxLambda = 8;       // per-lambda conditionals kept in registers
 constexpr int kMaxStack = 512;      // tree height limit of the unpaired kernel
 constexpr int kEigStride = 16 + 256 + 16;  // eigenvalues, U (row-major), sqrt(pi)
@@ -91,7 +94,7 @@ struct Band {
     float *PP, *SL, *nrm;
     double *b, *cb, *u, *Zd;
     int* maxspan;
-    unsigned int* sync;  // grid barrier of the wavefront kernels: count, generation, error flag, spare
+    unsigned int* sync;  // kSyncWords grid-barrier words of the wavefront kernels
 };
 
 // Band tables of a batch of alignments for the batched inside pass.  Bands

@@ -39,7 +39,8 @@ struct NoAllocScratch {
     float tabs[6][kNoAllocCells];           // Lrow, Lcol, Srow, Scol, Frow, pb
     float suf[2 * (kNoAllocMaxL + 1)];      // Ssuf (+ unused outside half)
     double vec[2 * kNoAllocMaxL + 8];       // b, cb
-    int maxspan[64];
+    int maxspan[16];
+    unsigned int sync[kSyncWords];          // grid-barrier words of the wavefront kernel
 };
 
 // Host code must not use this name as a device address: it is a host-side
@@ -109,7 +110,7 @@ extern "C" int messi_inside_noalloc(void* stream, int32_t L, const double* d_unp
     t.u = const_cast<double*>(d_unpaired);  // read only
     t.Zd = d_Z;
     t.maxspan = s->maxspan;
-    t.sync = reinterpret_cast<unsigned int*>(s->maxspan + 16);
+    t.sync = s->sync;
     t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = nullptr;
     if ((rc = launch_baseline(&local, t, B))) return rc;
     if ((rc = launch_bandprep_from_dense(&local, t, d_paired, B))) return rc;

@@ -138,7 +138,7 @@ int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
     if ((rc = ensure(ctx, 6, (size_t)(L + 1) * sizeof(float) * 2, &p))) return rc;
     t->Ssuf = (float*)p;
     t->Osuf = t->Ssuf + (L + 1);
-    if ((rc = ensure(ctx, 7, (size_t)(3 * L + 8) * sizeof(double), &p))) return rc;
+    if ((rc = ensure(ctx, 7, (size_t)(3 * L + 8 + kSyncWords / 2) * sizeof(double), &p))) return rc;
     t->b = (double*)p;
     t->cb = t->b + L;
     t->u = t->cb + (L + 1);
@@ -708,7 +708,7 @@ static int launch_wave2(messi_ctx* ctx, const void* grid_kernel, const void* clu
 {
     int threads = wave_threads(ctx, band_cells);
     const int cl = wave_cluster_size(ctx, cluster_kernel, kWaveMaxThreads, terms_per_diag);
-    cudaError_t e = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
     if (cl > 0) {
         threads = kWaveMaxThreads;
@@ -754,7 +754,7 @@ __global__ void barrier_selftest_kernel(unsigned int* sync, unsigned int limit)
 
 int launch_barrier_selftest(messi_ctx* ctx, unsigned int* d_sync)
 {
-    cudaError_t e = cudaMemsetAsync(d_sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    cudaError_t e = cudaMemsetAsync(d_sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier self-test reset");
     barrier_selftest_kernel<<<2, 32, 0, ctx->stream>>>(d_sync, 1u << 12);
     LAUNCH_CHECK(ctx, "barrier_selftest_kernel");
@@ -822,7 +822,7 @@ int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandB
     const size_t off_wbs = bytes;
     bytes = al(bytes + (size_t)n * sizeof(int));
     const size_t off_sync = bytes;
-    bytes = al(bytes + 4 * sizeof(unsigned int));
+    bytes = al(bytes + kSyncWords * sizeof(unsigned int));
     const size_t off_Z = bytes;
     bytes = al(bytes + (size_t)n * sizeof(double));
     cudaError_t e = cudaMalloc(&bb->mem, bytes);
@@ -913,7 +913,7 @@ int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
     const int grid = wave_grid(ctx, (const void*)inside_wave_batch_kernel,
                                (int)std::min<long long>(bb.total_cols, 1 << 30), threads);
     prof_begin(ctx, 1, cells);
-    cudaError_t e = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned int), ctx->stream);
+    cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
     e = cudaLaunchCooperativeKernel((const void*)inside_wave_batch_kernel, dim3(grid), dim3(threads), args, 0,
                                     ctx->stream);

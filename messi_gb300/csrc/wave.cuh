@@ -29,17 +29,12 @@ static __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int
 // from the same load, that the launch failed.
 constexpr unsigned int kBarrierError = 1u << 30;
 
-static __device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v)
-{
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // sync[0] = arrivals, monotonic within a launch (barrier g completes when it
-// reaches g * gridDim.x, so the last arrival's add is the release itself);
-// sync[2] = error flag for the host.  Returns false (in every thread of the
-// CTA) once any CTA has given up waiting.  The CTA barrier orders every
-// thread's cells before thread 0's release-add; thread 0's acquire poll and
-// the second CTA barrier order the other CTAs' cells before the CTA's next
+// reaches g * gridDim.x); sync[2] = error flag for the host.  Returns false
+// (in every thread of the CTA) once any CTA has given up waiting.  Arrival is
+// the cooperative-groups grid-barrier pattern: a CTA barrier, then thread 0's
+// device-scope fence and atomic add; thread 0 polls with acquire loads and a
+// second CTA barrier orders the other CTAs' cells before the CTA's next
 // reads.  Cells written by other CTAs before the barrier are read with
 // __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
 // those tables.
@@ -49,12 +44,13 @@ static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen, unsigned
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned int target = (gen + 1) * gridDim.x;
-        red_release_add_u32(&sync[0], 1u);
+        __threadfence();
+        atomicAdd(&sync[0], 1u);
         unsigned int v, spins = 0;
         while ((v = ld_acquire_u32(&sync[0])) < target) {
             if (++spins > spin_limit) {
                 atomicExch(&sync[2], 1u);
-                red_release_add_u32(&sync[0], kBarrierError);
+                atomicAdd(&sync[0], kBarrierError);
                 v = kBarrierError;
                 break;
             }

@@ -115,3 +115,25 @@ def test_bounded_wait_gives_up_and_context_stays_usable():
     Zref = co.inside(u, p)[0, 0, L - 1]
     assert abs(Z - Zref) <= REL * abs(Zref)
     assert ctx.selftest_bounded_wait() == MESSI_ETIMEOUT
+
+
+def test_wavefront_results_repeat_bit_for_bit():
+    """The grid-barrier wavefronts (inside, outside, decoding) give the same
+    bits on every run: a barrier that let a CTA read a cell before it was
+    written would show up as run-to-run differences."""
+    from messi_gb300 import api
+    rng = np.random.default_rng(11)
+    L, W = 400, 150
+    u = rng.uniform(-30.0, -8.0, L)
+    p = np.full((L, L), -np.inf)
+    for i in range(L):
+        for j in range(i + 1, min(L, i + W + 1)):
+            p[i, j] = p[j, i] = u[i] + u[j] + rng.normal(-2.0, 3.0)
+    Z0 = api.computeinsideKH99(u, p)
+    post0 = api.computeposteriors(u, p)
+    for _ in range(8):
+        assert api.computeinsideKH99(u, p) == Z0
+    for _ in range(3):
+        post = api.computeposteriors(u, p)
+        for a, b in zip(post, post0):
+            np.testing.assert_array_equal(a, b)
