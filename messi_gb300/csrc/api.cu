@@ -158,11 +158,10 @@ int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool p
     const double* d_bl = (const double*)(base + o_bl);
     if (pairs) {
         void* p;
-        // FP32 matrices followed by their TF32 hi/lo split
-        if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * 3 * sizeof(float), &p))) return rc;
+        if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * sizeof(float), &p))) return rc;
         md->P16 = (float*)p;
-        if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, nullptr, ds->numnodes, c.C, md->P16,
-                                    md->P16 + (size_t)c.C * ds->numnodes * 256))) return rc;
+        if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, nullptr, ds->numnodes, c.C, md->P16)))
+            return rc;
     }
     if (unpaired) {
         void* p;

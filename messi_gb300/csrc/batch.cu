@@ -344,13 +344,12 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     const int* d_grp = (const int*)(base + o_grp);
     const uint8_t* d_gap = gapfrequency ? (const uint8_t*)(base + o_gap) : nullptr;
     void *pt, *p4;
-    if (grow(b->P16, (size_t)C * b->total_nodes * 512 * sizeof(float), &pt))
+    if (grow(b->P16, (size_t)C * b->total_nodes * 256 * sizeof(float), &pt))
         return fail(ctx, MESSI_ENOMEM, "batch transition matrices");
     if (grow(b->P4, (size_t)nsite * b->total_nodes * 16 * sizeof(double), &p4))
         return fail(ctx, MESSI_ENOMEM, "batch unpaired transition matrices");
     const float* d_PT = (const float*)pt;
-    if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, d_grp, b->total_nodes, C, nullptr,
-                               (float*)pt)))
+    if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, d_grp, b->total_nodes, C, (float*)pt)))
         return rc;
     if ((rc = launch_build_P4(ctx, (const double*)(base + o_eig4), d_bl, d_grp, b->total_nodes, nsite,
                               (double*)p4)))

@@ -248,10 +248,10 @@ void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e
 // ---- pruning kernels (prune.cu) ----
 // nodegrp: [numnodes] model group of each node, -1 for a root (nullptr: one
 // tree, root = node 0, group 0).  Category tables are [group][C][...].
-// d_P (nullable): FP32 matrices [C][numnodes][256]; d_PT: their 3xTF32 split
-// [C][numnodes][2][256].
+// d_P: FP32 matrices [C][numnodes][256] (the pruning kernel splits them into
+// TF32 hi/lo parts in registers).
 int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, const int* d_nodegrp, int numnodes,
-                     int C, float* d_P, float* d_PT);
+                     int C, float* d_P);
 int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, const int* d_nodegrp, int numnodes,
                     int nsite, double* d_P4);
 // The tensor-core node update over `nt` tiles of one level (root tiles when root).

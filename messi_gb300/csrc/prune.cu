@@ -5,18 +5,18 @@
 // felsensteinhelper16 :153-200, sumfinal :428-442, storearr/logsumexparr
 // :135-151) with:
 //   * build_P16_kernel: P = exp(Qt) per (category, branch) in FP64 from the
-//     host eigensystem, stored as FP32 rows (row = parent state) and as their
-//     3xTF32 hi/lo split;
+//     host eigensystem, stored as FP32 rows (row = parent state);
 //   * prune_mma_kernel: one launch per tree level and category pass; a warp
 //     owns 32 unique pairs of one node, gathers the child rows with cp.async
 //     (two categories in flight) and does both child mat-vecs on the tensor
-//     cores (3xTF32 mma.sync).  Rows are rescaled by an exact power of two
+//     cores (3xTF32 mma.sync, operands split into hi/lo in registers).  Rows are rescaled by an exact power of two
 //     (exponent kept as an int), which computes the same likelihood as the
 //     reference's divide-by-max (felsenstein.cu:193-198);
 //   * the root variant folds sumfinal and the category log-sum-exp into the
 //     same pass (FP64 log-likelihood reduction).
-// unpaired_kernel restates computeunpairedlikelihoodscat (src/FARCE.jl:742-773)
-// in FP64 with the CPU rescaling rule.
+// unpaired_site_kernel + unpaired_mix_kernel restate
+// computeunpairedlikelihoodscat (src/FARCE.jl:742-773) in FP64 with the CPU
+// rescaling rule.
 #include <algorithm>
 #include <cmath>
 
@@ -24,18 +24,9 @@
 
 namespace messi {
 
-__device__ __forceinline__ uint32_t f32_to_tf32(float x)
-{
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-
-// P[c][v][a][d] in FP32 and, for the tensor-core pruning kernel, its 3xTF32
-// split PT[c][v][0|1][a][d] = hi, lo with P ~= hi + lo (both TF32 values).
+// P[c][v][a][d] in FP32 (row = parent state), from the FP64 eigensystem.
 __global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl,
-                                 const int* __restrict__ nodegrp, int numnodes, int C, float* __restrict__ P,
-                                 float* __restrict__ PT)
+                                 const int* __restrict__ nodegrp, int numnodes, int C, float* __restrict__ P)
 {
     const int v = blockIdx.x, c = blockIdx.y, t = threadIdx.x;
     const int grp = nodegrp ? nodegrp[v] : (v == 0 ? -1 : 0);
@@ -61,11 +52,7 @@ __global__ void build_P16_kernel(const double* __restrict__ eig, const double* _
         s *= sp[d] / sp[a];
         out = (s <= 0.0) ? 0.f : (float)s;  // absmat clamp (1e-50 rounds to 0 in FP32)
     }
-    if (P) P[((size_t)c * numnodes + v) * 256 + t] = out;
-    const uint32_t hi = f32_to_tf32(out);
-    const uint32_t lo = f32_to_tf32(out - __uint_as_float(hi));
-    PT[(((size_t)c * numnodes + v) * 2 + 0) * 256 + t] = __uint_as_float(hi);
-    PT[(((size_t)c * numnodes + v) * 2 + 1) * 256 + t] = __uint_as_float(lo);
+    P[((size_t)c * numnodes + v) * 256 + t] = out;
 }
 
 __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl,
@@ -91,9 +78,9 @@ __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* _
 }
 
 int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, const int* d_nodegrp, int numnodes,
-                     int C, float* d_P, float* d_PT)
+                     int C, float* d_P)
 {
-    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, d_nodegrp, numnodes, C, d_P, d_PT);
+    build_P16_kernel<<<dim3(numnodes, C), 256, 0, ctx->stream>>>(d_eig, d_bl, d_nodegrp, numnodes, C, d_P);
     LAUNCH_CHECK(ctx, "build_P16_kernel");
     return MESSI_OK;
 }
@@ -151,6 +138,19 @@ __device__ __forceinline__ void split_a(float x, uint32_t& hi, uint32_t& lo)
 {
     hi = (__float_as_uint(x) + 0x1000u) & 0xffffe000u;
     lo = __float_as_uint(x - __uint_as_float(hi));
+}
+
+// B operand (four entries of P) split the same way, in registers: one FP32
+// load per fragment instead of a hi and a lo load.
+__device__ __forceinline__ void split_b(const float4& p, float4& hi, float4& lo)
+{
+    uint32_t h[4], l[4];
+    split_a(p.x, h[0], l[0]);
+    split_a(p.y, h[1], l[1]);
+    split_a(p.z, h[2], l[2]);
+    split_a(p.w, h[3], l[3]);
+    hi = make_float4(__uint_as_float(h[0]), __uint_as_float(h[1]), __uint_as_float(h[2]), __uint_as_float(h[3]));
+    lo = make_float4(__uint_as_float(l[0]), __uint_as_float(l[1]), __uint_as_float(l[2]), __uint_as_float(l[3]));
 }
 
 // D[mt][nt][4] += X (rows g + 8k, k = 0..3) x P^T for one child.
@@ -297,8 +297,8 @@ __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
             XR[k] = st.x[4 + k][lane];
         }
         const int e = (le ? st.e[0][lane] : 0) + (re ? st.e[1][lane] : 0);
-        const float* ptl = PT + ((size_t)(c0 + cc) * numnodes + nd.left) * 512;
-        const float* ptr = PT + ((size_t)(c0 + cc) * numnodes + nd.right) * 512;
+        const float* ptl = PT + ((size_t)(c0 + cc) * numnodes + nd.left) * 256;
+        const float* ptr = PT + ((size_t)(c0 + cc) * numnodes + nd.right) * 256;
         float4 Bh[2], Bl[2];
         float DL[2][2][4], DR[2][2][4];
 #pragma unroll
@@ -308,16 +308,10 @@ __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
 #pragma unroll
                 for (int i = 0; i < 4; i++) { DL[mt][nt][i] = 0.f; DR[mt][nt][i] = 0.f; }
 #pragma unroll
-        for (int nt = 0; nt < 2; nt++) {
-            Bh[nt] = ldg4(ptl + (8 * nt + g) * 16 + 4 * t);
-            Bl[nt] = ldg4(ptl + 256 + (8 * nt + g) * 16 + 4 * t);
-        }
+        for (int nt = 0; nt < 2; nt++) split_b(ldg4(ptl + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
         child_mma(XL, Bh, Bl, DL);
 #pragma unroll
-        for (int nt = 0; nt < 2; nt++) {
-            Bh[nt] = ldg4(ptr + (8 * nt + g) * 16 + 4 * t);
-            Bl[nt] = ldg4(ptr + 256 + (8 * nt + g) * 16 + 4 * t);
-        }
+        for (int nt = 0; nt < 2; nt++) split_b(ldg4(ptr + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
         child_mma(XR, Bh, Bl, DR);
         // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}
         float V[4][4];
@@ -453,7 +447,7 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
 {
     (void)nlam;
     const int chunk = ds->chunk;
-    const float* d_PT = d_P + (size_t)C * ds->numnodes * 256;
+    const float* d_PT = d_P;
     for (int c0 = 0; c0 < C; c0 += chunk) {
         const int nc = std::min(chunk, C - c0);
         for (int lv = 1; lv <= ds->H; lv++) {
