@@ -391,59 +391,88 @@ __device__ __forceinline__ void inside_init_cell(const Band& t, int i, const Rul
     if (i == t.L - 1) t.Ssuf[i] = S;
 }
 
-// Cell (i, i+d) by a group of G lanes (every lane of the warp calls this,
-// `valid` false for padding groups: the shuffles need the whole warp).
-__device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool valid, int lane, int G, const Rules& R)
+// Cell (i, i+d) in two parts, by a group of G lanes (every lane of the warp
+// calls both, `valid` false for padding groups: the shuffles need the whole
+// warp).  The split sum runs over k = 0 .. d-1 of L(i, i+k) + S(i+k+1, j).
+// inside_cell_partial sums the split points k = 1 .. d-2, whose two cells
+// both have spans <= d-2, reduces them over the group and loads the pair
+// score and the enclosed F (span d-2); inside_cell_finish adds the two split
+// points that touch diagonal d-1 (k = 0 and k = d-1) and writes the cell
+// (lane 0).  Between the two a wavefront may wait for diagonal d-1.
+struct CellPartial {
+    float m, s, pbv, fin;
+};
+
+__device__ __forceinline__ CellPartial inside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G)
 {
     const int RS = t.RS;
-    float m = -INFINITY, s = 0.f;
-    // pair score and enclosed F (two diagonals back) issued before the split sum
-    float pbv = -INFINITY, fin = -INFINITY;
+    CellPartial c{-INFINITY, 0.f, -INFINITY, -INFINITY};
     if (valid && lane == 0 && d >= 2) {
-        pbv = t.pb[(size_t)i * RS + d];
-        fin = __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2));
+        c.pbv = t.pb[(size_t)i * RS + d];
+        c.fin = __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2));
     }
-    if (valid) {
+    if (valid && d >= 3) {
         const float* lrow = t.Lrow + (size_t)i * RS;
         const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
-        int k = lane;
-        for (; k + 7 * G < d; k += 8 * G) {
+        const int kend = d - 1;
+        int k = 1 + lane;
+        for (; k + 7 * G < kend; k += 8 * G) {
             float x[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) x[q] = __ldcg(lrow + k + q * G) + __ldcg(scol - k - q * G);
-            lse_add8(m, s, x);
+            lse_add8(c.m, c.s, x);
         }
-        for (; k + 3 * G < d; k += 4 * G)
-            lse_add4(m, s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
+        for (; k + 3 * G < kend; k += 4 * G)
+            lse_add4(c.m, c.s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
                      __ldcg(lrow + k + 2 * G) + __ldcg(scol - k - 2 * G),
                      __ldcg(lrow + k + 3 * G) + __ldcg(scol - k - 3 * G));
-        for (; k < d; k += G) lse_add(m, s, __ldcg(lrow + k) + __ldcg(scol - k));
+        for (; k < kend; k += G) lse_add(c.m, c.s, __ldcg(lrow + k) + __ldcg(scol - k));
     }
-    group_reduce_rt(m, s, G);
-    if (valid && lane == 0) {
-        const int j = i + d;
-        const float tmp = lse_val(m, s);
-        const float v = pbv + fin;
-        const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
-        const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
-        const float Lv = R.r[6] + v;
-        t.Lrow[(size_t)i * RS + d] = Lv;
-        t.Lcol[(size_t)j * RS + d] = Lv;
-        t.Srow[(size_t)i * RS + d] = S;
-        t.Scol[(size_t)j * RS + d] = S;
-        t.Frow[(size_t)i * RS + d] = F;
-        if (j == t.L - 1) t.Ssuf[i] = S;
-    }
+    group_reduce_rt(c.m, c.s, G);
+    return c;
+}
+
+__device__ __forceinline__ void inside_cell_finish(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
+                                                   const Rules& R)
+{
+    if (!(valid && lane == 0)) return;
+    const int RS = t.RS;
+    const int j = i + d;
+    const float* lrow = t.Lrow + (size_t)i * RS;
+    const float* scol = t.Scol + (size_t)j * RS + (d - 1);
+    lse_add(c.m, c.s, __ldcg(lrow) + __ldcg(scol));  // k = 0
+    if (d >= 2) lse_add(c.m, c.s, __ldcg(lrow + d - 1) + __ldcg(scol - (d - 1)));  // k = d - 1
+    const float tmp = lse_val(c.m, c.s);
+    const float v = c.pbv + c.fin;
+    const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
+    const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
+    const float Lv = R.r[6] + v;
+    t.Lrow[(size_t)i * RS + d] = Lv;
+    t.Lcol[(size_t)j * RS + d] = Lv;
+    t.Srow[(size_t)i * RS + d] = S;
+    t.Scol[(size_t)j * RS + d] = S;
+    t.Frow[(size_t)i * RS + d] = F;
+    if (j == t.L - 1) t.Ssuf[i] = S;
+}
+
+__device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool valid, int lane, int G, const Rules& R)
+{
+    inside_cell_finish(t, i, d, valid, lane, inside_cell_partial(t, i, d, valid, lane, G), R);
 }
 
 // All band diagonals of the inside pass (span 0 initialisation included).
+// Each diagonal d: the partial sums of the CTA's first cells of d (spans
+// <= d-2, complete) are computed between the CTA's arrival at the barrier of
+// diagonal d-1 and its wait there, so the barrier latency overlaps that work;
+// after the wait the cells are finished, and any further cells of d (more
+// cells than groups) are computed whole.
 template <int MODE>
 __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
     unsigned int gen = 0;
     const int L = t.L;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
-    if (!wave_sync<MODE>(t.sync, gen)) return;
+    wave_arrive<MODE>(t.sync);
     for (int d = 1; d <= t.Wb; d++) {
         const int G = group_width(d);
         const int gpb = blockDim.x / G;
@@ -451,12 +480,17 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
         const int lane = threadIdx.x & (G - 1);
         const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
         const int ncell = L - d;
-        for (int base = 0; base < ncell; base += total) {
+        const CellPartial c = inside_cell_partial(t, gid0, d, gid0 < ncell, lane, G);
+        if (!wave_wait<MODE>(t.sync, gen)) return;
+        inside_cell_finish(t, gid0, d, gid0 < ncell, lane, c, R);
+        for (int base = total; base < ncell; base += total) {
             const int i = base + gid0;
             inside_cell(t, i, d, i < ncell, lane, G, R);
         }
-        if (!wave_sync<MODE>(t.sync, gen)) return;
+        wave_arrive<MODE>(t.sync);
     }
+    // a cluster barrier's arrival is completed by a wait before the CTA exits
+    if (MODE == kCluster) wave_wait<MODE>(t.sync, gen);
 }
 
 // Batched inside over n alignments in one persistent launch: diagonal d of
@@ -500,7 +534,7 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
             inside_init_cell(bands[b], (int)(it - cumL[b]), R, B);
         }
     }
-    if (!grid_sync(sync, gen)) return;
+    grid_arrive(sync);
     const int maxW = n > 0 ? wbs[0] : 0;
     for (int d = 1; d <= maxW; d++) {
         const int nact = batch_active(wbs, n, d);
@@ -510,13 +544,20 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
         const long long total = (long long)gridDim.x * gpb;
         const int lane = threadIdx.x & (G - 1);
         const long long gid0 = (long long)blockIdx.x * gpb + threadIdx.x / G;
-        for (long long base = 0; base < ncell; base += total) {
+        // first cells: partial sums before the wait (as in inside_wave_kernel)
+        const bool v0 = gid0 < ncell;
+        const int b0 = v0 ? batch_band(cumL, nact, d, gid0) : 0;
+        const int i0 = v0 ? (int)(gid0 - (cumL[b0] - (long long)d * b0)) : 0;
+        const CellPartial c = inside_cell_partial(bands[b0], i0, d, v0, lane, G);
+        if (!grid_wait(sync, gen)) return;
+        inside_cell_finish(bands[b0], i0, d, v0, lane, c, R);
+        for (long long base = total; base < ncell; base += total) {
             const long long it = base + gid0;
             const bool valid = it < ncell;
             const int b = valid ? batch_band(cumL, nact, d, it) : 0;
             inside_cell(bands[b], valid ? (int)(it - (cumL[b] - (long long)d * b)) : 0, d, valid, lane, G, R);
         }
-        if (!grid_sync(sync, gen)) return;
+        grid_arrive(sync);
     }
 }
 

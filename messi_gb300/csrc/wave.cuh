@@ -38,14 +38,22 @@ constexpr unsigned int kBarrierError = 1u << 30;
 // reads.  Cells written by other CTAs before the barrier are read with
 // __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
 // those tables.
-static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen, unsigned int spin_limit = kSpinLimit)
+// The barrier in two halves, so that a CTA can work between its arrival and
+// its wait on cells that do not depend on the other CTAs' latest writes.
+static __device__ __forceinline__ void grid_arrive(unsigned int* sync)
 {
-    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned int target = (gen + 1) * gridDim.x;
         __threadfence();
         atomicAdd(&sync[0], 1u);
+    }
+}
+
+static __device__ bool grid_wait(unsigned int* sync, unsigned int& gen, unsigned int spin_limit = kSpinLimit)
+{
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        const unsigned int target = (gen + 1) * gridDim.x;
         unsigned int v, spins = 0;
         while ((v = ld_acquire_u32(&sync[0])) < target) {
             if (++spins > spin_limit) {
@@ -63,12 +71,38 @@ static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen, unsigned
     return s_ok != 0;
 }
 
+static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen, unsigned int spin_limit = kSpinLimit)
+{
+    grid_arrive(sync);
+    return grid_wait(sync, gen, spin_limit);
+}
+
 // Synchronisation of the wavefront kernels.  kGrid: the bounded grid
 // barrier above (any grid of co-resident CTAs); kCluster: the hardware
 // barrier of one thread-block cluster (the whole launch is one cluster), a
 // release/acquire at cluster scope.  Cells written by other CTAs of the
 // cluster are read through L2 (__ldcg) as in grid mode.
 enum WaveSync { kGrid = 0, kCluster = 1 };
+
+template <int MODE>
+static __device__ __forceinline__ void wave_arrive(unsigned int* sync)
+{
+    if (MODE == kCluster) {
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+        return;
+    }
+    grid_arrive(sync);
+}
+
+template <int MODE>
+static __device__ __forceinline__ bool wave_wait(unsigned int* sync, unsigned int& gen)
+{
+    if (MODE == kCluster) {
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+        return true;
+    }
+    return grid_wait(sync, gen);
+}
 
 template <int MODE>
 static __device__ __forceinline__ bool wave_sync(unsigned int* sync, unsigned int& gen)
