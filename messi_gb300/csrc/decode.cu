@@ -61,12 +61,92 @@ __global__ void to_double_kernel(const float* __restrict__ in, double* __restric
 
 // pair: L x L as uploaded from the Julia matrix (column-major); it is read as
 // pair[i*L + k], the reference kernel's indexing (the matrix is symmetric).
+//
+// Cell (i, j = i+d): the best split over k = i+1 .. j-1 of
+// alpha*pair(i,k) + e(i+1,k-1) + e(k+1,j) reads cells of spans <= d-2 only,
+// as does e2 = alpha*pair(i,j) + e(i+1,j-1); only e1 = single(i) + e(i+1,j)
+// reads diagonal d-1.  decode_cell_split computes the split maximum (lowest k
+// among equal values, the reference's order) and e2; decode_cell_finish adds
+// e1 and writes the cell.  The wavefront computes the split part of its first
+// cells between its arrival at the barrier of diagonal d-1 and its wait.
+struct DecodePart {
+    float bv, e2;
+    int bk;
+};
+
+__device__ __forceinline__ DecodePart decode_cell_split(const float* __restrict__ pair, const float* erow,
+                                                        const float* ecol, int L, float alpha, int i, int d,
+                                                        bool valid, int lane, int G)
+{
+    DecodePart p{-1e10f, -INFINITY, 0};  // the reference's initial maximum and index
+    const int j = i + d;
+    if (valid) {
+        const float* prow = pair + (size_t)i * L;
+        const float* er = erow + (size_t)(i + 1) * L;  // e(i+1, k-1)
+        const float* ec = ecol + (size_t)j * L;        // e(k+1, j)
+        int k = i + 1 + lane;
+        // four splits per step, loads issued together, compared in ascending k
+        for (; k + 3 * G <= j - 1; k += 4 * G) {
+            float v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int kq = k + q * G;
+                v[q] = __fmaf_rn(alpha, __ldg(prow + kq), __ldcg(er + kq - 1)) + __ldcg(ec + kq + 1);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (v[q] > p.bv) {
+                    p.bv = v[q];
+                    p.bk = k + q * G;
+                }
+        }
+        for (; k <= j - 1; k += G) {
+            const float v = __fmaf_rn(alpha, __ldg(prow + k), __ldcg(er + k - 1)) + __ldcg(ec + k + 1);
+            if (v > p.bv) {
+                p.bv = v;
+                p.bk = k;
+            }
+        }
+        if (lane == 0)
+            p.e2 = __fmaf_rn(alpha, __ldg(pair + (size_t)i * L + j), __ldcg(erow + (size_t)(i + 1) * L + j - 1));
+    }
+    for (int off = G >> 1; off > 0; off >>= 1) {
+        const float v2 = __shfl_xor_sync(0xffffffffu, p.bv, off);
+        const int k2 = __shfl_xor_sync(0xffffffffu, p.bk, off);
+        amax_merge(p.bv, p.bk, v2, k2);
+    }
+    return p;
+}
+
+__device__ __forceinline__ void decode_cell_finish(const float* __restrict__ single, float* erow, float* ecol,
+                                                   int* scol, int L, int i, int d, bool valid, int lane,
+                                                   const DecodePart& p)
+{
+    if (!(valid && lane == 0)) return;
+    const int j = i + d;
+    const float e1 = __ldg(single + i) + __ldcg(erow + (size_t)(i + 1) * L + j);
+    float mv = e1;
+    int sv = -1;
+    if (p.e2 > mv) {
+        mv = p.e2;
+        sv = -2;
+    }
+    if (p.bv > mv) {
+        mv = p.bv;
+        sv = p.bk + 1;
+    }
+    erow[(size_t)i * L + j] = mv;
+    ecol[(size_t)j * L + i] = mv;
+    scol[(size_t)j * L + i] = sv;
+}
+
 __global__ void __launch_bounds__(kWaveMaxThreads) decode_wave_kernel(const float* __restrict__ single,
                                                           const float* __restrict__ pair, int L, float alpha,
                                                           float* __restrict__ erow, float* __restrict__ ecol,
                                                           int* __restrict__ scol, unsigned int* sync)
 {
     unsigned int gen = 0;
+    grid_arrive(sync);  // spans 0 and -1 are the zero-filled tables
     for (int d = 1; d < L; d++) {
         const int G = group_width(d - 1);
         const int gpb = blockDim.x / G;
@@ -74,64 +154,16 @@ __global__ void __launch_bounds__(kWaveMaxThreads) decode_wave_kernel(const floa
         const int lane = threadIdx.x & (G - 1);
         const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
         const int ncell = L - d;
-        for (int base = 0; base < ncell; base += total) {
+        const DecodePart p0 = decode_cell_split(pair, erow, ecol, L, alpha, gid0, d, gid0 < ncell, lane, G);
+        if (!grid_wait(sync, gen)) return;
+        decode_cell_finish(single, erow, ecol, scol, L, gid0, d, gid0 < ncell, lane, p0);
+        for (int base = total; base < ncell; base += total) {
             const int i = base + gid0;
             const bool valid = i < ncell;
-            const int j = i + d;
-            float bv = -1e10f;  // the reference's initial maximum and index
-            int bk = 0;
-            if (valid) {
-                const float* prow = pair + (size_t)i * L;
-                const float* er = erow + (size_t)(i + 1) * L;  // e(i+1, k-1)
-                const float* ec = ecol + (size_t)j * L;        // e(k+1, j)
-                int k = i + 1 + lane;
-                // four splits per step, loads issued together, compared in ascending k
-                for (; k + 3 * G <= j - 1; k += 4 * G) {
-                    float v[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const int kq = k + q * G;
-                        v[q] = __fmaf_rn(alpha, __ldg(prow + kq), __ldcg(er + kq - 1)) + __ldcg(ec + kq + 1);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (v[q] > bv) {
-                            bv = v[q];
-                            bk = k + q * G;
-                        }
-                }
-                for (; k <= j - 1; k += G) {
-                    const float v = __fmaf_rn(alpha, __ldg(prow + k), __ldcg(er + k - 1)) + __ldcg(ec + k + 1);
-                    if (v > bv) {
-                        bv = v;
-                        bk = k;
-                    }
-                }
-            }
-            for (int off = G >> 1; off > 0; off >>= 1) {
-                const float v2 = __shfl_xor_sync(0xffffffffu, bv, off);
-                const int k2 = __shfl_xor_sync(0xffffffffu, bk, off);
-                amax_merge(bv, bk, v2, k2);
-            }
-            if (valid && lane == 0) {
-                const float e1 = __ldg(single + i) + __ldcg(erow + (size_t)(i + 1) * L + j);
-                const float e2 = __fmaf_rn(alpha, __ldg(pair + (size_t)i * L + j), __ldcg(erow + (size_t)(i + 1) * L + j - 1));
-                float mv = e1;
-                int sv = -1;
-                if (e2 > mv) {
-                    mv = e2;
-                    sv = -2;
-                }
-                if (bv > mv) {
-                    mv = bv;
-                    sv = bk + 1;
-                }
-                erow[(size_t)i * L + j] = mv;
-                ecol[(size_t)j * L + i] = mv;
-                scol[(size_t)j * L + i] = sv;
-            }
+            const DecodePart p = decode_cell_split(pair, erow, ecol, L, alpha, i, d, valid, lane, G);
+            decode_cell_finish(single, erow, ecol, scol, L, i, d, valid, lane, p);
         }
-        if (!grid_sync(sync, gen)) return;
+        grid_arrive(sync);
     }
 }
 
