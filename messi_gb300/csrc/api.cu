@@ -472,19 +472,22 @@ int messi_felsenstein_pairs(messi_ctx* ctx, messi_dataset* ds, const messi_model
     ModelDev md;
     if ((rc = upload_model(ctx, ds, model, true, true, nullptr, &md, true))) return rc;
     if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
-    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, museconditionals != nullptr)))
-        return rc;
     void *p, *pu;
     const size_t LL = (size_t)ds->L * ds->L;
     if ((rc = ensure(ctx, kSlotDense, LL * sizeof(double), &p))) return rc;
     double* d_dense = (double*)p;
     double* d_u = nullptr;
-    if (md.cat.lamF) {  // unpaired columns for the factorised lambda categories
+    if (md.cat.lamF) {  // unpaired columns for the factorised lambda categories, under the pruning
         if ((rc = ensure(ctx, kSlotVec, (size_t)ds->L * sizeof(double), &pu))) return rc;
         d_u = (double*)pu;
+        if ((rc = fork_side(ctx))) return rc;
+        SideLaunches side(ctx);
         if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, d_u, nullptr)))
             return rc;
     }
+    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, museconditionals != nullptr)))
+        return rc;
+    if (md.cat.lamF && (rc = join_side(ctx))) return rc;
     if ((rc = launch_scatter_dense(ctx, ds, ds->d_mix, d_u, md.cat.logwF, d_dense))) return rc;
     if ((rc = d2h(ctx, pairedlogprobs, d_dense, LL * sizeof(double)))) return rc;
     if (museconditionals) {
