@@ -561,12 +561,139 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
     }
 }
 
-// All band diagonals of the outside pass, descending spans.
+// Outside cell (i, j = i+d) in two parts, as the inside cells: the parent
+// sums run over q of OS/OF(i, j+1+q) * S(j+1, j+1+q) (L) and of
+// OS/OF(i-1-q, j) * L(i-1-q, i-1) (S), spans d+1+q.  outside_cell_partial
+// sums q >= 1 (spans >= d+2), the suffix-column terms and the F value (span
+// d+2) and reduces them over the group; outside_cell_finish adds the q = 0
+// terms, which read the diagonal d+1 finished just before, and writes the
+// cell (lane 0).
+struct OutPartial {
+    float mL, sL, mS, sS, oF;
+};
+
+__device__ __forceinline__ OutPartial outside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G,
+                                                           const Rules& R)
+{
+    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    const int j = i + d;
+    OutPartial c{-INFINITY, 0.f, -INFINITY, 0.f, -INFINITY};
+    if (valid) {
+        const int nL = min(i + Wb, L - 1) - j;
+        const float* osr = t.OSrow + (size_t)i * RS + d + 1;
+        const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
+        if (j + 1 <= L - 1) {
+            const float* srw = t.Srow + (size_t)(j + 1) * RS;
+            int q = 1 + lane;
+            for (; q + 3 * G < nL; q += 4 * G) {
+                float x[8];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const float sib = srw[q + u * G];
+                    x[2 * u] = R.r[0] + __ldcg(osr + q + u * G) + sib;
+                    x[2 * u + 1] = R.r[4] + __ldcg(ofr + q + u * G) + sib;
+                }
+                lse_add8(c.mL, c.sL, x);
+            }
+            for (; q + G < nL; q += 2 * G) {
+                const float sib0 = srw[q], sib1 = srw[q + G];
+                lse_add4(c.mL, c.sL, R.r[0] + __ldcg(osr + q) + sib0, R.r[4] + __ldcg(ofr + q) + sib0,
+                         R.r[0] + __ldcg(osr + q + G) + sib1, R.r[4] + __ldcg(ofr + q + G) + sib1);
+            }
+            for (; q < nL; q += G) {
+                const float sib = srw[q];
+                lse_add(c.mL, c.sL, R.r[0] + __ldcg(osr + q) + sib);
+                lse_add(c.mL, c.sL, R.r[4] + __ldcg(ofr + q) + sib);
+            }
+            if (lane == 0 && L - 1 > i + Wb) lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
+        }
+        if (i >= 1) {
+            const int ip0 = max(0, j - Wb);
+            const int nS = i - ip0;
+            const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
+            const float* osc = t.OScol + (size_t)j * RS + d + 1;
+            const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
+            int q = 1 + lane;
+            for (; q + 3 * G < nS; q += 4 * G) {
+                float x[8];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const float lft = lcol[q + u * G];
+                    x[2 * u] = R.r[0] + __ldcg(osc + q + u * G) + lft;
+                    x[2 * u + 1] = R.r[4] + __ldcg(ofc + q + u * G) + lft;
+                }
+                lse_add8(c.mS, c.sS, x);
+            }
+            for (; q + G < nS; q += 2 * G) {
+                const float l0 = lcol[q], l1 = lcol[q + G];
+                lse_add4(c.mS, c.sS, R.r[0] + __ldcg(osc + q) + l0, R.r[4] + __ldcg(ofc + q) + l0,
+                         R.r[0] + __ldcg(osc + q + G) + l1, R.r[4] + __ldcg(ofc + q + G) + l1);
+            }
+            for (; q < nS; q += G) {
+                const float lft = lcol[q];
+                lse_add(c.mS, c.sS, R.r[0] + __ldcg(osc + q) + lft);
+                lse_add(c.mS, c.sS, R.r[4] + __ldcg(ofc + q) + lft);
+            }
+            if (j == L - 1) {
+                const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
+                for (int ip = a + lane; ip <= bnd; ip += G) lse_add(c.mS, c.sS, R.r[0] + __ldcg(t.Osuf + ip) + lcol[i - 1 - ip]);
+            }
+        }
+        if (lane == 0 && i >= 1 && j <= L - 2 && d + 2 <= Wb) {
+            const size_t pr = (size_t)(i - 1) * RS + d + 2;
+            const float pp = t.pb[pr];
+            if (pp != -INFINITY) {
+                float m = -INFINITY, s = 0.f;
+                lse_add(m, s, R.r[2] + pp + __ldcg(t.OSrow + pr));
+                lse_add(m, s, R.r[3] + pp + __ldcg(t.OFrow + pr));
+                lse_add(m, s, R.r[6] + pp + __ldcg(t.OLrow + pr));
+                c.oF = lse_val(m, s);
+            }
+        }
+    }
+    group_reduce_rt(c.mL, c.sL, G);
+    group_reduce_rt(c.mS, c.sS, G);
+    return c;
+}
+
+__device__ __forceinline__ void outside_cell_finish(const Band& t, int i, int d, bool valid, int lane, OutPartial c,
+                                                    const Rules& R)
+{
+    if (!(valid && lane == 0)) return;
+    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    const int j = i + d;
+    if (min(i + Wb, L - 1) - j >= 1) {  // q = 0 of the L sum: OS/OF(i, j+1) * S(j+1, j+1)
+        const float sib = t.Srow[(size_t)(j + 1) * RS];
+        const size_t o = (size_t)i * RS + d + 1;
+        lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.OSrow + o) + sib);
+        lse_add(c.mL, c.sL, R.r[4] + __ldcg(t.OFrow + o) + sib);
+    }
+    if (i >= 1 && i - max(0, j - Wb) >= 1) {  // q = 0 of the S sum: OS/OF(i-1, j) * L(i-1, i-1)
+        const float lft = t.Lcol[(size_t)(i - 1) * RS];
+        const size_t o = (size_t)j * RS + d + 1;
+        lse_add(c.mS, c.sS, R.r[0] + __ldcg(t.OScol + o) + lft);
+        lse_add(c.mS, c.sS, R.r[4] + __ldcg(t.OFcol + o) + lft);
+    }
+    const float oL = lse_val(c.mL, c.sL);
+    float oS = lse_val(c.mS, c.sS);
+    if (i == 0 && j == L - 1) oS = 0.f;
+    t.OSrow[(size_t)i * RS + d] = oS;
+    t.OScol[(size_t)j * RS + d] = oS;
+    t.OFrow[(size_t)i * RS + d] = c.oF;
+    t.OFcol[(size_t)j * RS + d] = c.oF;
+    t.OLrow[(size_t)i * RS + d] = oL;
+    if (j == L - 1) t.Osuf[i] = oS;
+}
+
+// All band diagonals of the outside pass, descending spans; the partial sums
+// of a CTA's first cells of diagonal d are computed between its arrival at
+// the barrier of diagonal d+1 and its wait there.
 template <int MODE>
 __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, Rules R)
 {
     unsigned int gen = 0;
-    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    const int L = t.L, Wb = t.Wb;
+    wave_arrive<MODE>(t.sync);  // the suffix column was written by the previous launch
     for (int d = Wb; d >= 0; d--) {
         const int G = group_width(2 * (Wb - d) + 2);
         const int gpb = blockDim.x / G;
@@ -574,101 +701,17 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
         const int lane = threadIdx.x & (G - 1);
         const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
         const int ncell = L - d;
-        for (int base = 0; base < ncell; base += total) {
+        const OutPartial c = outside_cell_partial(t, gid0, d, gid0 < ncell, lane, G, R);
+        if (!wave_wait<MODE>(t.sync, gen)) return;
+        outside_cell_finish(t, gid0, d, gid0 < ncell, lane, c, R);
+        for (int base = total; base < ncell; base += total) {
             const int i = base + gid0;
             const bool valid = i < ncell;
-            const int j = i + d;
-            float mL = -INFINITY, sL = 0.f, mS = -INFINITY, sS = 0.f;
-            if (valid) {
-                const int nL = min(i + Wb, L - 1) - j;
-                const float* osr = t.OSrow + (size_t)i * RS + d + 1;
-                const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
-                if (j + 1 <= L - 1) {
-                    const float* srw = t.Srow + (size_t)(j + 1) * RS;
-                    int q = lane;
-                    for (; q + 3 * G < nL; q += 4 * G) {
-                        float x[8];
-#pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            const float sib = srw[q + u * G];
-                            x[2 * u] = R.r[0] + __ldcg(osr + q + u * G) + sib;
-                            x[2 * u + 1] = R.r[4] + __ldcg(ofr + q + u * G) + sib;
-                        }
-                        lse_add8(mL, sL, x);
-                    }
-                    for (; q + G < nL; q += 2 * G) {
-                        const float sib0 = srw[q], sib1 = srw[q + G];
-                        lse_add4(mL, sL, R.r[0] + __ldcg(osr + q) + sib0, R.r[4] + __ldcg(ofr + q) + sib0,
-                                 R.r[0] + __ldcg(osr + q + G) + sib1, R.r[4] + __ldcg(ofr + q + G) + sib1);
-                    }
-                    for (; q < nL; q += G) {
-                        const float sib = srw[q];
-                        lse_add(mL, sL, R.r[0] + __ldcg(osr + q) + sib);
-                        lse_add(mL, sL, R.r[4] + __ldcg(ofr + q) + sib);
-                    }
-                    if (lane == 0 && L - 1 > i + Wb) lse_add(mL, sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
-                }
-                if (i >= 1) {
-                    const int ip0 = max(0, j - Wb);
-                    const int nS = i - ip0;
-                    const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
-                    const float* osc = t.OScol + (size_t)j * RS + d + 1;
-                    const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
-                    int q = lane;
-                    for (; q + 3 * G < nS; q += 4 * G) {
-                        float x[8];
-#pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            const float lft = lcol[q + u * G];
-                            x[2 * u] = R.r[0] + __ldcg(osc + q + u * G) + lft;
-                            x[2 * u + 1] = R.r[4] + __ldcg(ofc + q + u * G) + lft;
-                        }
-                        lse_add8(mS, sS, x);
-                    }
-                    for (; q + G < nS; q += 2 * G) {
-                        const float l0 = lcol[q], l1 = lcol[q + G];
-                        lse_add4(mS, sS, R.r[0] + __ldcg(osc + q) + l0, R.r[4] + __ldcg(ofc + q) + l0,
-                                 R.r[0] + __ldcg(osc + q + G) + l1, R.r[4] + __ldcg(ofc + q + G) + l1);
-                    }
-                    for (; q < nS; q += G) {
-                        const float lft = lcol[q];
-                        lse_add(mS, sS, R.r[0] + __ldcg(osc + q) + lft);
-                        lse_add(mS, sS, R.r[4] + __ldcg(ofc + q) + lft);
-                    }
-                    if (j == L - 1) {
-                        const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
-                        for (int ip = a + lane; ip <= bnd; ip += G) lse_add(mS, sS, R.r[0] + __ldcg(t.Osuf + ip) + lcol[i - 1 - ip]);
-                    }
-                }
-            }
-            group_reduce_rt(mL, sL, G);
-            group_reduce_rt(mS, sS, G);
-            if (valid && lane == 0) {
-                const float oL = lse_val(mL, sL);
-                float oS = lse_val(mS, sS);
-                if (i == 0 && j == L - 1) oS = 0.f;
-                float oF = -INFINITY;
-                if (i >= 1 && j <= L - 2 && d + 2 <= Wb) {
-                    const size_t pr = (size_t)(i - 1) * RS + d + 2;
-                    const float pp = t.pb[pr];
-                    if (pp != -INFINITY) {
-                        float m = -INFINITY, s = 0.f;
-                        lse_add(m, s, R.r[2] + pp + __ldcg(t.OSrow + pr));
-                        lse_add(m, s, R.r[3] + pp + __ldcg(t.OFrow + pr));
-                        lse_add(m, s, R.r[6] + pp + __ldcg(t.OLrow + pr));
-                        oF = lse_val(m, s);
-                    }
-                }
-                t.OSrow[(size_t)i * RS + d] = oS;
-                t.OScol[(size_t)j * RS + d] = oS;
-                t.OFrow[(size_t)i * RS + d] = oF;
-                t.OFcol[(size_t)j * RS + d] = oF;
-                t.OLrow[(size_t)i * RS + d] = oL;
-                if (j == L - 1) t.Osuf[i] = oS;
-            }
+            outside_cell_finish(t, i, d, valid, lane, outside_cell_partial(t, i, d, valid, lane, G, R), R);
         }
-        if (!wave_sync<MODE>(t.sync, gen)) return;
+        wave_arrive<MODE>(t.sync);
     }
+    if (MODE == kCluster) wave_wait<MODE>(t.sync, gen);
 }
 
 // CTA size of a persistent wavefront launch.  The split sums are bound by
