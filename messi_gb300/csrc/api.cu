@@ -221,10 +221,6 @@ int d2h(messi_ctx* ctx, void* dst, const void* src, size_t bytes)
     return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "device to host copy");
 }
 
-// Work on the side stream: fork() makes the side stream wait for everything
-// queued on the main stream so far; while a SideLaunches is alive the launch
-// helpers (which use ctx->stream) queue on the side stream; join() makes the
-// main stream wait for the side stream's work.
 int fork_side(messi_ctx* ctx)
 {
     cudaError_t e = cudaEventRecord(ctx->fork_ev, ctx->stream);
@@ -238,13 +234,6 @@ int join_side(messi_ctx* ctx)
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0);
     return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "side stream join");
 }
-
-struct SideLaunches {
-    messi_ctx* ctx;
-    cudaStream_t main;
-    explicit SideLaunches(messi_ctx* c) : ctx(c), main(c->stream) { ctx->stream = ctx->side; }
-    ~SideLaunches() { ctx->stream = main; }
-};
 
 // Upload a dense L x L pair matrix, pick the band width, prepare the band.
 int dense_pairs_to_band(messi_ctx* ctx, int L, const double* unpaired, const double* paired, int maxspan,

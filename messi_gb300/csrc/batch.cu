@@ -356,6 +356,26 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
         return rc;
     if ((rc = prepare_batch_arena(ctx, b, C))) return rc;
     if ((rc = write_descriptors(ctx, b, grp))) return rc;
+    // unpaired columns (one scratch buffer, sized for the largest alignment
+    // and reused in stream order) and baselines do not need the pairs: they
+    // run on the side stream under the pruning
+    {
+        size_t scratch = 0;
+        for (int a = 0; a < n; a++)
+            scratch = std::max(scratch, (size_t)nsite * ((size_t)b->ds[a]->numnodes * b->ds[a]->L * 5 + b->ds[a]->L));
+        void* ps;
+        if ((rc = ensure(ctx, 20, scratch * sizeof(double), &ps))) return rc;
+        if ((rc = fork_side(ctx))) return rc;
+        SideLaunches side(ctx);
+        for (int a = 0; a < n; a++) {
+            const Band& t = b->bands.host[b->bands.slot[a]];
+            if ((rc = launch_unpaired(ctx, b->ds[a], (const double*)p4 + (size_t)b->node_base[a] * 16,
+                                      b->total_nodes, d_pi4 + 4 * grp[a], d_lws + (size_t)nsite * grp[a], nsite,
+                                      t.u, (double*)ps)))
+                return rc;
+        }
+        if ((rc = launch_baseline_batch(ctx, b->bands, 1.0))) return rc;
+    }
     // pair pruning over the merged levels
     for (int c0 = 0; c0 < C; c0 += b->chunk) {
         const int nc = std::min(b->chunk, C - c0);
@@ -380,15 +400,8 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
             }
         }
     }
-    // unpaired columns (one scratch buffer, reused in stream order), baselines,
     // banded pair scores, batched inside
-    for (int a = 0; a < n; a++) {
-        const Band& t = b->bands.host[b->bands.slot[a]];
-        if ((rc = launch_unpaired(ctx, b->ds[a], (const double*)p4 + (size_t)b->node_base[a] * 16, b->total_nodes,
-                                  d_pi4 + 4 * grp[a], d_lws + (size_t)nsite * grp[a], nsite, t.u, nullptr)))
-            return rc;
-    }
-    if ((rc = launch_baseline_batch(ctx, b->bands, 1.0))) return rc;
+    if ((rc = join_side(ctx))) return rc;
     for (int a = 0; a < n; a++) {
         const Band& t = b->bands.host[b->bands.slot[a]];
         if ((rc = launch_bandprep_from_mix(ctx, b->ds[a], t, d_gap ? d_gap + b->col_base[a] : nullptr, 1.0,

@@ -276,6 +276,20 @@ int launch_siterate_conditionals(messi_ctx* ctx, messi_dataset* ds, const double
 // 0-based partner of column c (or -1), logwF the factorised lambda weight.
 int launch_structure_sum(messi_ctx* ctx, int L, double* d_u, const int* d_colu, const int* d_partner,
                          const double* d_mix, double logwF, double* d_total, double* d_pairll);
+// Work on the context's side stream (api.cu): fork_side makes the side
+// stream wait for everything queued on the main stream so far; while a
+// SideLaunches is alive the launch helpers (which use ctx->stream) queue on
+// the side stream; join_side makes the main stream wait for the side
+// stream's work.
+int fork_side(messi_ctx* ctx);
+int join_side(messi_ctx* ctx);
+struct SideLaunches {
+    messi_ctx* ctx;
+    cudaStream_t main;
+    explicit SideLaunches(messi_ctx* c) : ctx(c), main(c->stream) { ctx->stream = ctx->side; }
+    ~SideLaunches() { ctx->stream = main; }
+};
+
 // Bounded-wait self-test (scfg.cu): a two-CTA grid barrier that one CTA never
 // reaches; d_sync[2] becomes 1 when the other CTA's wait gives up.
 int launch_barrier_selftest(messi_ctx* ctx, unsigned int* d_sync);
