@@ -348,7 +348,7 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
         return fail(ctx, MESSI_ENOMEM, "batch transition matrices");
     if (grow(b->P4, (size_t)nsite * b->total_nodes * 16 * sizeof(double), &p4))
         return fail(ctx, MESSI_ENOMEM, "batch unpaired transition matrices");
-    const float* d_PT = (const float*)pt;
+    const float* d_P = (const float*)pt;
     if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, d_grp, b->total_nodes, C, (float*)pt)))
         return rc;
     if ((rc = launch_build_P4(ctx, (const double*)(base + o_eig4), d_bl, d_grp, b->total_nodes, nsite,
@@ -393,7 +393,7 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
                     }
                     prof_begin(ctx, 0, units);
                 }
-                if ((rc = launch_prune_tiles(ctx, b->d_nodes, tl, nt, root != 0, d_PT, b->total_nodes, c0, nc, C,
+                if ((rc = launch_prune_tiles(ctx, b->d_nodes, tl, nt, root != 0, d_P, b->total_nodes, c0, nc, C,
                                              d_pi16, d_logw, d_lam, false)))
                     return rc;
                 prof_end(ctx);

@@ -256,7 +256,7 @@ int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, co
                     int nsite, double* d_P4);
 // The tensor-core node update over `nt` tiles of one level (root tiles when root).
 int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
-                       const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
+                       const float* d_P, int numnodes, int c0, int nc, int C, const float* d_pi16,
                        const double* d_logw, const int* d_lam, bool per_lambda);
 int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* d_pi16, const double* d_logw,
               const int* d_lam, int C, int nlam, bool per_lambda);

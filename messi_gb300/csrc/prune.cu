@@ -230,7 +230,7 @@ struct WarpStage {
 
 template <bool ROOT, int STAGES, int MINB>
 __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
-    const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ PT, int numnodes,
+    const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ P, int numnodes,
     int c0, int nc, int C, const float* __restrict__ pi16, const double* __restrict__ logw,
     const int* __restrict__ lam, int per_lambda)
 {
@@ -297,8 +297,8 @@ __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
             XR[k] = st.x[4 + k][lane];
         }
         const int e = (le ? st.e[0][lane] : 0) + (re ? st.e[1][lane] : 0);
-        const float* ptl = PT + ((size_t)(c0 + cc) * numnodes + nd.left) * 256;
-        const float* ptr = PT + ((size_t)(c0 + cc) * numnodes + nd.right) * 256;
+        const float* ptl = P + ((size_t)(c0 + cc) * numnodes + nd.left) * 256;
+        const float* ptr = P + ((size_t)(c0 + cc) * numnodes + nd.right) * 256;
         float4 Bh[2], Bl[2];
         float DL[2][2][4], DR[2][2][4];
 #pragma unroll
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
 
 template <int STAGES, int MINB>
 static int launch_prune_shape(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
-                              const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
+                              const float* d_P, int numnodes, int c0, int nc, int C, const float* d_pi16,
                               const double* d_logw, const int* d_lam, bool per_lambda)
 {
     static thread_local int smem_set_device = -1;
@@ -414,30 +414,29 @@ static int launch_prune_shape(messi_ctx* ctx, const NodeDev* d_nodes, const int2
     }
     if (root) {
         prune_mma_kernel<true, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
-            d_nodes, d_tiles, d_PT, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
+            d_nodes, d_tiles, d_P, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
         LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
     } else {
         prune_mma_kernel<false, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
-            d_nodes, d_tiles, d_PT, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
+            d_nodes, d_tiles, d_P, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
         LAUNCH_CHECK(ctx, "prune_mma_kernel");
     }
     return MESSI_OK;
 }
 
 int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
-                       const float* d_PT, int numnodes, int c0, int nc, int C, const float* d_pi16,
+                       const float* d_P, int numnodes, int c0, int nc, int C, const float* d_pi16,
                        const double* d_logw, const int* d_lam, bool per_lambda)
 {
     if (nt <= 0) return MESSI_OK;
-    // measured on GB300: 2 stages x 3 CTAs is 2-5% faster (c4, c2)
     // MESSI_PRUNE_SHAPE=1 / 2: 3 stages x 3 CTAs, 2 stages x 3 CTAs (measured
     // 6% and 5% slower on c2 and c4)
     switch (ctx->prune_shape) {
-        case 1: return launch_prune_shape<3, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16,
+        case 1: return launch_prune_shape<3, 3>(ctx, d_nodes, d_tiles, nt, root, d_P, numnodes, c0, nc, C, d_pi16,
                                                 d_logw, d_lam, per_lambda);
-        case 2: return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16,
+        case 2: return launch_prune_shape<2, 3>(ctx, d_nodes, d_tiles, nt, root, d_P, numnodes, c0, nc, C, d_pi16,
                                                 d_logw, d_lam, per_lambda);
-        default: return launch_prune_shape<2, 4>(ctx, d_nodes, d_tiles, nt, root, d_PT, numnodes, c0, nc, C, d_pi16,
+        default: return launch_prune_shape<2, 4>(ctx, d_nodes, d_tiles, nt, root, d_P, numnodes, c0, nc, C, d_pi16,
                                                  d_logw, d_lam, per_lambda);
     }
 }
@@ -447,7 +446,6 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
 {
     (void)nlam;
     const int chunk = ds->chunk;
-    const float* d_PT = d_P;
     for (int c0 = 0; c0 < C; c0 += chunk) {
         const int nc = std::min(chunk, C - c0);
         for (int lv = 1; lv <= ds->H; lv++) {
@@ -458,7 +456,7 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
                 for (int v : ds->level_nodes[lv]) units += (double)ds->nunique[v] * nc;
                 prof_begin(ctx, 0, units);
             }
-            int rc = launch_prune_tiles(ctx, ds->d_nodes, ds->d_tiles + ds->tile_off[lv], nt, lv == ds->H, d_PT,
+            int rc = launch_prune_tiles(ctx, ds->d_nodes, ds->d_tiles + ds->tile_off[lv], nt, lv == ds->H, d_P,
                                         ds->numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda);
             if (rc) return rc;
             prof_end(ctx);
