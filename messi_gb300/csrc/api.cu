@@ -327,8 +327,6 @@ int messi_ctx_create(int device, messi_ctx** out)
             const int v = std::atoi(ps);
             ctx->prune_shape = (v >= 0 && v <= 2) ? v : 0;
         }
-        const char* wm = std::getenv("MESSI_WAVE_MODE");
-        if (wm) ctx->wave_mode = std::strcmp(wm, "grid") == 0 ? 1 : (std::strcmp(wm, "cluster") == 0 ? 2 : 0);
     }
     *out = ctx;
     return MESSI_OK;

@@ -139,12 +139,9 @@ struct messi_ctx {
     // sequences) and their size (256, 512 or 1024 threads; 0 = by band size)
     int wave_ctas = 0;
     int wave_threads = 0;
-    // 0 = choose per pass, 1 = grid barrier, 2 = one thread-block cluster
-    int wave_mode = 0;
     // pair node-update pipeline (128-pair tiles): 0 = 2 stages x 4 CTAs/SM,
     // 1 = 3 stages x 3 CTAs/SM, 2 = 2 stages x 3 CTAs/SM
     int prune_shape = 0;
-    std::vector<std::pair<const void*, int>> cluster_sizes;  // kernel -> cluster size (0: none)
     // per-kernel event timing (messi_ctx_profile)
     bool profiling = false;
     std::vector<messi::ProfRec> prof_pending;

@@ -466,13 +466,12 @@ __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool va
 // diagonal d-1 and its wait there, so the barrier latency overlaps that work;
 // after the wait the cells are finished, and any further cells of d (more
 // cells than groups) are computed whole.
-template <int MODE>
 __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
     unsigned int gen = 0;
     const int L = t.L;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
-    wave_arrive<MODE>(t.sync);
+    grid_arrive(t.sync);
     for (int d = 1; d <= t.Wb; d++) {
         const int G = group_width(d);
         const int gpb = blockDim.x / G;
@@ -481,16 +480,14 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
         const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
         const int ncell = L - d;
         const CellPartial c = inside_cell_partial(t, gid0, d, gid0 < ncell, lane, G);
-        if (!wave_wait<MODE>(t.sync, gen)) return;
+        if (!grid_wait(t.sync, gen)) return;
         inside_cell_finish(t, gid0, d, gid0 < ncell, lane, c, R);
         for (int base = total; base < ncell; base += total) {
             const int i = base + gid0;
             inside_cell(t, i, d, i < ncell, lane, G, R);
         }
-        wave_arrive<MODE>(t.sync);
+        grid_arrive(t.sync);
     }
-    // a cluster barrier's arrival is completed by a wait before the CTA exits
-    if (MODE == kCluster) wave_wait<MODE>(t.sync, gen);
 }
 
 // Batched inside over n alignments in one persistent launch: diagonal d of
@@ -688,12 +685,11 @@ __device__ __forceinline__ void outside_cell_finish(const Band& t, int i, int d,
 // All band diagonals of the outside pass, descending spans; the partial sums
 // of a CTA's first cells of diagonal d are computed between its arrival at
 // the barrier of diagonal d+1 and its wait there.
-template <int MODE>
 __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, Rules R)
 {
     unsigned int gen = 0;
     const int L = t.L, Wb = t.Wb;
-    wave_arrive<MODE>(t.sync);  // the suffix column was written by the previous launch
+    grid_arrive(t.sync);  // the suffix column was written by the previous launch
     for (int d = Wb; d >= 0; d--) {
         const int G = group_width(2 * (Wb - d) + 2);
         const int gpb = blockDim.x / G;
@@ -702,16 +698,15 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
         const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
         const int ncell = L - d;
         const OutPartial c = outside_cell_partial(t, gid0, d, gid0 < ncell, lane, G, R);
-        if (!wave_wait<MODE>(t.sync, gen)) return;
+        if (!grid_wait(t.sync, gen)) return;
         outside_cell_finish(t, gid0, d, gid0 < ncell, lane, c, R);
         for (int base = total; base < ncell; base += total) {
             const int i = base + gid0;
             const bool valid = i < ncell;
             outside_cell_finish(t, i, d, valid, lane, outside_cell_partial(t, i, d, valid, lane, G, R), R);
         }
-        wave_arrive<MODE>(t.sync);
+        grid_arrive(t.sync);
     }
-    if (MODE == kCluster) wave_wait<MODE>(t.sync, gen);
 }
 
 // CTA size of a persistent wavefront launch.  The split sums are bound by
@@ -744,86 +739,18 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
     return grid;
 }
 
-// Cluster mode (MESSI_WAVE_MODE=cluster): one thread-block cluster runs the
-// whole wavefront and synchronises with the hardware cluster barrier.
-// Returns the cluster size to use, 0 for grid mode.
-static int probe_cluster_size(const void* kernel, int threads)
+// Launch a persistent wavefront kernel (cooperative: every CTA resident).
+static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
+                       double band_cells, const char* what)
 {
-    for (int cl : {16, 8}) {
-        if (cl > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(cl);
-        cfg.blockDim = dim3(threads);
-        cudaLaunchAttribute at;
-        at.id = cudaLaunchAttributeClusterDimension;
-        at.val.clusterDim.x = cl;
-        at.val.clusterDim.y = 1;
-        at.val.clusterDim.z = 1;
-        cfg.attrs = &at;
-        cfg.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, kernel, &cfg) == cudaSuccess && nclusters >= 1) return cl;
-        cudaGetLastError();
-    }
-    return 0;
-}
-
-static int wave_cluster_size(messi_ctx* ctx, const void* kernel, int threads, double terms_per_diag)
-{
-    // measured on GB300: the grid barrier is as fast as the cluster barrier for
-    // these passes (the per-diagonal cost is the L2 latency chain of the split
-    // sums) and the grid has 10x the SMs, so the cluster build runs only on request
-    (void)terms_per_diag;
-    if (ctx->wave_mode != 2) return 0;
-    // the largest cluster the device runs for this kernel, found once per context
-    for (const auto& kv : ctx->cluster_sizes)
-        if (kv.first == kernel) return kv.second;
-    const int cl = probe_cluster_size(kernel, threads);
-    ctx->cluster_sizes.push_back({kernel, cl});
-    return cl;
-}
-
-// Launch a wavefront kernel pair (grid-barrier and cluster-barrier builds).
-static int launch_wave2(messi_ctx* ctx, const void* grid_kernel, const void* cluster_kernel, void** args,
-                        unsigned int* sync, int L, double band_cells, double terms_per_diag, const char* what)
-{
-    int threads = wave_threads(ctx, band_cells);
-    const int cl = wave_cluster_size(ctx, cluster_kernel, kWaveMaxThreads, terms_per_diag);
+    const int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    if (cl > 0) {
-        threads = kWaveMaxThreads;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(cl);
-        cfg.blockDim = dim3(threads);
-        cfg.stream = ctx->stream;
-        cudaLaunchAttribute at;
-        at.id = cudaLaunchAttributeClusterDimension;
-        at.val.clusterDim.x = cl;
-        at.val.clusterDim.y = 1;
-        at.val.clusterDim.z = 1;
-        cfg.attrs = &at;
-        cfg.numAttrs = 1;
-        e = cudaLaunchKernelExC(&cfg, cluster_kernel, args);
-    } else {
-        const int grid = wave_grid(ctx, grid_kernel, L, threads);
-        e = cudaLaunchCooperativeKernel(grid_kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
-    }
+    const int grid = wave_grid(ctx, kernel, L, threads);
+    e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, what);
     return MESSI_OK;
-}
-
-// split terms per diagonal of a band pass, averaged over its diagonals
-static double band_terms_per_diag(int L, int Wb)
-{
-    if (Wb < 1) return 0.0;
-    double terms = 0.0;
-    for (int d = 1; d <= Wb; d++) terms += (double)(L - d) * d;
-    return terms / Wb;
 }
 
 // Self-test of the bounded grid barrier: CTA 1 never arrives, so CTA 0's wait
@@ -860,8 +787,8 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     double Bv = B;
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc = launch_wave2(ctx, (const void*)inside_wave_kernel<kGrid>, (const void*)inside_wave_kernel<kCluster>, args,
-                          t.sync, t.L, (double)t.L * (t.Wb + 1), band_terms_per_diag(t.L, t.Wb), "inside_wave_kernel");
+    int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
+                         "inside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
@@ -1072,9 +999,8 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
     Band tt = t;
     void* args[] = {&tt, &R};
     prof_begin(ctx, 3, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    int rc = launch_wave2(ctx, (const void*)outside_wave_kernel<kGrid>, (const void*)outside_wave_kernel<kCluster>,
-                          args, t.sync, t.L, (double)t.L * (t.Wb + 1), 2.0 * band_terms_per_diag(t.L, t.Wb),
-                          "outside_wave_kernel");
+    int rc = launch_wave(ctx, (const void*)outside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
+                         "outside_wave_kernel");
     if (rc) return rc;
     prof_end(ctx);
     return queue_status_readback(ctx, t);

@@ -77,43 +77,6 @@ static __device__ bool grid_sync(unsigned int* sync, unsigned int& gen, unsigned
     return grid_wait(sync, gen, spin_limit);
 }
 
-// Synchronisation of the wavefront kernels.  kGrid: the bounded grid
-// barrier above (any grid of co-resident CTAs); kCluster: the hardware
-// barrier of one thread-block cluster (the whole launch is one cluster), a
-// release/acquire at cluster scope.  Cells written by other CTAs of the
-// cluster are read through L2 (__ldcg) as in grid mode.
-enum WaveSync { kGrid = 0, kCluster = 1 };
-
-template <int MODE>
-static __device__ __forceinline__ void wave_arrive(unsigned int* sync)
-{
-    if (MODE == kCluster) {
-        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-        return;
-    }
-    grid_arrive(sync);
-}
-
-template <int MODE>
-static __device__ __forceinline__ bool wave_wait(unsigned int* sync, unsigned int& gen)
-{
-    if (MODE == kCluster) {
-        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-        return true;
-    }
-    return grid_wait(sync, gen);
-}
-
-template <int MODE>
-static __device__ __forceinline__ bool wave_sync(unsigned int* sync, unsigned int& gen)
-{
-    if (MODE == kCluster) {
-        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-        return true;
-    }
-    return grid_sync(sync, gen);
-}
-
 // Lanes per cell for a split sum of `nterms` terms: at most 8 terms per lane
 // up to 256 terms, so a lane's loads are issued together and the sum costs
 // one L2 round trip; longer sums use the whole warp.
