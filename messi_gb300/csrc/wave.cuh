@@ -37,9 +37,9 @@ constexpr unsigned int kBarrierError = 1u << 30;
 // second CTA barrier orders the other CTAs' cells before the CTA's next
 // reads.  Cells written by other CTAs before the barrier are read with
 // __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
-// those tables.
-// The barrier in two halves, so that a CTA can work between its arrival and
-// its wait on cells that do not depend on the other CTAs' latest writes.
+// those tables.  The barrier comes in two halves (grid_arrive, grid_wait) so
+// that a CTA can work between its arrival and its wait on cells that do not
+// depend on the other CTAs' latest writes; grid_sync is both at once.
 static __device__ __forceinline__ void grid_arrive(unsigned int* sync)
 {
     __syncthreads();
