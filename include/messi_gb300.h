@@ -81,6 +81,11 @@ int messi_ctx_destroy(messi_ctx* ctx);
 int messi_ctx_stream(messi_ctx* ctx, void** stream);
 /* Number of kernel launches issued by the last call on this context. */
 int messi_ctx_last_launches(messi_ctx* ctx, int64_t* launches);
+/* Number of messi_likelihood calls on this context whose device work was a
+ * replay of a captured CUDA graph (captured on the second call with the same
+ * dataset, category layout and buffers; MESSI_GRAPHS=0 at context creation
+ * turns graphs off). */
+int messi_ctx_graph_replays(messi_ctx* ctx, int64_t* replays);
 /* Text of the last error recorded on this context. */
 const char* messi_ctx_last_error(messi_ctx* ctx);
 /* Self-test of the bounded device waits (no counterpart in the reference):

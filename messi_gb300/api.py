@@ -60,6 +60,12 @@ class Context:
         _lib.check(self.lib.messi_ctx_last_launches(self.handle, ctypes.byref(n)), "messi_ctx_last_launches")
         return n.value
 
+    def graph_replays(self):
+        """messi_likelihood calls whose device work replayed a captured CUDA graph."""
+        n = ctypes.c_int64()
+        self.check(self.lib.messi_ctx_graph_replays(self.handle, ctypes.byref(n)), "messi_ctx_graph_replays")
+        return n.value
+
     def selftest_bounded_wait(self):
         """Status produced by a device wait that cannot complete (a grid
         barrier one CTA never reaches): MESSI_ETIMEOUT when the bounded wait

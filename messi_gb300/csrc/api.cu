@@ -28,6 +28,7 @@ int ensure(messi_ctx* ctx, int slot, size_t bytes, void** p)
     DevBuf& b = ctx->scratch[slot];
     if (bytes == 0) bytes = 16;
     if (b.bytes < bytes) {
+        ctx->alloc_epoch++;
         if (b.p) cudaFree(b.p);
         b.p = nullptr;
         b.bytes = 0;
@@ -45,6 +46,7 @@ int ensure(messi_ctx* ctx, int slot, size_t bytes, void** p)
 int ensure_pinned(messi_ctx* ctx, size_t bytes, void** p)
 {
     if (ctx->pinned_bytes < bytes) {
+        ctx->alloc_epoch++;
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
         ctx->pinned = nullptr;
         ctx->pinned_bytes = 0;
@@ -119,14 +121,37 @@ struct ModelDev {
     double* pi4 = nullptr;
     double* logw_site = nullptr;
     uint8_t* gapmask = nullptr;
+    double* logwF = nullptr;  // device copy of cat.logwF
+    // staged copy (pinned -> device) and the transition-matrix builds, queued
+    // by enqueue_model (separately, so that a captured graph can replay them)
+    void* stage_host = nullptr;
+    void* stage_dev = nullptr;
+    size_t stage_bytes = 0;
+    const double *eig = nullptr, *eig4 = nullptr, *bl = nullptr;
+    bool pairs = false, unpaired = false;
 };
 
-// Builds categories on the host, uploads them in one copy and assembles the
-// transition matrices on the device.
+// Queues the staged model's copy to the device and the transition-matrix
+// builds on ctx->stream.
+int enqueue_model(messi_ctx* ctx, messi_dataset* ds, ModelDev* md)
+{
+    int rc;
+    cudaError_t e = cudaMemcpyAsync(md->stage_dev, md->stage_host, md->stage_bytes, cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "model upload");
+    if (md->pairs && (rc = launch_build_P16(ctx, md->eig, md->bl, nullptr, ds->numnodes, md->cat.C, md->P16)))
+        return rc;
+    if (md->unpaired && (rc = launch_build_P4(ctx, md->eig4, md->bl, nullptr, ds->numnodes, md->cat.nsite, md->P4)))
+        return rc;
+    return MESSI_OK;
+}
+
+// Builds categories on the host, stages them in pinned memory and (with
+// enqueue) queues their upload and the transition-matrix builds.
 // factorise: leave the lambda = 1 categories out of the 16-state pruning (the
 // caller then adds md->cat.logwF + u[x] + u[y] to every pair mixture).
 int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool pairs, bool unpaired,
-                 const uint8_t* gapmask, ModelDev* md, bool factorise = false)
+                 const uint8_t* gapmask, ModelDev* md, bool factorise = false, bool enqueue = true)
 {
     std::string err;
     int rc = build_categories(m, ds->numnodes, &md->cat, &err, pairs, factorise && pairs && unpaired);
@@ -141,36 +166,39 @@ int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool p
     size_t o_eig4 = st.add(c.eig4.data(), c.eig4.size());
     size_t o_pi4 = st.add(c.pi4, 4);
     size_t o_lws = st.add(c.logw_site.data(), c.logw_site.size());
+    size_t o_lwF = st.add(&c.logwF, 1);
     size_t o_gap = gapmask ? st.add(gapmask, (size_t)ds->L) : 0;
     void *pin, *dev;
     if ((rc = ensure_pinned(ctx, st.host.size(), &pin))) return rc;
     if ((rc = ensure(ctx, kSlotStage, st.host.size(), &dev))) return rc;
     std::memcpy(pin, st.host.data(), st.host.size());
-    cudaError_t e = cudaMemcpyAsync(dev, pin, st.host.size(), cudaMemcpyHostToDevice, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "model upload");
+    md->stage_host = pin;
+    md->stage_dev = dev;
+    md->stage_bytes = st.host.size();
+    md->pairs = pairs;
+    md->unpaired = unpaired;
     char* base = (char*)dev;
+    md->logwF = (double*)(base + o_lwF);
     md->pi16 = (float*)(base + o_pi16);
     md->logw = (double*)(base + o_logw);
     md->lam = (int*)(base + o_lam);
     md->pi4 = (double*)(base + o_pi4);
     md->logw_site = (double*)(base + o_lws);
     md->gapmask = gapmask ? (uint8_t*)(base + o_gap) : nullptr;
-    const double* d_bl = (const double*)(base + o_bl);
+    md->bl = (const double*)(base + o_bl);
+    md->eig = (const double*)(base + o_eig);
+    md->eig4 = (const double*)(base + o_eig4);
     if (pairs) {
         void* p;
         if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * sizeof(float), &p))) return rc;
         md->P16 = (float*)p;
-        if ((rc = launch_build_P16(ctx, (const double*)(base + o_eig), d_bl, nullptr, ds->numnodes, c.C, md->P16)))
-            return rc;
     }
     if (unpaired) {
         void* p;
         if ((rc = ensure(ctx, kSlotP4, (size_t)c.nsite * ds->numnodes * 16 * sizeof(double), &p))) return rc;
         md->P4 = (double*)p;
-        if ((rc = launch_build_P4(ctx, (const double*)(base + o_eig4), d_bl, nullptr, ds->numnodes, c.nsite, md->P4)))
-            return rc;
     }
-    return MESSI_OK;
+    return enqueue ? enqueue_model(ctx, ds, md) : MESSI_OK;
 }
 
 int prepare_arena(messi_ctx* ctx, messi_dataset* ds, int C)
@@ -233,6 +261,61 @@ int join_side(messi_ctx* ctx)
     cudaError_t e = cudaEventRecord(ctx->join_ev, ctx->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0);
     return (e == cudaSuccess) ? MESSI_OK : cuda_fail(ctx, e, "side stream join");
+}
+
+// Every device step of one likelihood evaluation after the host staging:
+// model upload and transition matrices, unpaired columns and baselines on the
+// side stream, pair pruning, banded pair scores, inside pass.
+int enqueue_likelihood(messi_ctx* ctx, messi_dataset* ds, ModelDev& md, const Band& t)
+{
+    int rc;
+    if ((rc = enqueue_model(ctx, ds, &md))) return rc;
+    // the unpaired columns and the baselines do not need the pairs: they run
+    // on the side stream under the pruning
+    if ((rc = fork_side(ctx))) return rc;
+    {
+        SideLaunches side(ctx);
+        if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, t.u, nullptr)))
+            return rc;
+        if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
+    }
+    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
+    if ((rc = join_side(ctx))) return rc;
+    if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0, md.cat.logwF, md.logwF))) return rc;
+    return run_inside(ctx, t, 1.0);
+}
+
+// Capture enqueue_likelihood into ctx->lgraph (key: what its pointers and
+// launch shapes depend on).  On any capture error graphs are switched off for
+// the context and the caller runs the steps eagerly.
+bool capture_likelihood(messi_ctx* ctx, messi_dataset* ds, ModelDev& md, const Band& t, const LikelihoodKey& key)
+{
+    if (ctx->lgraph.exec) {
+        cudaGraphExecDestroy(ctx->lgraph.exec);
+        ctx->lgraph.exec = nullptr;
+    }
+    const int64_t l0 = ctx->launches;
+    bool ok = false;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int rc = enqueue_likelihood(ctx, ds, md, t);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        cudaGraphExec_t ex = nullptr;
+        if (rc == MESSI_OK && e == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+            ctx->lgraph.exec = ex;
+            ctx->lgraph.key = key;
+            ctx->lgraph.launches = ctx->launches - l0;
+            ok = true;
+        }
+        if (g) cudaGraphDestroy(g);
+    }
+    if (!ok) {
+        cudaGetLastError();
+        ctx->graphs = false;
+        ctx->last_error.clear();
+    }
+    ctx->launches = l0;
+    return ok;
 }
 
 // Upload a dense L x L pair matrix, pick the band width, prepare the band.
@@ -322,6 +405,8 @@ int messi_ctx_create(int device, messi_ctx** out)
         if (w) ctx->wave_ctas = std::max(0, std::atoi(w));
         const char* wt = std::getenv("MESSI_WAVE_THREADS");
         if (wt) ctx->wave_threads = std::atoi(wt);
+        const char* gr = std::getenv("MESSI_GRAPHS");
+        if (gr && std::atoi(gr) == 0) ctx->graphs = false;
         const char* ps = std::getenv("MESSI_PRUNE_SHAPE");
         if (ps) {
             const int v = std::atoi(ps);
@@ -367,6 +452,7 @@ int messi_ctx_destroy(messi_ctx* ctx)
         if (b.p) cudaFree(b.p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->status_host) cudaFreeHost(ctx->status_host);
+    if (ctx->lgraph.exec) cudaGraphExecDestroy(ctx->lgraph.exec);
     cudaStreamSynchronize(ctx->side);
     cudaEventDestroy(ctx->fork_ev);
     cudaEventDestroy(ctx->join_ev);
@@ -380,6 +466,13 @@ int messi_ctx_stream(messi_ctx* ctx, void** stream)
 {
     if (!ctx || !stream) return MESSI_EINVAL;
     *stream = (void*)ctx->stream;
+    return MESSI_OK;
+}
+
+int messi_ctx_graph_replays(messi_ctx* ctx, int64_t* replays)
+{
+    if (!ctx || !replays) return MESSI_EINVAL;
+    *replays = ctx->graph_replays;
     return MESSI_OK;
 }
 
@@ -577,25 +670,38 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
         gm.resize(ds->L);
         for (int i = 0; i < ds->L; i++) gm[i] = (gapfrequency[i] >= gapcutoff) ? 1 : 0;
     }
+    // host staging and every allocation first; the device steps are then one
+    // replayable sequence (a CUDA graph from the second identical call on)
     ModelDev md;
-    if ((rc = upload_model(ctx, ds, model, true, true, gapfrequency ? gm.data() : nullptr, &md, true))) return rc;
+    if ((rc = upload_model(ctx, ds, model, true, true, gapfrequency ? gm.data() : nullptr, &md, true, false)))
+        return rc;
     if ((rc = prepare_arena(ctx, ds, md.cat.C))) return rc;
     Band t;
     const int Wb = std::max(0, std::min(ds->W, ds->L - 1));
     if ((rc = band_alloc(ctx, ds->L, Wb, false, &t))) return rc;
-    // the unpaired columns and the baselines do not need the pairs: they run
-    // on the side stream under the pruning
-    if ((rc = fork_side(ctx))) return rc;
-    {
-        SideLaunches side(ctx);
-        if ((rc = launch_unpaired(ctx, ds, md.P4, ds->numnodes, md.pi4, md.logw_site, md.cat.nsite, t.u, nullptr)))
-            return rc;
-        if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
+    LikelihoodKey key;
+    key.ds = ds;
+    key.C = md.cat.C;
+    key.nsite = md.cat.nsite;
+    key.nlam = md.cat.nlam;
+    key.Wb = Wb;
+    key.lamF = md.cat.lamF;
+    key.gapmask = gapfrequency != nullptr;
+    key.staged = md.stage_bytes;
+    key.epoch = ctx->alloc_epoch;
+    key.arena_gen = ds->arena_gen;
+    const bool graphs = ctx->graphs && !ctx->profiling;
+    bool replay = graphs && ctx->lgraph.exec && ctx->lgraph.key == key;
+    if (!replay && graphs && ctx->lgraph.seen == key) replay = capture_likelihood(ctx, ds, md, t, key);
+    if (replay) {
+        cudaError_t e = cudaGraphLaunch(ctx->lgraph.exec, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "likelihood graph launch");
+        ctx->launches += ctx->lgraph.launches;
+        ctx->graph_replays++;
+    } else {
+        if ((rc = enqueue_likelihood(ctx, ds, md, t))) return rc;
+        ctx->lgraph.seen = key;
     }
-    if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
-    if ((rc = join_side(ctx))) return rc;
-    if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0, md.cat.logwF))) return rc;
-    if ((rc = run_inside(ctx, t, 1.0))) return rc;
     if ((rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;
     if (unpaired && (rc = d2h(ctx, unpaired, t.u, (size_t)ds->L * sizeof(double)))) return rc;
     return finish(ctx);

@@ -133,6 +133,31 @@ struct ProfRec {
 constexpr int kProfKernels = 4;
 }  // namespace messi
 
+namespace messi {
+// What a captured likelihood launch sequence depends on besides the staged
+// model bytes: the dataset, the category layout, the gap mask's presence and
+// every device pointer (through the context's allocation epoch).
+struct LikelihoodKey {
+    const void* ds = nullptr;
+    int C = -1, nsite = -1, nlam = -1, Wb = -1;
+    uint32_t lamF = 0;
+    bool gapmask = false;
+    size_t staged = 0;
+    uint64_t epoch = 0, arena_gen = 0;
+    bool operator==(const LikelihoodKey& o) const
+    {
+        return ds == o.ds && C == o.C && nsite == o.nsite && nlam == o.nlam && Wb == o.Wb && lamF == o.lamF &&
+               gapmask == o.gapmask && staged == o.staged && epoch == o.epoch && arena_gen == o.arena_gen;
+    }
+};
+struct LikelihoodGraph {
+    cudaGraphExec_t exec = nullptr;
+    LikelihoodKey key;      // of exec
+    LikelihoodKey seen;     // of the last eager call (capture on the second identical call)
+    int64_t launches = 0;   // kernel launches in exec
+};
+}  // namespace messi
+
 struct messi_ctx {
     int device = 0;
     // CTAs of the persistent wavefront kernels (0 = one per SM, fewer for short
@@ -162,6 +187,13 @@ struct messi_ctx {
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
     unsigned int* status_host = nullptr;  // pinned word: wavefront barrier status of the last call
+    // device buffers are reallocated only when they grow; every reallocation
+    // bumps the epoch, so a captured launch sequence knows its pointers are stale
+    uint64_t alloc_epoch = 0;
+    // CUDA graph of messi_likelihood's device work (MESSI_GRAPHS=0 disables)
+    bool graphs = true;
+    messi::LikelihoodGraph lgraph;
+    int64_t graph_replays = 0;
 };
 
 struct messi_dataset {
@@ -177,6 +209,7 @@ struct messi_dataset {
     std::vector<int> tile_off, tile_cnt;        // per level: offset/count into d_tiles
     int chunk = 0;                     // categories per pass (0 = arena not allocated yet)
     int arena_C = 0;                   // category count the arena was laid out for
+    uint64_t arena_gen = 0;            // bumped whenever the arena and node descriptors are rewritten
     // device
     int* d_bandidx = nullptr;          // [L][W+1]
     int* d_lr = nullptr;               // concatenated li/ri arrays
@@ -295,9 +328,10 @@ int launch_barrier_selftest(messi_ctx* ctx, unsigned int* d_sync);
 int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals, const double* d_u, double addw,
                          double* d_out);
 // Banded pair scores from the root mixtures of ds, with the factorised term
-// logwF + u[i] + u[j] (u = t.u) when logwF is finite.
+// logwF + u[i] + u[j] (u = t.u) when logwF is finite; d_logwF (nullable)
+// holds logwF on the device instead.
 int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask,
-                             double B, double logwF);
+                             double B, double logwF, const double* d_logwF = nullptr);
 
 // ---- column patterns on the device (ingest.cu) ----
 // d_refs: [numnodes][L] first-column pattern ids; d_out_julia (nullable):

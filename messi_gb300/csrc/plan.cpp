@@ -417,6 +417,7 @@ int allocate_arena(messi_dataset* ds, int C, std::string* err)
         }
         ds->chunk = chunk;
     }
+    ds->arena_gen++;
     ds->nodes_host.assign(ds->numnodes, NodeDev{});
     fill_node_descriptors(ds, ds->d_arena_f, ds->d_arena_e, 0, ds->arena_rows, 0, 0, ds->nodes_host.data());
     const int nn = ds->numnodes;

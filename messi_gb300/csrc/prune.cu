@@ -603,14 +603,18 @@ int launch_scatter_dense(messi_ctx* ctx, messi_dataset* ds, const double* d_vals
 
 // Banded log-odds pair scores from the root mixtures (device-resident path),
 // with maskgapped! (src/RNATools.jl:441-451) folded in.
-// The factorised lambda categories add logwF + u[i] + u[j] to the mixture.
+// The factorised lambda categories add logwF + u[i] + u[j] to the mixture
+// (logwF read from d_logwF when given: a replayed graph then sees each call's
+// value).
 __global__ void bandprep_from_mix_kernel(const int* __restrict__ bandidx, const double* __restrict__ mix, int L, int W,
                                          int Wb, int RS, const uint8_t* __restrict__ gapmask,
-                                         const double* __restrict__ u, double logwF,
-                                         const double* __restrict__ b, double B, float* __restrict__ pb)
+                                         const double* __restrict__ u, double logwF_value,
+                                         const double* __restrict__ d_logwF, const double* __restrict__ b, double B,
+                                         float* __restrict__ pb)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)L * RS) return;
+    const double logwF = d_logwF ? *d_logwF : logwF_value;
     const int i = (int)(idx / RS), k = (int)(idx % RS);
     float out = -INFINITY;
     if (k >= 1 && k <= Wb && i + k < L && k <= W) {
@@ -625,12 +629,12 @@ __global__ void bandprep_from_mix_kernel(const int* __restrict__ bandidx, const 
 }
 
 int launch_bandprep_from_mix(messi_ctx* ctx, messi_dataset* ds, const Band& t, const uint8_t* d_gapmask, double B,
-                             double logwF)
+                             double logwF, const double* d_logwF)
 {
     const long long n = (long long)t.L * t.RS;
     const int bs = 256;
     bandprep_from_mix_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, ctx->stream>>>(
-        ds->d_bandidx, ds->d_mix, ds->L, ds->W, t.Wb, t.RS, d_gapmask, t.u, logwF, t.b, B, t.pb);
+        ds->d_bandidx, ds->d_mix, ds->L, ds->W, t.Wb, t.RS, d_gapmask, t.u, logwF, d_logwF, t.b, B, t.pb);
     LAUNCH_CHECK(ctx, "bandprep_from_mix_kernel");
     return MESSI_OK;
 }

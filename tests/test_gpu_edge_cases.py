@@ -137,3 +137,36 @@ def test_wavefront_results_repeat_bit_for_bit():
         post = api.computeposteriors(u, p)
         for a, b in zip(post, post0):
             np.testing.assert_array_equal(a, b)
+
+
+def test_likelihood_graph_replay_equals_eager(c1, monkeypatch):
+    """From the second identical call on, messi_likelihood replays a captured
+    CUDA graph of its device work; the staged model is rewritten each call,
+    so replays with new parameters must give exactly the eager results."""
+    from messi_gb300 import api
+    from messi_gb300 import model as M
+    ds = c1.dataset
+    rng = np.random.default_rng(5)
+    p15s = []
+    for _ in range(5):
+        p = c1.params15.copy()
+        p[0:3] *= np.exp(rng.normal(0, 0.1, 3))
+        p[14] = min(0.9, max(0.1, p[14] + rng.normal(0, 0.05)))  # lambda-zero weight: the factorised term
+        p15s.append(p)
+    ctx = api.Context(0)
+    try:
+        Zg = [api.computestructureintegratedlikelihood(ds, M.getparams(p, ds.branchlengths), c1.W, ctx=ctx)
+              for p in p15s]
+        replays = ctx.graph_replays()
+    finally:
+        ctx.close()
+    monkeypatch.setenv("MESSI_GRAPHS", "0")
+    ctx = api.Context(0)
+    try:
+        Ze = [api.computestructureintegratedlikelihood(ds, M.getparams(p, ds.branchlengths), c1.W, ctx=ctx)
+              for p in p15s]
+        assert ctx.graph_replays() == 0
+    finally:
+        ctx.close()
+    assert Zg == Ze
+    assert replays >= 3, replays
