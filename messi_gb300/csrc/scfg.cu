@@ -393,29 +393,30 @@ __device__ __forceinline__ void inside_init_cell(const Band& t, int i, const Rul
 
 // Cell (i, i+d) in two parts, by a group of G lanes (every lane of the warp
 // calls both, `valid` false for padding groups: the shuffles need the whole
-// warp).  The split sum runs over k = 0 .. d-1 of L(i, i+k) + S(i+k+1, j).
-// inside_cell_partial sums the split points k = 1 .. d-2, whose two cells
-// both have spans <= d-2, reduces them over the group and loads the pair
-// score and the enclosed F (span d-2); inside_cell_finish adds the two split
-// points that touch diagonal d-1 (k = 0 and k = d-1) and writes the cell
-// (lane 0).  Between the two a wavefront may wait for diagonal d-1.
+// warp).  The split sum runs over k = 0 .. d-1 of L(i, i+k) + S(i+k+1, j),
+// spans k and d-1-k.  The partial part sums the middle split points k =
+// NLO .. d-NHI-1 (both spans <= d-1-min(NLO, NHI)), reduces them over the
+// group and loads the pair score; the finishing part (lane 0) adds the
+// outer split points k < NLO and k >= d-NHI in ascending order, the enclosed
+// F (span d-2) and writes the cell.  Odd spans use NLO = NHI = 2, even spans
+// 3: the partial sums of a diagonal pair (2p-1, 2p) then read spans <= 2p-4
+// only, which the paired wavefront has before its wait, and every kernel
+// splits a cell the same way, so all of them give the same bits.
 struct CellPartial {
-    float m, s, pbv, fin;
+    float m, s, pbv;
 };
 
-__device__ __forceinline__ CellPartial inside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G)
+template <int NLO, int NHI>
+__device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int d, bool valid, int lane, int G)
 {
     const int RS = t.RS;
-    CellPartial c{-INFINITY, 0.f, -INFINITY, -INFINITY};
-    if (valid && lane == 0 && d >= 2) {
-        c.pbv = t.pb[(size_t)i * RS + d];
-        c.fin = __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2));
-    }
-    if (valid && d >= 3) {
+    CellPartial c{-INFINITY, 0.f, -INFINITY};
+    if (valid && lane == 0 && d >= 2) c.pbv = t.pb[(size_t)i * RS + d];
+    const int kend = d - NHI;
+    if (valid && kend > NLO) {
         const float* lrow = t.Lrow + (size_t)i * RS;
         const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
-        const int kend = d - 1;
-        int k = 1 + lane;
+        int k = NLO + lane;
         for (; k + 7 * G < kend; k += 8 * G) {
             float x[8];
 #pragma unroll
@@ -432,18 +433,32 @@ __device__ __forceinline__ CellPartial inside_cell_partial(const Band& t, int i,
     return c;
 }
 
-__device__ __forceinline__ void inside_cell_finish(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
-                                                   const Rules& R)
+template <int NLO, int NHI>
+__device__ __forceinline__ void cell_finish_t(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
+                                              const Rules& R)
 {
     if (!(valid && lane == 0)) return;
     const int RS = t.RS;
     const int j = i + d;
     const float* lrow = t.Lrow + (size_t)i * RS;
     const float* scol = t.Scol + (size_t)j * RS + (d - 1);
-    lse_add(c.m, c.s, __ldcg(lrow) + __ldcg(scol));  // k = 0
-    if (d >= 2) lse_add(c.m, c.s, __ldcg(lrow + d - 1) + __ldcg(scol - (d - 1)));  // k = d - 1
+    // outer split points k < NLO and k >= hb = max(NLO, d-NHI), loaded
+    // together and added in ascending k (an absent one is -inf, which
+    // lse_add skips exactly)
+    float xl[NLO], xh[NHI];
+#pragma unroll
+    for (int q = 0; q < NLO; q++) xl[q] = (q < d) ? __ldcg(lrow + q) + __ldcg(scol - q) : -INFINITY;
+    const int hb = max(NLO, d - NHI);
+#pragma unroll
+    for (int q = 0; q < NHI; q++)
+        xh[q] = (hb + q < d) ? __ldcg(lrow + hb + q) + __ldcg(scol - (hb + q)) : -INFINITY;
+    const float fin = (d >= 2) ? __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2)) : -INFINITY;
+#pragma unroll
+    for (int q = 0; q < NLO; q++) lse_add(c.m, c.s, xl[q]);
+#pragma unroll
+    for (int q = 0; q < NHI; q++) lse_add(c.m, c.s, xh[q]);
     const float tmp = lse_val(c.m, c.s);
-    const float v = c.pbv + c.fin;
+    const float v = c.pbv + fin;
     const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
     const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
     const float Lv = R.r[6] + v;
@@ -455,37 +470,84 @@ __device__ __forceinline__ void inside_cell_finish(const Band& t, int i, int d, 
     if (j == t.L - 1) t.Ssuf[i] = S;
 }
 
+__device__ __forceinline__ CellPartial inside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G)
+{
+    return (d & 1) ? cell_partial_t<2, 2>(t, i, d, valid, lane, G) : cell_partial_t<3, 3>(t, i, d, valid, lane, G);
+}
+
+__device__ __forceinline__ void inside_cell_finish(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
+                                                   const Rules& R)
+{
+    if (d & 1) cell_finish_t<2, 2>(t, i, d, valid, lane, c, R);
+    else cell_finish_t<3, 3>(t, i, d, valid, lane, c, R);
+}
+
 __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool valid, int lane, int G, const Rules& R)
 {
     inside_cell_finish(t, i, d, valid, lane, inside_cell_partial(t, i, d, valid, lane, G), R);
 }
 
-// All band diagonals of the inside pass (span 0 initialisation included).
-// Each diagonal d: the partial sums of the CTA's first cells of d (spans
-// <= d-2, complete) are computed between the CTA's arrival at the barrier of
-// diagonal d-1 and its wait there, so the barrier latency overlaps that work;
-// after the wait the cells are finished, and any further cells of d (more
-// cells than groups) are computed whole.
+// The cells of one diagonal that a CTA owns (rows [r0, end)), in two phases:
+// partial sums of the first two rows of every group, then (after the caller's
+// wait) their finishing parts and any further rows whole.
+struct RowsPart {
+    CellPartial c[2];
+};
+
+__device__ __forceinline__ RowsPart rows_partial(const Band& t, int d, int r0, int end)
+{
+    const int G = group_width(d), gpb = blockDim.x / G;
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+    RowsPart p;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const int i = r0 + g + it * gpb;
+        p.c[it] = inside_cell_partial(t, i, d, i < end, lane, G);
+    }
+    return p;
+}
+
+__device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int end, const RowsPart& p, const Rules& R)
+{
+    const int G = group_width(d), gpb = blockDim.x / G;
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const int i = r0 + g + it * gpb;
+        inside_cell_finish(t, i, d, i < end, lane, p.c[it], R);
+    }
+    for (int base = r0 + 2 * gpb; base < end; base += gpb) {
+        const int i = base + g;
+        inside_cell(t, i, d, i < end, lane, G, R);
+    }
+}
+
+// All band diagonals of the inside pass, two per grid barrier.  CTA b owns
+// rows [b*R, (b+1)*R) of every diagonal (R = ceil(L / CTAs)).  For the pair
+// (2p-1, 2p) it computes diagonal 2p-1 for its rows plus row (b+1)*R (which
+// the next CTA also computes, to the same bits) and then, after a CTA
+// barrier, diagonal 2p, whose cells read diagonal 2p-1 only at rows i and
+// i+1, its own.  The partial sums of both diagonals read spans <= 2p-4 and
+// are computed between the CTA's arrival at the barrier that completes
+// diagonal 2p-2 and its wait there.
 __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
     unsigned int gen = 0;
     const int L = t.L;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
     grid_arrive(t.sync);
-    for (int d = 1; d <= t.Wb; d++) {
-        const int G = group_width(d);
-        const int gpb = blockDim.x / G;
-        const int total = gridDim.x * gpb;
-        const int lane = threadIdx.x & (G - 1);
-        const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
-        const int ncell = L - d;
-        const CellPartial c = inside_cell_partial(t, gid0, d, gid0 < ncell, lane, G);
+    const int rows = (L + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * rows;
+    for (int eA = 1; eA <= t.Wb; eA += 2) {
+        const int eB = eA + 1;
+        const int endA = min(r0 + rows + 1, L - eA);
+        const int endB = (eB <= t.Wb) ? min(r0 + rows, L - eB) : r0;
+        const RowsPart pa = rows_partial(t, eA, r0, endA);
+        const RowsPart pb = rows_partial(t, eB, r0, endB);
         if (!grid_wait(t.sync, gen)) return;
-        inside_cell_finish(t, gid0, d, gid0 < ncell, lane, c, R);
-        for (int base = total; base < ncell; base += total) {
-            const int i = base + gid0;
-            inside_cell(t, i, d, i < ncell, lane, G, R);
-        }
+        rows_finish(t, eA, r0, endA, pa, R);
+        __syncthreads();  // diagonal 2p-1 of this CTA's rows before diagonal 2p reads it
+        rows_finish(t, eB, r0, endB, pb, R);
         grid_arrive(t.sync);
     }
 }
@@ -740,13 +802,20 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
 }
 
 // Launch a persistent wavefront kernel (cooperative: every CTA resident).
+// paired: the CTA owns ceil(L / grid) rows of every diagonal plus one; the
+// grid grows (up to one CTA per SM) until those fit one row per warp.
 static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
-                       double band_cells, const char* what)
+                       double band_cells, const char* what, bool paired = false)
 {
     const int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    const int grid = wave_grid(ctx, kernel, L, threads);
+    int grid = wave_grid(ctx, kernel, L, threads);
+    if (paired && ctx->wave_ctas <= 0) {
+        const int warps = threads / 32;
+        const int want = (warps > 1) ? (L + warps - 2) / (warps - 1) : L;
+        grid = std::max(grid, std::min(want, ctx->num_sms));
+    }
     e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_fail(ctx, e, what);
@@ -788,7 +857,7 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
     int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
-                         "inside_wave_kernel");
+                         "inside_wave_kernel", true);
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
