@@ -98,6 +98,8 @@ class Context:
         key = (id(dataset), W, mkey)
         h = self._datasets.get(key)
         if h is None or h.dataset is not dataset:
+            if h is not None:  # id() reused by a new dataset object
+                h.close()
             h = DatasetHandle(self, dataset, W, pairmask)
             self._datasets[key] = h
         return h

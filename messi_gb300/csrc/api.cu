@@ -524,8 +524,15 @@ int messi_dataset_destroy(messi_dataset* ds)
 {
     if (!ds) return MESSI_EINVAL;
     if (ds->ctx) {
-        cudaSetDevice(ds->ctx->device);
-        cudaStreamSynchronize(ds->ctx->stream);
+        messi_ctx* ctx = ds->ctx;
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        // a captured graph holds this dataset's pointers, and a later dataset
+        // may be allocated at the same address: drop it with the dataset
+        if (ctx->lgraph.key.ds == ds || ctx->lgraph.seen.ds == ds) {
+            if (ctx->lgraph.exec) cudaGraphExecDestroy(ctx->lgraph.exec);
+            ctx->lgraph = LikelihoodGraph{};
+        }
     }
     void* bufs[] = {ds->d_bandidx, ds->d_lr, ds->d_leaf, ds->d_nodes, ds->d_tiles, ds->d_masks, ds->d_tree,
                     ds->d_post, ds->d_arena_f, ds->d_arena_e, ds->d_mix, ds->d_mixlam};

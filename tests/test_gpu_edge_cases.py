@@ -2,6 +2,8 @@
 alignments and trees, ambiguity codes, all-gap columns, a band of one,
 constant columns, and invalid inputs that must be rejected with a status
 (relative 1e-6 on every log-likelihood)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -170,3 +172,43 @@ def test_likelihood_graph_replay_equals_eager(c1, monkeypatch):
         ctx.close()
     assert Zg == Ze
     assert replays >= 3, replays
+
+
+def test_likelihood_graph_dropped_with_its_dataset(c1):
+    """A captured likelihood graph holds its dataset's device pointers:
+    destroying the dataset drops it, so a dataset created afterwards (which
+    may reuse the host address) starts with eager calls and replays only its
+    own capture, with the eager values."""
+    from messi_gb300 import api
+    from messi_gb300 import model as M
+    ds = c1.dataset
+    params = M.getparams(c1.params15, ds.branchlengths)
+    ctx = api.Context(0)
+    handles = []
+    try:
+        h1 = api.DatasetHandle(ctx, ds, c1.W)
+        handles.append(h1)
+        m = api.ModelArgs(params)
+
+        def Z(h):
+            z = ctypes.c_double()
+            ctx.check(ctx.lib.messi_likelihood(ctx.handle, h.handle, ctypes.byref(m.struct), None, 1.0,
+                                               ctypes.byref(z), None), "messi_likelihood")
+            return z.value
+
+        # the first call's scratch allocations change the key: capture from the third call
+        first = [Z(h1) for _ in range(4)]
+        r0 = ctx.graph_replays()
+        assert r0 >= 1, r0
+        h1.close()
+        h2 = api.DatasetHandle(ctx, ds, c1.W)
+        handles.append(h2)
+        second = [Z(h2)]
+        assert ctx.graph_replays() == r0  # no replay of the destroyed dataset's graph
+        second += [Z(h2) for _ in range(3)]
+        assert ctx.graph_replays() > r0
+    finally:
+        for h in handles:
+            h.close()
+        ctx.close()
+    assert len(set(first + second)) == 1, first + second
