@@ -433,32 +433,60 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
     return c;
 }
 
+// Operands of a cell's outer split points, k < NLO and k >= hb = max(NLO,
+// d-NHI) in ascending k: L(i, i+k) and S(i+k+1, j), both -inf where the
+// split point is absent (an absent term is then -inf, which lse_add skips
+// exactly), and the enclosed F(i+1, j-1).
 template <int NLO, int NHI>
-__device__ __forceinline__ void cell_finish_t(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
-                                              const Rules& R)
+struct Outer {
+    float l[NLO + NHI], s[NLO + NHI], fin;
+};
+
+// defer: leave L(i, i+d-1) and S(i+1, j), the two operands on diagonal d-1,
+// to outer_patch.
+template <int NLO, int NHI>
+__device__ __forceinline__ Outer<NLO, NHI> outer_load(const Band& t, int i, int d, bool defer)
 {
-    if (!(valid && lane == 0)) return;
+    Outer<NLO, NHI> o;
     const int RS = t.RS;
-    const int j = i + d;
     const float* lrow = t.Lrow + (size_t)i * RS;
-    const float* scol = t.Scol + (size_t)j * RS + (d - 1);
-    // outer split points k < NLO and k >= hb = max(NLO, d-NHI), loaded
-    // together and added in ascending k (an absent one is -inf, which
-    // lse_add skips exactly)
-    float xl[NLO], xh[NHI];
-#pragma unroll
-    for (int q = 0; q < NLO; q++) xl[q] = (q < d) ? __ldcg(lrow + q) + __ldcg(scol - q) : -INFINITY;
+    const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
     const int hb = max(NLO, d - NHI);
 #pragma unroll
-    for (int q = 0; q < NHI; q++)
-        xh[q] = (hb + q < d) ? __ldcg(lrow + hb + q) + __ldcg(scol - (hb + q)) : -INFINITY;
-    const float fin = (d >= 2) ? __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2)) : -INFINITY;
+    for (int q = 0; q < NLO + NHI; q++) {
+        const int k = (q < NLO) ? q : hb + (q - NLO);
+        const bool present = k < d;
+        o.l[q] = !present ? -INFINITY : ((defer && k == d - 1) ? 0.f : __ldcg(lrow + k));
+        o.s[q] = !present ? -INFINITY : ((defer && k == 0) ? 0.f : __ldcg(scol - k));
+    }
+    o.fin = (d >= 2) ? __ldcg(t.Frow + (size_t)(i + 1) * RS + (d - 2)) : -INFINITY;
+    return o;
+}
+
+template <int NLO, int NHI>
+__device__ __forceinline__ void outer_patch(Outer<NLO, NHI>& o, int d, float l_last, float s_first)
+{
+    const int hb = max(NLO, d - NHI);
 #pragma unroll
-    for (int q = 0; q < NLO; q++) lse_add(c.m, c.s, xl[q]);
+    for (int q = 0; q < NLO + NHI; q++) {
+        const int k = (q < NLO) ? q : hb + (q - NLO);
+        if (k < d && k == d - 1) o.l[q] = l_last;
+        if (k < d && k == 0) o.s[q] = s_first;
+    }
+}
+
+// Adds the outer split points to the partial sum and writes cell (i, i+d);
+// lv/sv, when given, also receive its L and S.
+template <int NLO, int NHI>
+__device__ __forceinline__ void cell_write_t(const Band& t, int i, int d, CellPartial c, const Outer<NLO, NHI>& o,
+                                             const Rules& R, float* lv = nullptr, float* sv = nullptr)
+{
+    const int RS = t.RS;
+    const int j = i + d;
 #pragma unroll
-    for (int q = 0; q < NHI; q++) lse_add(c.m, c.s, xh[q]);
+    for (int q = 0; q < NLO + NHI; q++) lse_add(c.m, c.s, o.l[q] + o.s[q]);
     const float tmp = lse_val(c.m, c.s);
-    const float v = c.pbv + fin;
+    const float v = c.pbv + o.fin;
     const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
     const float F = lse2f(R.r[4] + tmp, R.r[3] + v);
     const float Lv = R.r[6] + v;
@@ -468,6 +496,18 @@ __device__ __forceinline__ void cell_finish_t(const Band& t, int i, int d, bool 
     t.Scol[(size_t)j * RS + d] = S;
     t.Frow[(size_t)i * RS + d] = F;
     if (j == t.L - 1) t.Ssuf[i] = S;
+    if (lv) {
+        *lv = Lv;
+        *sv = S;
+    }
+}
+
+template <int NLO, int NHI>
+__device__ __forceinline__ void cell_finish_t(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
+                                              const Rules& R)
+{
+    if (!(valid && lane == 0)) return;
+    cell_write_t<NLO, NHI>(t, i, d, c, outer_load<NLO, NHI>(t, i, d, false), R);
 }
 
 __device__ __forceinline__ CellPartial inside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G)
@@ -487,18 +527,30 @@ __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool va
     inside_cell_finish(t, i, d, valid, lane, inside_cell_partial(t, i, d, valid, lane, G), R);
 }
 
-// The cells of one diagonal that a CTA owns (rows [r0, end)), in two phases:
-// partial sums of the first two rows of every group, then (after the caller's
-// wait) their finishing parts and any further rows whole.
+// The cells of one diagonal that a CTA owns (rows [r0, end)), computed by the
+// CTA's warps [w0, w0 + nw) in two phases: partial sums of the first two rows
+// of every group, then (after the caller's wait) their finishing parts and any
+// further rows whole.  Which warp computes a cell does not change its bits.
 struct RowsPart {
     CellPartial c[2];
 };
 
-__device__ __forceinline__ RowsPart rows_partial(const Band& t, int d, int r0, int end)
+struct WarpSet {
+    int w0, nw;
+    __device__ __forceinline__ bool mine() const
+    {
+        const int w = threadIdx.x >> 5;
+        return w >= w0 && w < w0 + nw;
+    }
+};
+
+__device__ __forceinline__ RowsPart rows_partial(const Band& t, int d, int r0, int end, WarpSet ws)
 {
-    const int G = group_width(d), gpb = blockDim.x / G;
-    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
     RowsPart p;
+    p.c[0] = p.c[1] = CellPartial{-INFINITY, 0.f, -INFINITY};
+    if (!ws.mine()) return p;  // warp-uniform: the group shuffles stay within the warp
+    const int G = group_width(d), gpb = ws.nw * (32 / G);
+    const int lane = threadIdx.x & (G - 1), g = (threadIdx.x - 32 * ws.w0) / G;
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int i = r0 + g + it * gpb;
@@ -507,10 +559,12 @@ __device__ __forceinline__ RowsPart rows_partial(const Band& t, int d, int r0, i
     return p;
 }
 
-__device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int end, const RowsPart& p, const Rules& R)
+__device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int end, const RowsPart& p, const Rules& R,
+                                            WarpSet ws)
 {
-    const int G = group_width(d), gpb = blockDim.x / G;
-    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+    if (!ws.mine()) return;
+    const int G = group_width(d), gpb = ws.nw * (32 / G);
+    const int lane = threadIdx.x & (G - 1), g = (threadIdx.x - 32 * ws.w0) / G;
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int i = r0 + g + it * gpb;
@@ -529,25 +583,57 @@ __device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int en
 // barrier, diagonal 2p, whose cells read diagonal 2p-1 only at rows i and
 // i+1, its own.  The partial sums of both diagonals read spans <= 2p-4 and
 // are computed between the CTA's arrival at the barrier that completes
-// diagonal 2p-2 and its wait there.
+// diagonal 2p-2 and its wait there.  When R + 1 rows fit one per warp in
+// half of the CTA, the two diagonals' partial sums run in disjoint halves
+// at the same time; otherwise every warp computes both, one after the other.
 __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
+    // L and S of diagonal 2p-1 at the CTA's rows (halves: at most one row per warp of a half)
+    __shared__ float s_lv[kWaveMaxThreads / 64], s_sv[kWaveMaxThreads / 64];
     unsigned int gen = 0;
     const int L = t.L;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
     grid_arrive(t.sync);
     const int rows = (L + gridDim.x - 1) / gridDim.x;
     const int r0 = blockIdx.x * rows;
+    const int nw = blockDim.x >> 5;
+    const bool halves = nw >= 2 * (rows + 1);
+    const WarpSet wa{0, halves ? nw / 2 : nw}, wb{halves ? nw / 2 : 0, halves ? nw - nw / 2 : nw};
     for (int eA = 1; eA <= t.Wb; eA += 2) {
         const int eB = eA + 1;
         const int endA = min(r0 + rows + 1, L - eA);
         const int endB = (eB <= t.Wb) ? min(r0 + rows, L - eB) : r0;
-        const RowsPart pa = rows_partial(t, eA, r0, endA);
-        const RowsPart pb = rows_partial(t, eB, r0, endB);
+        const RowsPart pa = rows_partial(t, eA, r0, endA, wa);
+        const RowsPart pb = rows_partial(t, eB, r0, endB, wb);
         if (!grid_wait(t.sync, gen)) return;
-        rows_finish(t, eA, r0, endA, pa, R);
-        __syncthreads();  // diagonal 2p-1 of this CTA's rows before diagonal 2p reads it
-        rows_finish(t, eB, r0, endB, pb, R);
+        if (halves) {
+            // one cell per group; diagonal 2p's outer operands off diagonal
+            // 2p-1 are loaded while diagonal 2p-1 finishes, the two on it
+            // (rows i and i+1 of this CTA) come through shared memory
+            int ib = -1;
+            Outer<3, 3> ob;
+            if (wa.mine()) {
+                const int G = group_width(eA), g = threadIdx.x / G, i = r0 + g;
+                if (i < endA && (threadIdx.x & (G - 1)) == 0)
+                    cell_write_t<2, 2>(t, i, eA, pa.c[0], outer_load<2, 2>(t, i, eA, false), R, s_lv + g, s_sv + g);
+            } else if (wb.mine()) {
+                const int G = group_width(eB), g = (threadIdx.x - 32 * wb.w0) / G, i = r0 + g;
+                if (i < endB && (threadIdx.x & (G - 1)) == 0) {
+                    ob = outer_load<3, 3>(t, i, eB, true);
+                    ib = i;
+                }
+            }
+            __syncthreads();
+            if (ib >= 0) {
+                outer_patch<3, 3>(ob, eB, s_lv[ib - r0], s_sv[ib + 1 - r0]);
+                cell_write_t<3, 3>(t, ib, eB, pb.c[0], ob, R);
+            }
+            // (grid_arrive's CTA barrier orders these reads before the next pair's writes)
+        } else {
+            rows_finish(t, eA, r0, endA, pa, R, wa);
+            __syncthreads();  // diagonal 2p-1 of this CTA's rows before diagonal 2p reads it
+            rows_finish(t, eB, r0, endB, pb, R, wb);
+        }
         grid_arrive(t.sync);
     }
 }
@@ -801,19 +887,36 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
     return grid;
 }
 
+// CTAs for which a CTA's ceil(L / CTAs) rows plus one fit one per warp in
+// `warps` warps.
+static int ctas_for_rows(int L, int warps) { return (warps > 1) ? (L + warps - 2) / (warps - 1) : L; }
+
 // Launch a persistent wavefront kernel (cooperative: every CTA resident).
-// paired: the CTA owns ceil(L / grid) rows of every diagonal plus one; the
-// grid grows (up to one CTA per SM) until those fit one row per warp.
+// paired: the CTA owns ceil(L / grid) rows of every diagonal plus one.  The
+// CTA doubles (once, unless its size is set) when that lets each half of it
+// hold those rows one per warp with at most one CTA per SM, so that the two
+// diagonals' partial sums run at the same time; the grid then grows (up to
+// one CTA per SM) until the rows fit one per warp of a half, or else of the
+// whole CTA.
 static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
                        double band_cells, const char* what, bool paired = false)
 {
-    const int threads = wave_threads(ctx, band_cells);
+    int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
-    int grid = wave_grid(ctx, kernel, L, threads);
+    int grid = wave_grid(ctx, kernel, L, threads);  // also sets ctx->num_sms
     if (paired && ctx->wave_ctas <= 0) {
+        for (int t2 = threads; t2 <= (ctx->wave_threads ? threads : std::min(2 * threads, kWaveMaxThreads)); t2 *= 2)
+            if (ctas_for_rows(L, t2 / 64) <= ctx->num_sms) {
+                if (t2 != threads) {
+                    threads = t2;
+                    grid = wave_grid(ctx, kernel, L, threads);
+                }
+                break;
+            }
         const int warps = threads / 32;
-        const int want = (warps > 1) ? (L + warps - 2) / (warps - 1) : L;
+        const int half = ctas_for_rows(L, warps / 2);
+        const int want = (half <= ctx->num_sms) ? half : ctas_for_rows(L, warps);
         grid = std::max(grid, std::min(want, ctx->num_sms));
     }
     e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
