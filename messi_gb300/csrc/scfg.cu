@@ -416,18 +416,18 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
     if (valid && kend > NLO) {
         const float* lrow = t.Lrow + (size_t)i * RS;
         const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
-        int k = NLO + lane;
-        for (; k + 7 * G < kend; k += 8 * G) {
+        // blocks of eight split points per lane, the sixteen loads of a block
+        // issued together (a lane has at most eight points up to span 256);
+        // points past the end are -inf, which lse_add8 skips exactly
+        for (int k = NLO + lane; k < kend; k += 8 * G) {
             float x[8];
 #pragma unroll
-            for (int q = 0; q < 8; q++) x[q] = __ldcg(lrow + k + q * G) + __ldcg(scol - k - q * G);
+            for (int q = 0; q < 8; q++) {
+                const int kq = k + q * G;
+                x[q] = (kq < kend) ? __ldcg(lrow + kq) + __ldcg(scol - kq) : -INFINITY;
+            }
             lse_add8(c.m, c.s, x);
         }
-        for (; k + 3 * G < kend; k += 4 * G)
-            lse_add4(c.m, c.s, __ldcg(lrow + k) + __ldcg(scol - k), __ldcg(lrow + k + G) + __ldcg(scol - k - G),
-                     __ldcg(lrow + k + 2 * G) + __ldcg(scol - k - 2 * G),
-                     __ldcg(lrow + k + 3 * G) + __ldcg(scol - k - 3 * G));
-        for (; k < kend; k += G) lse_add(c.m, c.s, __ldcg(lrow + k) + __ldcg(scol - k));
     }
     group_reduce_rt(c.m, c.s, G);
     return c;
