@@ -433,6 +433,67 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
     return c;
 }
 
+// cell_partial_t in two steps, for a wavefront that issues a cell's loads
+// one phase before it needs them: partial_issue loads the pair score and the
+// operands of the first two blocks (sixteen split points per lane) without
+// using them, so that the loads stay in flight; partial_complete adds them
+// and any further blocks in the same order and reduces over the group, so the
+// result has the bits of cell_partial_t.
+struct PartialPre {
+    float a[16], b[16];
+    float pbv;
+};
+
+template <int NLO, int NHI>
+__device__ __forceinline__ void partial_issue(const Band& t, int i, int d, bool valid, int lane, int G,
+                                              PartialPre& pp)
+{
+    const int RS = t.RS;
+    pp.pbv = (valid && lane == 0 && d >= 2) ? t.pb[(size_t)i * RS + d] : -INFINITY;
+    const int kend = d - NHI;
+    const float* lrow = t.Lrow + (size_t)i * RS;
+    const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int kq = NLO + lane + q * G;
+        const bool on = valid && kq < kend;
+        pp.a[q] = on ? __ldcg(lrow + kq) : -INFINITY;
+        pp.b[q] = on ? __ldcg(scol - kq) : -INFINITY;
+    }
+}
+
+template <int NLO, int NHI>
+__device__ __forceinline__ CellPartial partial_complete(const Band& t, int i, int d, bool valid, int lane, int G,
+                                                        const PartialPre& pp)
+{
+    CellPartial c{-INFINITY, 0.f, pp.pbv};
+    const int kend = d - NHI;
+    if (valid && kend > NLO) {
+        // a block that cell_partial_t would not reach is all -inf: lse_add8 leaves (m, s) as they are
+        float x0[8], x1[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            x0[q] = pp.a[q] + pp.b[q];
+            x1[q] = pp.a[8 + q] + pp.b[8 + q];
+        }
+        lse_add8(c.m, c.s, x0);
+        lse_add8(c.m, c.s, x1);
+        const float* lrow = t.Lrow + (size_t)i * t.RS;
+        const float* scol = t.Scol + (size_t)(i + d) * t.RS + (d - 1);
+        for (int k = NLO + lane + 16 * G; k < kend; k += 8 * G) {
+            float x[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int kq = k + q * G;
+                x[q] = (kq < kend) ? __ldcg(lrow + kq) + __ldcg(scol - kq) : -INFINITY;
+            }
+            lse_add8(c.m, c.s, x);
+        }
+    }
+    group_reduce_rt(c.m, c.s, G);
+    return c;
+}
+
 // Operands of a cell's outer split points, k < NLO and k >= hb = max(NLO,
 // d-NHI) in ascending k: L(i, i+k) and S(i+k+1, j), both -inf where the
 // split point is absent (an absent term is then -inf, which lse_add skips
@@ -635,6 +696,91 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
             rows_finish(t, eB, r0, endB, pb, R, wb);
         }
         grid_arrive(t.sync);
+    }
+}
+
+// inside_wave_kernel when the CTA's rows fit one per warp in each half of
+// the CTA (the host launches it only then): the odd diagonals' cells go to
+// the first half, the even ones' to the second, one cell per lane group.
+// The wait that completes diagonal 2p-2 also completes every span that the
+// next pair's partial sums read (<= 2p-2), so right after it a warp issues
+// the loads of its next cell's partial sum, finishes its current cell while
+// they are in flight, and adds them after its arrival.
+constexpr int kPipeThreads = 512;
+
+__global__ void __launch_bounds__(kPipeThreads) inside_wave_pipe_kernel(Band t, Rules R, double B)
+{
+    __shared__ float s_lv[kPipeThreads / 64], s_sv[kPipeThreads / 64];
+    unsigned int gen = 0;
+    const int L = t.L, Wb = t.Wb;
+    const int rows = (L + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * rows;
+    const int half = (int)(blockDim.x >> 6);
+    if (half < rows + 1) {  // not launched so; leave with the launch marked failed
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&t.sync[2], 1u);
+        return;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
+    grid_arrive(t.sync);
+    const bool odd = (int)(threadIdx.x >> 5) < half;
+    const int tid = (int)threadIdx.x - (odd ? 0 : 32 * half);
+    // this warp's diagonal of pair p is 2p-1 (odd) or 2p; its cell's row r0 + g
+    auto row_end = [&](int d) {
+        return (d > Wb) ? r0 : (odd ? min(r0 + rows + 1, L - d) : min(r0 + rows, L - d));
+    };
+    int d = odd ? 1 : 2;
+    int G = group_width(d), lane = tid & (G - 1), i = r0 + tid / G;
+    bool valid = i < row_end(d);
+    CellPartial c;
+    {
+        PartialPre pp;
+        if (odd) {
+            partial_issue<2, 2>(t, i, d, valid, lane, G, pp);
+            c = partial_complete<2, 2>(t, i, d, valid, lane, G, pp);
+        } else {
+            partial_issue<3, 3>(t, i, d, valid, lane, G, pp);
+            c = partial_complete<3, 3>(t, i, d, valid, lane, G, pp);
+        }
+    }
+    for (int eA = 1; eA <= Wb; eA += 2) {
+        if (!grid_wait(t.sync, gen)) return;
+        const int dn = d + 2;
+        const int Gn = group_width(dn), lanen = tid & (Gn - 1), in = r0 + tid / Gn;
+        const bool validn = in < row_end(dn);
+        PartialPre pn;
+        int ib = -1;
+        Outer<3, 3> ob;
+        // the current cell's operands first (they are on the critical path),
+        // then the next cell's, then the current cell's arithmetic
+        if (odd) {
+            Outer<2, 2> oa;
+            const bool fin = valid && lane == 0;
+            if (fin) oa = outer_load<2, 2>(t, i, d, false);
+            partial_issue<2, 2>(t, in, dn, validn, lanen, Gn, pn);
+            if (fin) cell_write_t<2, 2>(t, i, d, c, oa, R, s_lv + (i - r0), s_sv + (i - r0));
+        } else {
+            if (valid && lane == 0) {
+                ob = outer_load<3, 3>(t, i, d, true);
+                ib = i;
+            }
+            partial_issue<3, 3>(t, in, dn, validn, lanen, Gn, pn);
+        }
+        __syncthreads();  // diagonal 2p-1 of this CTA's rows in s_lv / s_sv
+        if (ib >= 0) {
+            outer_patch<3, 3>(ob, d, s_lv[ib - r0], s_sv[ib + 1 - r0]);
+            cell_write_t<3, 3>(t, ib, d, c, ob, R);
+        }
+        // the last warp never has a cell (its group index is >= rows), so no
+        // loads in flight for the fence to wait for; the CTA barrier also
+        // orders these reads before the next pair's writes
+        grid_arrive(t.sync, blockDim.x - 1);
+        c = odd ? partial_complete<2, 2>(t, in, dn, validn, lanen, Gn, pn)
+                : partial_complete<3, 3>(t, in, dn, validn, lanen, Gn, pn);
+        d = dn;
+        G = Gn;
+        lane = lanen;
+        i = in;
+        valid = validn;
     }
 }
 
@@ -899,7 +1045,8 @@ static int ctas_for_rows(int L, int warps) { return (warps > 1) ? (L + warps - 2
 // one CTA per SM) until the rows fit one per warp of a half, or else of the
 // whole CTA.
 static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
-                       double band_cells, const char* what, bool paired = false)
+                       double band_cells, const char* what, bool paired = false, const void* halves_kernel = nullptr,
+                       int halves_max_threads = 0)
 {
     int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
@@ -918,6 +1065,9 @@ static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned
         const int half = ctas_for_rows(L, warps / 2);
         const int want = (half <= ctx->num_sms) ? half : ctas_for_rows(L, warps);
         grid = std::max(grid, std::min(want, ctx->num_sms));
+        // the halves shape (rows + 1 <= warps / 2 for ceil(L / grid) rows)
+        const int rows = (L + grid - 1) / grid;
+        if (halves_kernel && threads <= halves_max_threads && rows + 1 <= warps / 2) kernel = halves_kernel;
     }
     e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
     ctx->launches++;
@@ -960,7 +1110,7 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
     int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
-                         "inside_wave_kernel", true);
+                         "inside_wave_kernel", true, (const void*)inside_wave_pipe_kernel, kPipeThreads);
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {

@@ -39,11 +39,14 @@ constexpr unsigned int kBarrierError = 1u << 30;
 // __ldcg (L2, coherent across SMs): the per-SM L1 may hold stale lines of
 // those tables.  The barrier comes in two halves (grid_arrive, grid_wait) so
 // that a CTA can work between its arrival and its wait on cells that do not
-// depend on the other CTAs' latest writes; grid_sync is both at once.
-static __device__ __forceinline__ void grid_arrive(unsigned int* sync)
+// depend on the other CTAs' latest writes; grid_sync is both at once.  Any
+// thread may arrive for the CTA (`leader`): the fence waits for that
+// thread's own loads still in flight, so a kernel that keeps loads in flight
+// across its arrival picks a thread without any.
+static __device__ __forceinline__ void grid_arrive(unsigned int* sync, unsigned int leader = 0)
 {
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == leader) {
         __threadfence();
         atomicAdd(&sync[0], 1u);
     }
