@@ -703,9 +703,9 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
 // the CTA (the host launches it only then): the odd diagonals' cells go to
 // the first half, the even ones' to the second, one cell per lane group.
 // The wait that completes diagonal 2p-2 also completes every span that the
-// next pair's partial sums read (<= 2p-2), so right after it a warp issues
-// the loads of its next cell's partial sum, finishes its current cell while
-// they are in flight, and adds them after its arrival.
+// next pair's partial sums read (<= 2p-2), so a warp issues the loads of its
+// next cell's partial sum as soon as its current cell is finished, before
+// the arrival, and adds them after it.
 constexpr int kPipeThreads = 512;
 
 __global__ void __launch_bounds__(kPipeThreads) inside_wave_pipe_kernel(Band t, Rules R, double B)
@@ -750,26 +750,23 @@ __global__ void __launch_bounds__(kPipeThreads) inside_wave_pipe_kernel(Band t, 
         PartialPre pn;
         int ib = -1;
         Outer<3, 3> ob;
-        // the current cell's operands first (they are on the critical path),
-        // then the next cell's, then the current cell's arithmetic
         if (odd) {
-            Outer<2, 2> oa;
-            const bool fin = valid && lane == 0;
-            if (fin) oa = outer_load<2, 2>(t, i, d, false);
-            partial_issue<2, 2>(t, in, dn, validn, lanen, Gn, pn);
-            if (fin) cell_write_t<2, 2>(t, i, d, c, oa, R, s_lv + (i - r0), s_sv + (i - r0));
-        } else {
-            if (valid && lane == 0) {
-                ob = outer_load<3, 3>(t, i, d, true);
-                ib = i;
-            }
-            partial_issue<3, 3>(t, in, dn, validn, lanen, Gn, pn);
+            if (valid && lane == 0)
+                cell_write_t<2, 2>(t, i, d, c, outer_load<2, 2>(t, i, d, false), R, s_lv + (i - r0), s_sv + (i - r0));
+        } else if (valid && lane == 0) {
+            ob = outer_load<3, 3>(t, i, d, true);
+            ib = i;
         }
         __syncthreads();  // diagonal 2p-1 of this CTA's rows in s_lv / s_sv
         if (ib >= 0) {
             outer_patch<3, 3>(ob, d, s_lv[ib - r0], s_sv[ib + 1 - r0]);
             cell_write_t<3, 3>(t, ib, d, c, ob, R);
         }
+        // the next cell's loads go out after the current cells' (issued
+        // earlier they queue ahead of the finishing loads, which are on the
+        // critical path) and stay in flight across the arrival
+        if (odd) partial_issue<2, 2>(t, in, dn, validn, lanen, Gn, pn);
+        else partial_issue<3, 3>(t, in, dn, validn, lanen, Gn, pn);
         // the last warp never has a cell (its group index is >= rows), so no
         // loads in flight for the fence to wait for; the CTA barrier also
         // orders these reads before the next pair's writes
