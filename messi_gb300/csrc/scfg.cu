@@ -644,57 +644,27 @@ __device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int en
 // barrier, diagonal 2p, whose cells read diagonal 2p-1 only at rows i and
 // i+1, its own.  The partial sums of both diagonals read spans <= 2p-4 and
 // are computed between the CTA's arrival at the barrier that completes
-// diagonal 2p-2 and its wait there.  When R + 1 rows fit one per warp in
-// half of the CTA, the two diagonals' partial sums run in disjoint halves
-// at the same time; otherwise every warp computes both, one after the other.
+// diagonal 2p-2 and its wait there; every warp computes both diagonals'
+// cells, one after the other.
 __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Rules R, double B)
 {
-    // L and S of diagonal 2p-1 at the CTA's rows (halves: at most one row per warp of a half)
-    __shared__ float s_lv[kWaveMaxThreads / 64], s_sv[kWaveMaxThreads / 64];
     unsigned int gen = 0;
     const int L = t.L;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) inside_init_cell(t, i, R, B);
     grid_arrive(t.sync);
     const int rows = (L + gridDim.x - 1) / gridDim.x;
     const int r0 = blockIdx.x * rows;
-    const int nw = blockDim.x >> 5;
-    const bool halves = nw >= 2 * (rows + 1);
-    const WarpSet wa{0, halves ? nw / 2 : nw}, wb{halves ? nw / 2 : 0, halves ? nw - nw / 2 : nw};
+    const WarpSet all{0, (int)(blockDim.x >> 5)};
     for (int eA = 1; eA <= t.Wb; eA += 2) {
         const int eB = eA + 1;
         const int endA = min(r0 + rows + 1, L - eA);
         const int endB = (eB <= t.Wb) ? min(r0 + rows, L - eB) : r0;
-        const RowsPart pa = rows_partial(t, eA, r0, endA, wa);
-        const RowsPart pb = rows_partial(t, eB, r0, endB, wb);
+        const RowsPart pa = rows_partial(t, eA, r0, endA, all);
+        const RowsPart pb = rows_partial(t, eB, r0, endB, all);
         if (!grid_wait(t.sync, gen)) return;
-        if (halves) {
-            // one cell per group; diagonal 2p's outer operands off diagonal
-            // 2p-1 are loaded while diagonal 2p-1 finishes, the two on it
-            // (rows i and i+1 of this CTA) come through shared memory
-            int ib = -1;
-            Outer<3, 3> ob;
-            if (wa.mine()) {
-                const int G = group_width(eA), g = threadIdx.x / G, i = r0 + g;
-                if (i < endA && (threadIdx.x & (G - 1)) == 0)
-                    cell_write_t<2, 2>(t, i, eA, pa.c[0], outer_load<2, 2>(t, i, eA, false), R, s_lv + g, s_sv + g);
-            } else if (wb.mine()) {
-                const int G = group_width(eB), g = (threadIdx.x - 32 * wb.w0) / G, i = r0 + g;
-                if (i < endB && (threadIdx.x & (G - 1)) == 0) {
-                    ob = outer_load<3, 3>(t, i, eB, true);
-                    ib = i;
-                }
-            }
-            __syncthreads();
-            if (ib >= 0) {
-                outer_patch<3, 3>(ob, eB, s_lv[ib - r0], s_sv[ib + 1 - r0]);
-                cell_write_t<3, 3>(t, ib, eB, pb.c[0], ob, R);
-            }
-            // (grid_arrive's CTA barrier orders these reads before the next pair's writes)
-        } else {
-            rows_finish(t, eA, r0, endA, pa, R, wa);
-            __syncthreads();  // diagonal 2p-1 of this CTA's rows before diagonal 2p reads it
-            rows_finish(t, eB, r0, endB, pb, R, wb);
-        }
+        rows_finish(t, eA, r0, endA, pa, R, all);
+        __syncthreads();  // diagonal 2p-1 of this CTA's rows before diagonal 2p reads it
+        rows_finish(t, eB, r0, endB, pb, R, all);
         grid_arrive(t.sync);
     }
 }
@@ -706,11 +676,9 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
 // next pair's partial sums read (<= 2p-2), so a warp issues the loads of its
 // next cell's partial sum as soon as its current cell is finished, before
 // the arrival, and adds them after it.
-constexpr int kPipeThreads = 512;
-
-__global__ void __launch_bounds__(kPipeThreads) inside_wave_pipe_kernel(Band t, Rules R, double B)
+__global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_pipe_kernel(Band t, Rules R, double B)
 {
-    __shared__ float s_lv[kPipeThreads / 64], s_sv[kPipeThreads / 64];
+    __shared__ float s_lv[kWaveMaxThreads / 64], s_sv[kWaveMaxThreads / 64];
     unsigned int gen = 0;
     const int L = t.L, Wb = t.Wb;
     const int rows = (L + gridDim.x - 1) / gridDim.x;
@@ -1042,8 +1010,7 @@ static int ctas_for_rows(int L, int warps) { return (warps > 1) ? (L + warps - 2
 // one CTA per SM) until the rows fit one per warp of a half, or else of the
 // whole CTA.
 static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
-                       double band_cells, const char* what, bool paired = false, const void* halves_kernel = nullptr,
-                       int halves_max_threads = 0)
+                       double band_cells, const char* what, bool paired = false, const void* halves_kernel = nullptr)
 {
     int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
@@ -1064,7 +1031,7 @@ static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned
         grid = std::max(grid, std::min(want, ctx->num_sms));
         // the halves shape (rows + 1 <= warps / 2 for ceil(L / grid) rows)
         const int rows = (L + grid - 1) / grid;
-        if (halves_kernel && threads <= halves_max_threads && rows + 1 <= warps / 2) kernel = halves_kernel;
+        if (halves_kernel && rows + 1 <= warps / 2) kernel = halves_kernel;
     }
     e = cudaLaunchCooperativeKernel(kernel, dim3(grid), dim3(threads), args, 0, ctx->stream);
     ctx->launches++;
@@ -1107,7 +1074,7 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
     int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
-                         "inside_wave_kernel", true, (const void*)inside_wave_pipe_kernel, kPipeThreads);
+                         "inside_wave_kernel", true, (const void*)inside_wave_pipe_kernel);
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {

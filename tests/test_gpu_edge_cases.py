@@ -212,3 +212,41 @@ def test_likelihood_graph_dropped_with_its_dataset(c1):
             h.close()
         ctx.close()
     assert len(set(first + second)) == 1, first + second
+
+
+@pytest.mark.parametrize("env", [{"MESSI_WAVE_THREADS": "1024"},
+                                 {"MESSI_WAVE_THREADS": "256", "MESSI_WAVE_CTAS": "7"},
+                                 {"MESSI_WAVE_CTAS": "1"}])
+def test_inside_kernels_and_grids_bit_identical(env, monkeypatch):
+    """Which kernel and grid run the inside pass changes only which warp
+    computes a cell: the pipelined halves kernel (the default here, 256 and
+    1,024 threads), the plain wavefront with 7 CTAs of 58 rows and with one
+    CTA (rows beyond two per lane group computed whole) give the same bits."""
+    from messi_gb300 import api
+    rng = np.random.default_rng(12)
+    L, W = 400, 150
+    u = rng.uniform(-30.0, -8.0, L)
+    p = np.full((L, L), -np.inf)
+    for i in range(L):
+        for j in range(i + 1, min(L, i + W + 1)):
+            p[i, j] = p[j, i] = u[i] + u[j] + rng.normal(-2.0, 3.0)
+    ctx = api.Context(0)
+    try:
+        T0 = api.computeinsideKH99(u, p, zonly=False, ctx=ctx)
+        Z0 = api.computeinsideKH99(u, p, ctx=ctx)
+        post0 = api.computeposteriors(u, p, ctx=ctx)
+    finally:
+        ctx.close()
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    ctx = api.Context(0)
+    try:
+        T1 = api.computeinsideKH99(u, p, zonly=False, ctx=ctx)
+        Z1 = api.computeinsideKH99(u, p, ctx=ctx)
+        post1 = api.computeposteriors(u, p, ctx=ctx)
+    finally:
+        ctx.close()
+    np.testing.assert_array_equal(T1, T0)
+    assert Z1 == Z0
+    for a, b in zip(post1, post0):
+        np.testing.assert_array_equal(a, b)
