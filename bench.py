@@ -73,8 +73,14 @@ class Clocks:
                                          stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the sampler is live before the timed region starts; samples
+            # taken before it (the first one) are left out of the summary
+            t0 = time.perf_counter()
+            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
+        self.start = len(self.lines)
         return self
 
     def _read(self):
@@ -92,7 +98,7 @@ class Clocks:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in (self.lines[self.start:] or self.lines):
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -625,7 +631,9 @@ def run_structures(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 100 for the bench line and the reference arm, about 1 s of "
+                         "timed work; 5 with --structures, 3 with --batch)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -642,6 +650,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = 3 if args.batch else (5 if args.structures else 100)
     if args.mcmc:
         run_mcmc(args)
     elif args.batch:
