@@ -27,12 +27,16 @@
 //
 // Schedule.  One persistent cooperative launch walks the band diagonals (a
 // wavefront): all cells of a span are independent, so each diagonal is spread
-// over the whole grid and a grid barrier separates diagonals.  The barrier
-// spins with a bounded iteration count; on timeout it raises an error flag,
-// every CTA leaves, Z becomes NaN and the host returns MESSI_ETIMEOUT.  A
-// cell's split sum is reduced by a group of G lanes (G grows with the number
-// of split points) with shuffle log-sum-exp.  The suffix recurrences run in
-// one CTA in blocks of 32 cells: the terms that reach outside the block are
+// over the whole grid and grid barriers separate diagonals (the inside pass
+// takes two diagonals per barrier: a CTA owns a block of rows and the second
+// diagonal of a pair reads the first only at the CTA's own rows).  The
+// barrier spins with a bounded iteration count; on timeout it raises an
+// error flag, every CTA leaves, Z becomes NaN and the host returns
+// MESSI_ETIMEOUT.  A cell's split sum is reduced by a group of G lanes (G
+// grows with the number of split points) with shuffle log-sum-exp; its
+// middle split points, which do not read the diagonals just finished, are
+// summed while a barrier is in progress.  The suffix recurrences run in one
+// CTA in blocks of 32 cells: the terms that reach outside the block are
 // summed by 32 warps in parallel, the in-block triangle by one warp.
 #include <algorithm>
 #include <cmath>
