@@ -280,20 +280,24 @@ int messi_mlp_train_step(messi_ctx* ctx, messi_mlp* mlp, int32_t batch, const fl
 
 /* KH99 inside pass that allocates nothing (no counterpart in the reference;
  * computeinsideKH99 always allocates its tables).  For callers that must not
- * call cudaMalloc -- code running under CUDA stream capture, inside a
- * framework that owns the device allocator, or in a loop that must not enter
- * the driver's allocator.  Inputs and output are DEVICE pointers; the work is
- * queued on `stream` (a cudaStream_t) of the current device:
+ * call cudaMalloc -- code inside a framework that owns the device allocator,
+ * or a loop that must not enter the driver's allocator (whose calls can
+ * synchronise the device).  Inputs and output are DEVICE pointers; the work
+ * is queued on `stream` (a cudaStream_t) of the current device:
  *   d_unpaired [L] doubles, d_paired [L x L] column-major doubles, d_Z one
  *   double.  maxspan as in messi_inside (< 0 infers it, which synchronises
- *   `stream` once to read the span back).
+ *   `stream` once to read the span back, and returns MESSI_EINVAL on a
+ *   stream that is being captured).
  * Scratch lives in one fixed file-scope device array (about 25 MB per GPU
  * that loads the library, held until exit): each of its six band tables
  * holds L * RS <= 2^20 floats, RS = 32 * ceil((maxspan + 1) / 32), and
  * L <= 16384; larger problems return MESSI_ETOOBIG.  Every call shares that
  * array, so calls that overlap on the GPU race; serialise them.  The first
- * call on a device resolves the array's address (set-up) and should come
- * before any stream capture. */
+ * call on a device (and the first in a new CUDA context of that device)
+ * resolves the array's address (set-up) and should come before any stream
+ * capture.  The kernels run after the call returns: a bounded device wait
+ * that gives up shows only as *d_Z == NaN (the return value is MESSI_OK), so
+ * callers check Z. */
 int messi_inside_noalloc(void* stream, int32_t L, const double* d_unpaired, const double* d_paired, int32_t maxspan,
                          double B, double* d_Z);
 

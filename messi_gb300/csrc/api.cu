@@ -697,6 +697,9 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     key.staged = md.stage_bytes;
     key.epoch = ctx->alloc_epoch;
     key.arena_gen = ds->arena_gen;
+    key.wave_ctas = ctx->wave_ctas;
+    key.wave_threads = ctx->wave_threads;
+    key.prune_shape = ctx->prune_shape;
     const bool graphs = ctx->graphs && !ctx->profiling;
     bool replay = graphs && ctx->lgraph.exec && ctx->lgraph.key == key;
     if (!replay && graphs && ctx->lgraph.seen == key) replay = capture_likelihood(ctx, ds, md, t, key);

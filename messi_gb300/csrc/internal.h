@@ -144,10 +144,13 @@ struct LikelihoodKey {
     bool gapmask = false;
     size_t staged = 0;
     uint64_t epoch = 0, arena_gen = 0;
+    // launch shapes the captured sequence was recorded with
+    int wave_ctas = -1, wave_threads = -1, prune_shape = -1;
     bool operator==(const LikelihoodKey& o) const
     {
         return ds == o.ds && C == o.C && nsite == o.nsite && nlam == o.nlam && Wb == o.Wb && lamF == o.lamF &&
-               gapmask == o.gapmask && staged == o.staged && epoch == o.epoch && arena_gen == o.arena_gen;
+               gapmask == o.gapmask && staged == o.staged && epoch == o.epoch && arena_gen == o.arena_gen &&
+               wave_ctas == o.wave_ctas && wave_threads == o.wave_threads && prune_shape == o.prune_shape;
     }
 };
 struct LikelihoodGraph {

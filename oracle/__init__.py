@@ -10,7 +10,14 @@ arm).  The product package ``messi_gb300`` never imports it.
 * ``oracle.oracle_np`` -- an independent numpy/pure-Python restatement for
   tiny cases, used to cross-check the C oracle.
 
-Parity anchor: the reference ships no golden vectors and cannot run here (it is
-Julia), so the oracle is pinned by derived known-answer tests
-(tests/test_oracle.py) and by the agreement of the two restatements.
+Parity anchor: the reference ships no golden vectors and its host language
+(Julia) is absent, but its CUDA kernels (src/cuda/felsenstein.cu, inside.cu)
+compile unmodified (``make -C oracle ref``, replayed by
+``oracle.ref_kernels``).  Their outputs on seeded inputs are committed as
+fixtures (tests/golden/reference_outputs.npz, written by
+tests/golden/make_reference_fixtures.py) and the CPU suite checks the oracle
+against them (tests/test_reference_fixtures.py): pair matrices, inside Z and
+tables, outside tables and the posterior decoding bit for bit.  Derived
+known-answer tests (tests/test_oracle.py) and the agreement of the two
+restatements cover what the kernels do not.
 """
