@@ -144,6 +144,19 @@ def whole_job_rate(units_per_rank, steps, max_ms, ws):
     return ws * units_per_rank * steps / (max_ms / 1e3)
 
 
+def workload_config(workload, npairs, ws):
+    """The `config` object both arms print (identical, so the two lines
+    describe the same workload)."""
+    return {"workload": WORKLOAD_TEXT[workload] + ", 45 categories (3 x 3 site rates x 5 lambda; the 9 with "
+                        "lambda = 1 are the product of two unpaired columns, as in the reference's CPU path), "
+                        "synthetic from seed, 5% gaps",
+            "pairs_per_step": npairs,
+            "step": "unpaired columns + pair pruning + gap mask + inside pass -> Z",
+            "l2": "GPU arm: L2 flushed between steps (256 MB write outside the timed events); CPU arm: host "
+                  "caches not flushed",
+            "parallelism": f"replicas x{ws}"}
+
+
 def make_params(s, count, seed):
     """`count` parameter vectors around the workload's generating vector (the
     moves an MCMC chain makes); discretised on the host like getparams."""
@@ -160,45 +173,70 @@ def make_params(s, count, seed):
     return out
 
 
-def cpu_oracle_rate(s, rows, nthreads):
-    """FP64 CPU restatement timed on a bounded sample: pair pruning for a block
-    of rows, plus the full unpaired and inside passes pro-rated to the sample.
-    The lambda = 1 categories take the product of the unpaired columns, as the
-    reference's CPU path does (src/FARCE.jl:1891-1901)."""
+def fp64_step(s, nthreads, rows=None):
+    """One evaluation by the FP64 CPU restatement of the reference's CPU path
+    (oracle/): unpaired columns, pair pruning of every pair in the band (the
+    lambda = 1 categories as the product of the unpaired columns, as
+    src/FARCE.jl:1891-1901 does), maskgapped!, and the dense inside pass
+    (computeinsideparallel, src/InsideOutsideAlgorithm.jl:682-749).  rows =
+    (x0, x1) restricts the pairs to a block of alignment rows (a warm-up
+    sample).  Returns (seconds, Z, u, masked pair matrix, pairs evaluated)."""
     import numpy as np
 
     from oracle import c_oracle as co
     from oracle import model_ref as mr
     ds = s.dataset
+    t0 = time.perf_counter()
     rp = mr.getparams(s.params15, ds.branchlengths)
     P, pi16, logw, _, l1, s1, s2 = mr.pair_categories(rp)
-    t0 = time.perf_counter()
     u, ubs = mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
-    t_unp = time.perf_counter() - t0
-    t0 = time.perf_counter()
     p, _ = co.pair_matrix(ds.children, ds.seqindex, ds.masks, P, pi16, logw, s.W, rows=rows, nthreads=nthreads,
                           lambda1_cat=l1, u_by_site=ubs, site1=s1, site2=s2)
-    t_pairs = time.perf_counter() - t0
-    sample = int(np.isfinite(p[np.triu_indices(ds.numcols, 1)]).sum())
-    return u, t_unp, t_pairs, sample
+    pm = co.maskgapped(p, ds.gapfrequency, 1.0)
+    Z = float(co.inside(u, pm, 1.0, nthreads=nthreads)[0, 0, ds.numcols - 1])
+    dt = time.perf_counter() - t0
+    npairs = int(np.isfinite(p[np.triu_indices(ds.numcols, 1)]).sum())
+    return dt, Z, u, pm, npairs
 
 
-def cpu_inside_time(u, W, L, nthreads):
+def parity_against_fp64(ctx, s, h, Z_ref, u_ref, pm_ref):
+    """Errors of the timed GPU path against the FP64 chain on the same
+    workload and parameters (outside the timed region): Z of
+    messi_likelihood, every pair log-likelihood, and the base-pairing
+    posteriors of the GPU chain (messi_posteriors on the GPU's scores) against
+    those of the FP64 chain (banded FP64 inside/outside/posteriors on the
+    FP64 scores; equal to the dense chain, which the CPU tests pin)."""
     import numpy as np
 
+    from messi_gb300 import api
+    from messi_gb300 import model as M
     from oracle import c_oracle as co
-    rng = np.random.default_rng(0)
-    p = np.full((L, L), -np.inf)
-    for i in range(L):
-        j = np.arange(i + 1, min(L, i + W + 1))
-        p[i, j] = u[i] + u[j] + rng.normal(-3, 4, len(j))
-    p = np.triu(p, 1)
-    p = p + p.T
-    p[np.tril_indices(L)] = -np.inf
-    p = np.maximum(p, p.T)
-    t0 = time.perf_counter()
-    co.inside(u, p, 1.0, nthreads=nthreads)
-    return time.perf_counter() - t0
+    ds = s.dataset
+    prm = M.getparams(s.params15, ds.branchlengths)
+    m = api.ModelArgs(prm)
+    gf = np.ascontiguousarray(ds.gapfrequency, np.float64)
+    import ctypes
+    Zc = ctypes.c_double()
+    ctx.check(ctx.lib.messi_likelihood(ctx.handle, h.handle, ctypes.byref(m.struct),
+                                       gf.ctypes.data_as(ctypes.c_void_p), 1.0, ctypes.byref(Zc), None),
+              "messi_likelihood")
+    u = api.computeunpairedlikelihoods(ds, prm, ctx=ctx)
+    mat, _ = api.felsensteincuda(ds, prm, None, s.W, ctx=ctx)
+    api.maskgapped(mat, ds.gapfrequency, 1.0, -np.inf)
+    fin = np.isfinite(pm_ref)
+    same_pattern = bool(np.array_equal(fin, np.isfinite(mat)))
+    pair_err = float((np.abs(mat[fin] - pm_ref[fin]) / np.maximum(np.abs(pm_ref[fin]), 1.0)).max())
+    _, single, pair = api.computeposteriors(u, mat, maxspan=s.W, ctx=ctx)
+    _, s_ref, up_ref, lo_ref = co.posteriors_banded(u_ref, pm_ref, s.W)
+    up, lo = co.band_of(pair, s.W)
+    post_err = max(float(np.abs(single - s_ref).max()), float(np.abs(up - up_ref).max()),
+                   float(np.abs(lo - lo_ref).max()))
+    return {"rel_loglik_err": abs(Zc.value - Z_ref) / abs(Z_ref), "Z": Zc.value, "Z_fp64": Z_ref,
+            "max_pair_loglik_rel_err": pair_err, "pair_pattern_equal": same_pattern,
+            "max_unpaired_rel_err": float(np.max(np.abs(u - u_ref) / np.abs(u_ref))),
+            "max_posterior_err": post_err,
+            "against": "FP64 CPU chain (oracle/) on the same workload and parameters: unpaired, all pairs, "
+                       "maskgapped, dense inside; posteriors from the FP64 scores"}
 
 
 def reference_gpu_rate(s, npairs):
@@ -217,13 +255,20 @@ def reference_gpu_rate(s, npairs):
         plan = rk.index_plan(ds.children, ds.seqindex, ds.masks, s.W)
         u, _ = mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
         tp, ti = {}, {}
+        t0 = time.perf_counter()
+        mr.unpaired_loglik(ds.tree_arrays(), ds.masks, rp)
+        t_unp = 1e3 * (time.perf_counter() - t0)
         p = rk.pair_matrix(ds.children, ds.seqindex, ds.masks, P, pi16, logw, s.W, plan=plan, timing=tp)
         p = co.maskgapped(p, ds.gapfrequency, 1.0)
         Zr, _ = rk.inside(u, p, timing=ti)
-        return {"value": npairs / ((tp["ms"] + ti["ms"]) / 1e3), "unit": UNIT, "pairs_ms": tp["ms"],
-                "inside_ms": ti["ms"], "Z": Zr,
-                "kind": "reference CUDA kernels compiled unmodified for sm_103a, Julia launch sequence replayed "
-                        "(oracle/ref_kernels.py); unpaired pass on the host excluded"}
+        total = tp["ms"] + ti["ms"] + t_unp
+        return {"value": npairs / (total / 1e3), "unit": UNIT, "kind": "reference",
+                "impl": "the reference's CUDA kernels (src/cuda/felsenstein.cu, inside.cu) compiled unmodified "
+                        "for sm_103a, its Julia launch sequence replayed (oracle/ref_kernels.py), on this GPU; "
+                        "unpaired columns on the host in FP64 as the reference does",
+                "same_workload": True, "pairs_ms": tp["ms"], "inside_ms": ti["ms"], "unpaired_ms": t_unp,
+                "ms_per_step": total, "Z": Zr,
+                "ours_vs_this": None}
     except Exception as exc:  # the reference path is a reported baseline only
         return {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
 
@@ -233,6 +278,12 @@ def total_pairs(L, W):
 
 
 def run_reference(args):
+    """The reference arm: the reference's path cannot run here (Julia is
+    absent), so its FP64 CPU restatement (oracle/, kind "port") evaluates the
+    full workload on every host core, one whole evaluation per timed step.
+    Warm-up is one small sample (a block of rows) whatever --warmup says:
+    CPU code has no JIT or caches worth warming, and full warm-up steps
+    would only lengthen the run."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -241,29 +292,24 @@ def run_reference(args):
     L, W = s.dataset.numcols, s.W
     npairs = total_pairs(L, W)
     nthreads = os.cpu_count() or 1
-    rows_per_step = 16
-    u, t_unp, _, _ = cpu_oracle_rate(s, (0, 1), nthreads)
-    t_in = cpu_inside_time(u, W, L, nthreads)
-    times, samples = [], []
-    for k in range(args.warmup + args.steps):
-        x0 = (k * rows_per_step) % (L - rows_per_step)
-        _, _, t_pairs, sample = cpu_oracle_rate(s, (x0, x0 + rows_per_step), nthreads)
-        frac = sample / npairs
-        if k >= args.warmup:
-            times.append(t_pairs + (t_unp + t_in) * frac)
-            samples.append(sample)
-    value = sum(samples) / sum(times)
+    fp64_step(s, nthreads, rows=(0, 8))
+    times = []
+    Z = None
+    for k in range(args.steps):
+        dt, Z, _, _, n = fp64_step(s, nthreads)
+        assert n == npairs, (n, npairs)
+        times.append(dt)
+    value = npairs * len(times) / sum(times)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories (lambda = 1 factorised, as the "
-                               "reference's CPU path does)",
-                   "pairs_per_full_step": npairs},
+        "config": workload_config(args.workload, npairs, ws),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{rows_per_step} alignment rows of pairs per step (~{int(statistics.mean(samples))} "
-                                   f"pairs) with the unpaired and inside passes pro-rated by pair fraction"},
+                         "sample": f"the full workload every step ({npairs} pairs, unpaired columns, gap mask, "
+                                   f"dense inside pass); warm-up: one 8-row block of pairs"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "Z": Z,
     }
     print(json.dumps(line), flush=True)
 
@@ -321,14 +367,20 @@ def run_ours(args):
     launches = 0
     barrier()
     torch.cuda.synchronize()
+    t_flush = t_call = 0.0
     with Clocks(local) as clk:
         t_wall = time.perf_counter()
         for k in range(args.steps):
+            a = time.perf_counter()
             flush.zero_()
             torch.cuda.synchronize()
+            b = time.perf_counter()
             ev[k][0].record(stream)
             launches += step(margs[args.warmup + k])
             ev[k][1].record(stream)
+            c = time.perf_counter()
+            t_flush += b - a
+            t_call += c - b
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
     barrier()
@@ -336,6 +388,11 @@ def run_ours(args):
     ms = max_over_ranks(sum(per), ws)
     ms_per_step = ms / args.steps
     value = whole_job_rate(npairs, args.steps, ms, ws)
+    # host wall clock of the timed loop: the L2 flush and its synchronise
+    # (outside the events) and the messi_likelihood call, which returns after
+    # its stream synchronise (host staging + device work + Z read-back)
+    wall = {"ms_per_step": 1e3 * t_wall / args.steps, "flush_ms_per_step": 1e3 * t_flush / args.steps,
+            "call_ms_per_step": 1e3 * t_call / args.steps}
 
     # ---- kernel-level timing pass (event pairs around each pruning launch)
     ctx.profile(True)
@@ -385,33 +442,30 @@ def run_ours(args):
     d2h = L * 8 + L * L * 8 + 8
     e2e_value = whole_job_rate(npairs, 1, 1e3 * max_over_ranks(statistics.mean(t_e2e), ws), ws)
 
-    # ---- CPU baseline (rank 0, single process)
-    cpu = None
+    # ---- CPU baseline and parity (rank 0, single process): one full FP64
+    # evaluation of the same workload, whose outputs also check the GPU path
+    cpu = parity = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        rows = 24
-        u_c, t_unp, t_pairs, sample = cpu_oracle_rate(s, (0, rows), nthreads)
-        t_in = cpu_inside_time(u_c, W, L, nthreads)
-        t_full = t_pairs * npairs / sample + t_unp + t_in
-        cpu = {"value": npairs / t_full, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": f"pairs of the first {rows} alignment rows ({sample} pairs, {t_pairs:.1f} s) extrapolated "
-                         f"to {npairs} pairs, plus full unpaired ({t_unp:.2f} s) and inside ({t_in:.1f} s) passes"}
+        t_full, Z_ref, u_ref, pm_ref, n_cpu = fp64_step(s, nthreads)
+        cpu = {"value": n_cpu / t_full, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"one full evaluation ({n_cpu} pairs, unpaired columns, gap mask, dense inside pass; "
+                         f"{t_full:.1f} s)"}
+        parity = parity_against_fp64(ctx, s, h, Z_ref, u_ref, pm_ref)
 
-    # ---- the reference's own CUDA kernels on the same GPU (launch sequence replayed)
+    # ---- second baseline: the reference's own CUDA kernels on this GPU
     refgpu = None
     if rank == 0 and ws == 1 and not args.no_reference_gpu:
         refgpu = reference_gpu_rate(s, npairs)
+        if refgpu.get("value"):
+            refgpu["ours_vs_this"] = {"value": value / refgpu["value"], "e2e": e2e_value / refgpu["value"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories "
-                               "(3 x 3 site rates x 5 lambda; the 9 with lambda = 1 factorised into unpaired "
-                               "columns), synthetic from seed, 5% gaps",
-                   "pairs_per_step": npairs, "step": "unpaired + pair pruning + gap mask + banded inside -> Z",
-                   "l2": "flushed between steps (256 MB write outside the timed events)",
-                   "parallelism": f"replicas x{ws}", "plan": stats},
+        "config": workload_config(args.workload, npairs, ws),
+        "plan": stats,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "chain": "computeunpairedlikelihoods + felsensteincuda + maskgapped + computeinsideKH99"},
         "gpu_launches": launches,
@@ -419,10 +473,11 @@ def run_ours(args):
         "inside": {"cells_per_s": band_cells / (inside_ms / 1e3) if inside_ms > 0 else None,
                    "band_cells": band_cells, "full_triangle_cells": L * (L + 1) // 2,
                    "ms_per_pass": inside_ms, "launches_per_pass": (i_n + s_n) / nprof},
-        "wall_ms_per_step": 1e3 * t_wall / args.steps,
+        "wall": wall,
         "clocks": clk.summary(),
+        "parity": parity,
         "cpu_baseline": cpu,
-        "reference_gpu": refgpu,
+        "baseline_gpu": refgpu,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -651,7 +706,7 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.steps is None:
-        args.steps = 3 if args.batch else (5 if args.structures else 100)
+        args.steps = 3 if args.batch else (5 if args.structures or args.impl == "reference" else 100)
     if args.mcmc:
         run_mcmc(args)
     elif args.batch:

@@ -55,12 +55,15 @@ def lib():
             L.mo_inside.argtypes = [_f64p, _f64pF, c_int, c_double, _f64pF, c_int]
             L.mo_inside_banded.argtypes = [_f64p, _f64pF, c_int, c_int, c_double, ctypes.POINTER(c_double), c_int]
             L.mo_outside.argtypes = [_f64pF, _f64p, _f64pF, c_int, _f64pF, c_int]
+            L.mo_posteriors_banded.argtypes = [_f64p, _f64pF, c_int, c_int, ctypes.POINTER(c_double), _f64p, _f64p,
+                                               _f64p, c_int]
             _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
             L.mo_posterior_decoding.argtypes = [_f32p, _f32p, c_int, ctypes.c_float, _f32p, _i32p]
             L.mo_posterior_traceback.argtypes = [_i32p, c_int, _i32p]
             L.mo_basepairprobs.argtypes = [_f64pF, _f64pF, _f64p, _f64pF, c_int, _f64p, _f64pF]
             for name in ("mo_reversible_eig", "mo_transition_matrices", "mo_subcolumnrefs", "mo_pair_matrix",
                          "mo_unpaired", "mo_inside", "mo_inside_banded", "mo_outside", "mo_basepairprobs",
+                         "mo_posteriors_banded",
                          "mo_posterior_decoding", "mo_posterior_traceback"):
                 getattr(L, name).restype = c_int
             _lib = L
@@ -196,6 +199,39 @@ def inside_banded_Z(u, p, W, B=1.0, nthreads=0):
     _check(lib().mo_inside_banded(u, np.asfortranarray(p, np.float64), len(u), int(W), float(B), ctypes.byref(Z),
                                   int(nthreads)), "inside_banded")
     return Z.value
+
+
+def posteriors_banded(u, p, W, nthreads=0):
+    """Banded inside -> outside -> posteriors (B = 1; pairs of span > W must
+    be -Inf in p).  Returns (Z, single[L], up, lo): up[x, d] / lo[x, d] are
+    the row-normalised posteriors of the pairs (x, x + d) / (x - d, x) in
+    row x, d = 1..W (index 0 unused)."""
+    u = np.ascontiguousarray(u, np.float64)
+    L = len(u)
+    W = max(0, min(int(W), L - 1))
+    Z = ctypes.c_double()
+    single = np.zeros(L)
+    up = np.zeros(L * (W + 1))
+    lo = np.zeros(L * (W + 1))
+    _check(lib().mo_posteriors_banded(u, np.asfortranarray(p, np.float64), L, W, ctypes.byref(Z), single, up, lo,
+                                      int(nthreads)), "posteriors_banded")
+    return Z.value, single, up.reshape(L, W + 1), lo.reshape(L, W + 1)
+
+
+def band_of(pair, W):
+    """(up, lo) band views of a dense L x L posterior matrix, the layout of
+    posteriors_banded."""
+    pair = np.asarray(pair)
+    L = pair.shape[0]
+    W = max(0, min(int(W), L - 1))
+    up = np.zeros((L, W + 1))
+    lo = np.zeros((L, W + 1))
+    x = np.arange(L)
+    for d in range(1, W + 1):
+        k = x[: L - d]
+        up[k, d] = pair[k, k + d]
+        lo[k + d, d] = pair[k + d, k]
+    return up, lo
 
 
 def outside(ins, u, p, nthreads=0):

@@ -56,6 +56,21 @@ static double lse2(double a, double b)
 
 double mo_logsumexp(double a, double b) { return lse2(a, b); }
 
+/* log of a sum of n terms given as logs: max + log(sum exp(t - max)).  The
+ * same value as folding lse2 over the terms, with one exp per term instead
+ * of an exp and a log1p. */
+static double mo_lse_terms(const double* t, int n)
+{
+    double m = -INFINITY;
+    for (int k = 0; k < n; k++)
+        if (t[k] > m) m = t[k];
+    if (m == -INFINITY) return -INFINITY;
+    double s = 0.0;
+    for (int k = 0; k < n; k++) s += exp(t[k] - m);
+    return m + log(s);
+}
+
+
 /* ---------------------------------------------------------------------- */
 /* Substitution models: src/RateMatrices.jl                               */
 /* ---------------------------------------------------------------------- */
@@ -743,11 +758,14 @@ int mo_inside_banded(const double* u, const double* p, int L, int W, double B, d
     (void)nthreads;
 #endif
     for (int d = 1; d <= W; d++) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel
+        {
+        double* terms = (double*)malloc(sizeof(double) * W1);
+#pragma omp for schedule(static)
         for (int i = 0; i < L - d; i++) {
             int j = i + d;
-            double tmp = -INFINITY;
-            for (int k = 0; k < d; k++) tmp = lse2(tmp, Lt[i * W1 + k] + S[(size_t)(i + k + 1) * W1 + (d - 1 - k)]);
+            for (int k = 0; k < d; k++) terms[k] = Lt[i * W1 + k] + S[(size_t)(i + k + 1) * W1 + (d - 1 - k)];
+            double tmp = mo_lse_terms(terms, d);
             double fin = (d >= 2) ? F[(size_t)(i + 1) * W1 + (d - 2)] : -INFINITY;
             double pij = p[i + (size_t)j * L];
             double s = lse2(-INFINITY, r[0] * B + tmp);
@@ -759,17 +777,188 @@ int mo_inside_banded(const double* u, const double* p, int L, int W, double B, d
             Lt[i * W1 + d] = lse2(-INFINITY, (r[6] + pij) * B + fin);
             if (j == L - 1) suf[i] = s;
         }
+        free(terms);
+        }
     }
-    for (int i = L - 2 - W; i >= 0; i--) {
-        double tmp = -INFINITY;
-        for (int k = 0; k <= W; k++) tmp = lse2(tmp, Lt[i * W1 + k] + suf[i + k + 1]);
-        suf[i] = r[0] * B + tmp;
+    {
+        double* terms = (double*)malloc(sizeof(double) * W1);
+        for (int i = L - 2 - W; i >= 0; i--) {
+            for (int k = 0; k <= W; k++) terms[k] = Lt[i * W1 + k] + suf[i + k + 1];
+            suf[i] = r[0] * B + mo_lse_terms(terms, W + 1);
+        }
+        free(terms);
     }
     *Zout = suf[0];
     free(S);
     free(F);
     free(Lt);
     free(suf);
+    return MO_OK;
+}
+
+/*
+ * Banded inside -> outside -> base-pairing posteriors (FP64, B = 1): the
+ * chain computeinside / computeoutside / computebasepairprobs
+ * (src/InsideOutsideAlgorithm.jl:682-749, 447-483, 486-533) restricted to
+ * pairs of span <= W, for genome-scale checks where the dense O(L^3) tables
+ * are out of reach.  With every pair of span > W at -Inf, the only cells
+ * beyond the band that carry probability are the S cells of the last column
+ * (an S->LS chain ends at j = L-1), inside and outside; F and L need an
+ * enclosing or own pair.  The outside recurrences are the adjoints of the
+ * inside ones, written with A(i,j) = log(e^{OS(i,j)+r1} + e^{OF(i,j)+r5})
+ * (the two LS parents):
+ *   OS(k,j) = lse_{i<k} A(i,j) + L(i,k-1)
+ *   OL(k,h) = lse_{j>h} A(k,j) + S(h+1,j)
+ *   OF(k,j) = lse_{X in S,F,L} OX(k-1,j+1) + r_X(dFd) + p(k-1,j+1)
+ * with OS(0,L-1) = 0.  Sums of many terms are taken as max + log(sum exp).
+ * Outputs: Z; single[L]; up[x][d] = normalised posterior of the pair
+ * (x, x+d) in row x and lo[x][d] that of (x-d, x) in row x (d = 1..W, rows
+ * of W+1 entries, 0 outside the matrix), after the per-row normalisation of
+ * computebasepairprobs.  tests/test_oracle.py pins it to the dense chain.
+ */
+int mo_posteriors_banded(const double* u, const double* p, int L, int W, double* Zout, double* single, double* up,
+                         double* lo, int nthreads)
+{
+    double r[7];
+    mo_kh99_logprobs(r);
+    if (L < 1) return MO_EINVAL;
+    if (W > L - 1) W = L - 1;
+    if (W < 0) W = 0;
+    const size_t W1 = (size_t)W + 1, n = (size_t)L * W1;
+    double* buf = (double*)malloc(sizeof(double) * (7 * n + 2 * (size_t)L));
+    if (!buf) return MO_ENOMEM;
+    double *S = buf, *F = S + n, *Lt = F + n, *OS = Lt + n, *OF = OS + n, *OL = OF + n, *A = OL + n;
+    double *Scol = A + n, *OScol = Scol + L;
+    for (size_t k = 0; k < 7 * n + 2 * (size_t)L; k++) buf[k] = -INFINITY;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    /* inside, band */
+    for (int i = 0; i < L; i++) {
+        S[i * W1] = u[i] + r[1];
+        Lt[i * W1] = u[i] + r[5];
+    }
+    for (int d = 1; d <= W; d++) {
+#pragma omp parallel
+        {
+            double* t = (double*)malloc(sizeof(double) * (W1 + 1));
+#pragma omp for schedule(static)
+            for (int i = 0; i < L - d; i++) {
+                const int j = i + d;
+                for (int k = 0; k < d; k++) t[k] = Lt[i * W1 + k] + S[(size_t)(i + k + 1) * W1 + (d - 1 - k)];
+                const double tmp = mo_lse_terms(t, d);
+                const double fin = (d >= 2) ? F[(size_t)(i + 1) * W1 + (d - 2)] : -INFINITY;
+                const double pij = p[i + (size_t)j * L];
+                S[i * W1 + d] = lse2(r[0] + tmp, (r[2] + pij) + fin);
+                F[i * W1 + d] = lse2(r[4] + tmp, (r[3] + pij) + fin);
+                Lt[i * W1 + d] = (r[6] + pij) + fin;
+            }
+            free(t);
+        }
+    }
+    /* inside, S cells of the last column (band, then the suffix beyond it) */
+    for (int i = L - 1; i >= 0 && L - 1 - i <= W; i--) Scol[i] = S[i * W1 + (L - 1 - i)];
+    {
+        double* t = (double*)malloc(sizeof(double) * (W1 + 1));
+        for (int i = L - 2 - W; i >= 0; i--) {
+            for (int k = 0; k <= W; k++) t[k] = Lt[i * W1 + k] + Scol[i + k + 1];
+            Scol[i] = r[0] + mo_lse_terms(t, W + 1);
+        }
+        free(t);
+    }
+    const double Z = Scol[0];
+    *Zout = Z;
+    /* outside: the last column beyond the band (increasing start) */
+    OScol[0] = 0.0;
+    {
+        double* t = (double*)malloc(sizeof(double) * (W1 + 1));
+        for (int k = 1; k < L - 1 - W; k++) {
+            int m = 0;
+            for (int i = (k - 1 - W > 0 ? k - 1 - W : 0); i <= k - 1; i++) t[m++] = OScol[i] + r[0] + Lt[i * W1 + (k - 1 - i)];
+            OScol[k] = mo_lse_terms(t, m);
+        }
+        free(t);
+    }
+    /* outside, band, decreasing span */
+    for (int d = W; d >= 0; d--) {
+#pragma omp parallel
+        {
+            double* t = (double*)malloc(sizeof(double) * (W1 + 2));
+#pragma omp for schedule(static)
+            for (int k = 0; k <= L - 1 - d; k++) {
+                const int j = k + d;
+                double os;
+                if (k == 0 && j == L - 1) {
+                    os = 0.0;
+                } else {
+                    int m = 0;
+                    for (int i = (k - 1 - W > 0 ? k - 1 - W : 0); i <= k - 1; i++) {
+                        double a;
+                        if (j - i <= W) a = A[i * W1 + (j - i)];
+                        else if (j == L - 1) a = OScol[i] + r[0];
+                        else a = -INFINITY;
+                        t[m++] = a + Lt[i * W1 + (k - 1 - i)];
+                    }
+                    os = mo_lse_terms(t, m);
+                }
+                double of = -INFINITY;
+                if (k >= 1 && j + 1 < L && d + 2 <= W) {
+                    const size_t q = (size_t)(k - 1) * W1 + (d + 2);
+                    const double pp = p[(size_t)(k - 1) + (size_t)(j + 1) * L];
+                    double tt[3] = {OS[q] + r[2] + pp, OF[q] + r[3] + pp, OL[q] + r[6] + pp};
+                    of = mo_lse_terms(tt, 3);
+                }
+                double ol;
+                {
+                    int m = 0;
+                    const int jmax = (k + W < L - 1) ? k + W : L - 1;
+                    for (int jj = j + 1; jj <= jmax; jj++) t[m++] = A[k * W1 + (jj - k)] + S[(size_t)(j + 1) * W1 + (jj - j - 1)];
+                    if (L - 1 > k + W) t[m++] = OScol[k] + r[0] + Scol[j + 1];
+                    ol = mo_lse_terms(t, m);
+                }
+                OS[k * W1 + d] = os;
+                OF[k * W1 + d] = of;
+                OL[k * W1 + d] = ol;
+                A[k * W1 + d] = lse2(os + r[0], of + r[4]);
+                if (j == L - 1) OScol[k] = os;
+            }
+            free(t);
+        }
+    }
+    /* posteriors (log), then the global max shift and row normalisation */
+    double m = -INFINITY;
+    for (int j = 0; j < L; j++) {
+        single[j] = lse2(OS[j * W1] + r[1], OL[j * W1] + r[5]) + u[j] - Z;
+        if (single[j] > m) m = single[j];
+    }
+    for (size_t k = 0; k < n; k++) up[k] = lo[k] = -INFINITY;
+    for (int j = 0; j < L; j++)
+        for (int d = 1; d <= W && j + d < L; d++) {
+            const size_t q = (size_t)j * W1 + d;
+            const double fin = (d >= 2) ? F[(size_t)(j + 1) * W1 + (d - 2)] : -INFINITY;
+            double tt[3] = {OS[q] + r[2], OF[q] + r[3], OL[q] + r[6]};
+            const double v = mo_lse_terms(tt, 3) + fin + p[(size_t)j + (size_t)(j + d) * L] - Z;
+            up[q] = v;
+            lo[(size_t)(j + d) * W1 + d] = v;
+            if (v > m) m = v;
+        }
+    for (int j = 0; j < L; j++) single[j] = exp(single[j] - m);
+    for (size_t k = 0; k < n; k++) {
+        up[k] = exp(up[k] - m);
+        lo[k] = exp(lo[k] - m);
+    }
+    for (int x = 0; x < L; x++) {
+        double s = single[x];
+        for (int d = 1; d <= W; d++) s += up[(size_t)x * W1 + d] + lo[(size_t)x * W1 + d];
+        single[x] /= s;
+        for (int d = 0; d <= W; d++) {
+            up[(size_t)x * W1 + d] /= s;
+            lo[(size_t)x * W1 + d] /= s;
+        }
+    }
+    free(buf);
     return MO_OK;
 }
 

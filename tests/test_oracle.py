@@ -247,3 +247,24 @@ def test_posterior_decoding_equals_brute_force(L):
     for i in range(L):
         if paired[i]:
             assert paired[paired[i] - 1] == i + 1
+
+
+@pytest.mark.parametrize("L,W", [(1, 0), (2, 1), (9, 8), (40, 12), (60, 59), (130, 40), (200, 20)])
+def test_banded_posterior_chain_matches_dense(L, W):
+    """The banded inside -> outside -> posterior chain (used at genome scale)
+    equals the dense chain when every pair beyond the band is -Inf."""
+    rng = np.random.default_rng(L * 7 + W)
+    u = rng.uniform(-80.0, -20.0, L)
+    p = np.full((L, L), -np.inf)
+    for i in range(L):
+        j = np.arange(i + 1, min(L, i + W + 1))
+        p[i, j] = u[i] + u[j] + rng.normal(-3.0, 4.0, len(j)) + (rng.random(len(j)) < 0.05) * 25.0
+    p = np.maximum(p, p.T)
+    ins = co.inside(u, p)
+    outs = co.outside(ins, u, p)
+    s_ref, p_ref = co.basepairprobs(ins, outs, u, p)
+    Z, s, up, lo = co.posteriors_banded(u, p, W)
+    up_ref, lo_ref = co.band_of(p_ref, W)
+    assert abs(Z - ins[0, 0, L - 1]) <= 1e-12 * max(1.0, abs(Z))
+    assert np.abs(s - s_ref).max() <= 1e-11
+    assert np.abs(up - up_ref).max() <= 1e-11 and np.abs(lo - lo_ref).max() <= 1e-11
