@@ -535,7 +535,8 @@ int messi_dataset_destroy(messi_dataset* ds)
         }
     }
     void* bufs[] = {ds->d_bandidx, ds->d_lr, ds->d_leaf, ds->d_nodes, ds->d_tiles, ds->d_masks, ds->d_tree,
-                    ds->d_post, ds->d_arena_f, ds->d_arena_e, ds->d_mix, ds->d_mixlam};
+                    ds->d_post, ds->d_arena_f, ds->d_arena_e, ds->d_mix, ds->d_mixlam, ds->d_leafnode,
+                    ds->d_leafmsg};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete ds;

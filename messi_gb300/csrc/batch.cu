@@ -41,6 +41,13 @@ struct messi_batch {
     int* d_arena_e = nullptr;
     std::vector<int64_t> row_base;
     int64_t total_rows = 0;
+    // leaf rows of every alignment, concatenated, with their global node ids,
+    // and the leaf messages of the current category pass
+    std::vector<int64_t> leaf_base;
+    int64_t total_leaf_rows = 0;
+    float* d_leafrows = nullptr;
+    int* d_leafnode = nullptr;
+    float* d_leafmsg = nullptr;
     int chunk = 0, arena_C = 0;
     BandBatch bands;
     DevBuf stage, P16, P4;
@@ -82,7 +89,8 @@ void destroy_batch(messi_batch* b)
     if (!b) return;
     for (messi_dataset* d : b->ds)
         if (d) messi_dataset_destroy(d);
-    void* bufs[] = {b->d_tiles, b->d_nodes, b->d_arena_f, b->d_arena_e, b->stage.p, b->P16.p, b->P4.p};
+    void* bufs[] = {b->d_tiles, b->d_nodes, b->d_arena_f, b->d_arena_e, b->stage.p, b->P16.p, b->P4.p,
+                    b->d_leafrows, b->d_leafnode, b->d_leafmsg};
     for (void* p : bufs)
         if (p) cudaFree(p);
     bandbatch_free(&b->bands);
@@ -96,16 +104,20 @@ int prepare_batch_arena(messi_ctx* ctx, messi_batch* b, int C)
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     const size_t row_bytes = 16 * sizeof(float) + sizeof(int);
+    const int64_t leaf_rows = std::max<int64_t>(b->total_leaf_rows, 1);
     int chunk = C;
-    while (chunk > 1 && (size_t)chunk * b->total_rows * row_bytes > freeb / 2) chunk = (chunk + 1) / 2;
+    while (chunk > 1 && (size_t)chunk * (b->total_rows + leaf_rows) * row_bytes > freeb / 2) chunk = (chunk + 1) / 2;
     if (b->d_arena_f) cudaFree(b->d_arena_f);
     if (b->d_arena_e) cudaFree(b->d_arena_e);
+    if (b->d_leafmsg) cudaFree(b->d_leafmsg);
     b->d_arena_f = nullptr;
     b->d_arena_e = nullptr;
+    b->d_leafmsg = nullptr;
     b->chunk = 0;
     cudaError_t e = cudaMalloc((void**)&b->d_arena_f, (size_t)chunk * b->total_rows * 16 * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_arena_e, (size_t)chunk * b->total_rows * sizeof(int));
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "batch partial arena");
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_leafmsg, (size_t)chunk * leaf_rows * 16 * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batch message arena");
     b->chunk = chunk;
     b->arena_C = C;
     b->desc_grp.clear();  // descriptors point into the old arena
@@ -117,8 +129,9 @@ int write_descriptors(messi_ctx* ctx, messi_batch* b, const std::vector<int>& gr
     if (b->desc_grp == grp) return MESSI_OK;
     b->nodes_host.assign(b->total_nodes, NodeDev{});
     for (int a = 0; a < b->n; a++)
-        fill_node_descriptors(b->ds[a], b->d_arena_f, b->d_arena_e, b->row_base[a], b->total_rows, b->node_base[a],
-                              grp[a], b->nodes_host.data() + b->node_base[a]);
+        fill_node_descriptors(b->ds[a], b->d_arena_f, b->d_arena_e, b->row_base[a], b->total_rows, b->d_leafmsg,
+                              b->leaf_base[a], std::max<int64_t>(b->total_leaf_rows, 1), b->node_base[a], grp[a],
+                              b->nodes_host.data() + b->node_base[a]);
     cudaError_t e = cudaMemcpyAsync(b->d_nodes, b->nodes_host.data(), sizeof(NodeDev) * b->total_nodes,
                                     cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batch node descriptors");
@@ -172,8 +185,11 @@ int messi_batch_create(messi_ctx* ctx, int32_t n, const messi_alignment* alns, c
     b->node_base.resize(n);
     b->col_base.resize(n);
     b->row_base.resize(n);
+    b->leaf_base.resize(n);
     for (int a = 0; a < n; a++) {
         const messi_dataset* d = b->ds[a];
+        b->leaf_base[a] = b->total_leaf_rows;
+        b->total_leaf_rows += d->leaf_rows;
         b->node_base[a] = b->total_nodes;
         b->total_nodes += d->numnodes;
         b->col_base[a] = b->total_cols;
@@ -213,6 +229,22 @@ int messi_batch_create(messi_ctx* ctx, int32_t n, const messi_alignment* alns, c
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_nodes, sizeof(NodeDev) * std::max(1, b->total_nodes));
+    {
+        // leaf rows of all alignments and their global node ids
+        const size_t R = (size_t)std::max<int64_t>(b->total_leaf_rows, 1);
+        std::vector<float> rows(R * 16, 0.f);
+        std::vector<int> rownode(R, 0);
+        for (int a = 0; a < n; a++) {
+            const messi_dataset* d = b->ds[a];
+            std::copy(d->leaf_host.begin(), d->leaf_host.begin() + (size_t)d->leaf_rows * 16,
+                      rows.begin() + (size_t)b->leaf_base[a] * 16);
+            for (int64_t r = 0; r < d->leaf_rows; r++) rownode[b->leaf_base[a] + r] = b->node_base[a] + d->leafnode_host[r];
+        }
+        if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_leafrows, R * 16 * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_leafnode, R * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemcpy(b->d_leafrows, rows.data(), R * 16 * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(b->d_leafnode, rownode.data(), R * sizeof(int), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) {
         destroy_batch(b);
         return cuda_fail(ctx, e, "batch upload");
@@ -379,6 +411,9 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     // pair pruning over the merged levels
     for (int c0 = 0; c0 < C; c0 += b->chunk) {
         const int nc = std::min(b->chunk, C - c0);
+        if ((rc = launch_leaf_messages(ctx, b->d_leafrows, b->d_leafnode, b->total_leaf_rows, d_P, b->total_nodes, c0,
+                                       nc, b->d_leafmsg)))
+            return rc;
         for (int lv = 1; lv <= b->H; lv++) {
             for (int root = 0; root < 2; root++) {
                 const int nt = root ? b->rtile_cnt[lv] : b->tile_cnt[lv];

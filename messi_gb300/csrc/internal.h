@@ -45,26 +45,30 @@ struct Staged {
     }
 };
 
-// Per-internal-node descriptor of one pruning step (device resident).
+// Per-internal-node descriptor of one pruning step (device resident).  Rows
+// are messages: the row a node sends to its parent is its partial likelihood
+// vector multiplied by its own branch's transition matrix, so a node update
+// is the elementwise product of its two children's messages followed by one
+// mat-vec (none at the root).
 struct NodeDev {
     const int* li;     // [n] row of the left child for each unique pair
     const int* ri;     // [n]
-    const float* lf;   // left child rows (16 floats each)
+    const float* lf;   // left child message rows (16 floats each)
     const int* le;     // left child exponents (nullptr for leaves: exponent 0)
-    long long lcs;     // left child category stride in rows (0 for leaves)
+    long long lcs;     // left child category stride in rows
     const float* rf;
     const int* re;
     long long rcs;
-    float* of;         // output rows (unused at the root)
+    float* of;         // output message rows (unused at the root)
     int* oe;
     long long ocs;
     double* mix;       // root only: [n] category mixture per unique root pair
     double* mixlam;    // root only: [kMaxLambda][n] per-lambda mixtures (nullable)
     double* catll;     // root only: [C][n] per-category log-likelihoods (nullable)
     int n;             // unique pairs at this node
-    int left;          // child node ids (index of their transition matrices)
-    int right;
+    int self;          // this node's id (index of its branch's transition matrices)
     int grp;           // model group (index of the category tables pi16/logw)
+    int pad;
 };
 
 // Discretised model categories built on the host for one call.
@@ -229,6 +233,11 @@ struct messi_dataset {
     std::vector<messi::NodeDev> nodes_host;
     std::vector<int64_t> lr_off;       // per internal node offset into d_lr (li at off, ri at off+n)
     std::vector<int64_t> leaf_off;     // per leaf offset (rows) into d_leaf
+    int64_t leaf_rows = 0;             // rows of d_leaf (unique pairs summed over the leaves)
+    std::vector<float> leaf_host;      // [leaf_rows][16] host copy of d_leaf
+    std::vector<int> leafnode_host;    // [leaf_rows] leaf node of each row
+    int* d_leafnode = nullptr;         // device copy of leafnode_host
+    float* d_leafmsg = nullptr;        // [chunk][leaf_rows][16] leaf messages of the current pass
 };
 
 namespace messi {
@@ -272,11 +281,14 @@ int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8
                const std::vector<int2>* pairs = nullptr, std::vector<int32_t>* pair_unique = nullptr);
 int allocate_arena(messi_dataset* ds, int C, std::string* err);
 
-// Node descriptors of one dataset whose partial rows live at `arena_f/e` +
-// row_base rows, category stride `cstride` rows; transition matrices of local
-// node v are those of node node_base + v; model group `grp`.
+// Node descriptors of one dataset whose message rows live at `arena_f/e` +
+// row_base rows, category stride `cstride` rows, and whose leaf messages live
+// at `leafmsg` + leaf_base rows, category stride `leaf_cstride` rows;
+// transition matrices of local node v are those of node node_base + v; model
+// group `grp`.
 void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e, int64_t row_base, int64_t cstride,
-                           int node_base, int grp, NodeDev* out);
+                           float* leafmsg, int64_t leaf_base, int64_t leaf_cstride, int node_base, int grp,
+                           NodeDev* out);
 
 // ---- pruning kernels (prune.cu) ----
 // nodegrp: [numnodes] model group of each node, -1 for a root (nullptr: one
@@ -287,6 +299,10 @@ int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, co
                      int C, float* d_P);
 int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, const int* d_nodegrp, int numnodes,
                     int nsite, double* d_P4);
+// Leaf messages of categories c0 .. c0+nc-1: out[cc][r] = P[c0+cc][rownode[r]]
+// x rows[r] for the R leaf rows (FP64 accumulation, stored FP32).
+int launch_leaf_messages(messi_ctx* ctx, const float* d_rows, const int* d_rownode, int64_t R, const float* d_P,
+                         int numnodes, int c0, int nc, float* d_out);
 // The tensor-core node update over `nt` tiles of one level (root tiles when root).
 int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
                        const float* d_P, int numnodes, int c0, int nc, int C, const float* d_pi16,

@@ -8,9 +8,15 @@
 //
 // Layout: three linear layers in -> H -> H -> out with SiLU after the first
 // two.  Weights are kept in FP32 (Adam master copy) and BF16 (the copy the
-// forward/backward kernels read); activations are BF16, every product is
-// accumulated in FP32.  The GEMMs are tiny (batch <= a few hundred, width
-// 256) and latency bound, so they run as 32x32-tiled CUDA-core kernels.
+// forward/backward kernels read); activations are BF16, and so are the
+// gradient operands of the backward GEMMs (rounded while a tile is staged);
+// every product is accumulated in FP32.  Every GEMM runs on the tensor cores
+// (gemm_bf16_kernel: 64 x 64 CTA tiles, four warps of 32 x 32, BF16
+// mma.sync m16n8k16 with FP32 accumulators) with its epilogue fused: bias,
+// bias + SiLU (writing the FP32 pre-activation and the BF16 activation), or
+// the SiLU derivative of the backward pass.  The network is small (batch a
+// few hundred, width 256), so a GEMM is a few CTAs and latency bound; the
+// fused epilogues remove the elementwise launches between the GEMMs.
 //
 // Head per sample: [K logits | K*D means | K*D log-sd]; the loss is the
 // negative log-likelihood of a target vector under the mixture.
@@ -46,58 +52,125 @@ namespace messi {
 
 namespace {
 
-constexpr int kT = 32;  // GEMM tile
+__device__ __forceinline__ float silu(float z);
+__device__ __forceinline__ float dsilu(float z);
 
-__device__ __forceinline__ float to_f(float v) { return v; }
-__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ __nv_bfloat16 to_bf(float v) { return __float2bfloat16(v); }
+__device__ __forceinline__ __nv_bfloat16 to_bf(__nv_bfloat16 v) { return v; }
 
-// C[m][n] = sum_k A(m, k) * B(k, n), A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn].
-// mode 0: C = acc + bias[n] (FP32 out); mode 1: C += acc (FP32 accumulate into C).
-template <typename TA, typename TB>
-__global__ void gemm_kernel(int M, int N, int K, const TA* __restrict__ A, long long sam, long long sak,
-                            const TB* __restrict__ B, long long sbk, long long sbn, const float* __restrict__ bias,
-                            float* __restrict__ C, long long scm, int mode)
+constexpr int kBM = 64, kBN = 64, kBK = 32, kPad = 8;  // CTA tile, k step, row padding (bf16)
+
+// GEMM epilogues
+enum GemmMode {
+    kStoreBias = 0,  // C = acc + bias[n]
+    kAccumulate = 1, // C += acc
+    kBiasSilu = 2,   // z = acc + bias[n]; C = z (FP32); act = bf16(silu(z))
+    kDsilu = 3       // C = acc * dsilu(z[m][n])
+};
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
 {
-    __shared__ float As[kT][kT + 1];
-    __shared__ float Bs[kT][kT + 1];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
-    const int m0 = blockIdx.y * kT, n0 = blockIdx.x * kT;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k0 = 0; k0 < K; k0 += kT) {
-        for (int r = ty; r < kT; r += 8) {
-            const int m = m0 + r, k = k0 + tx;
-            As[r][tx] = (m < M && k < K) ? to_f(A[m * sam + k * sak]) : 0.f;
-            const int kk = k0 + r, n = n0 + tx;
-            Bs[r][tx] = (kk < K && n < N) ? to_f(B[kk * sbk + n * sbn]) : 0.f;
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// C[m][n] (row stride scm) = epilogue(sum_k A(m, k) * B(k, n)) with
+// A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn]; operands are rounded
+// to BF16 as the tile is staged in shared memory ([row][k], k contiguous,
+// rows padded by 8 so the fragment loads hit 32 distinct banks).
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, const TA* __restrict__ A, long long sam,
+                                                        long long sak, const TB* __restrict__ B, long long sbk,
+                                                        long long sbn, const float* __restrict__ bias,
+                                                        float* __restrict__ C, long long scm, int mode,
+                                                        const float* __restrict__ z, __nv_bfloat16* __restrict__ act)
+{
+    __shared__ __align__(16) __nv_bfloat16 As[kBM][kBK + kPad];
+    __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kBK + kPad];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
+    // consecutive threads walk the operand's unit-stride index (coalesced)
+    const bool a_k_fast = (sak == 1), b_k_fast = (sbk == 1);
+    for (int k0 = 0; k0 < K; k0 += kBK) {
+        for (int e = tid; e < kBM * kBK; e += 128) {
+            const int r = a_k_fast ? e / kBK : e % kBM, c = a_k_fast ? e % kBK : e / kBM;
+            const int m = m0 + r, k = k0 + c;
+            As[r][c] = (m < M && k < K) ? to_bf(A[m * sam + k * sak]) : __float2bfloat16(0.f);
+            const int r2 = b_k_fast ? e / kBK : e % kBN, c2 = b_k_fast ? e % kBK : e / kBN;
+            const int n = n0 + r2, kk = k0 + c2;
+            Bs[r2][c2] = (n < N && kk < K) ? to_bf(B[kk * sbk + n * sbn]) : __float2bfloat16(0.f);
         }
         __syncthreads();
-#pragma unroll 8
-        for (int k = 0; k < kT; k++) {
-            const float b = Bs[k][tx];
 #pragma unroll
-            for (int q = 0; q < 4; q++) acc[q] = fmaf(As[ty + 8 * q][k], b, acc[q]);
+        for (int ks = 0; ks < kBK; ks += 16) {
+            uint32_t af[2][4], bf[4][2];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                const int r = wm + mt * 16 + g;
+                af[mt][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t]);
+                af[mt][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t]);
+                af[mt][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t + 8]);
+                af[mt][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const int c = wn + nt * 8 + g;
+                bf[nt][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * t]);
+                bf[nt][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
         }
         __syncthreads();
     }
-    const int n = n0 + tx;
-    if (n >= N) return;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        const int m = m0 + ty + 8 * q;
-        if (m >= M) continue;
-        float* c = C + m * scm + n;
-        if (mode == 0) *c = acc[q] + (bias ? bias[n] : 0.f);
-        else *c += acc[q];
-    }
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int m = m0 + wm + mt * 16 + g + 8 * (q >> 1);
+                const int n = n0 + wn + nt * 8 + 2 * t + (q & 1);
+                if (m >= M || n >= N) continue;
+                const long long o = m * scm + n;
+                const float v = acc[mt][nt][q];
+                if (mode == kStoreBias) {
+                    C[o] = v + (bias ? bias[n] : 0.f);
+                } else if (mode == kAccumulate) {
+                    C[o] += v;
+                } else if (mode == kBiasSilu) {
+                    const float zz = v + (bias ? bias[n] : 0.f);
+                    C[o] = zz;
+                    act[o] = __float2bfloat16(silu(zz));
+                } else {
+                    C[o] = v * dsilu(z[o]);
+                }
+            }
 }
 
 template <typename TA, typename TB>
 int gemm(messi_ctx* ctx, int M, int N, int K, const TA* A, long long sam, long long sak, const TB* B, long long sbk,
-         long long sbn, const float* bias, float* C, long long scm, int mode)
+         long long sbn, const float* bias, float* C, long long scm, int mode, const float* z = nullptr,
+         __nv_bfloat16* act = nullptr)
 {
-    dim3 grid((N + kT - 1) / kT, (M + kT - 1) / kT);
-    gemm_kernel<TA, TB><<<grid, 256, 0, ctx->stream>>>(M, N, K, A, sam, sak, B, sbk, sbn, bias, C, scm, mode);
-    LAUNCH_CHECK(ctx, "gemm_kernel");
+    dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
+    gemm_bf16_kernel<TA, TB><<<grid, 128, 0, ctx->stream>>>(M, N, K, A, sam, sak, B, sbk, sbn, bias, C, scm, mode, z,
+                                                            act);
+    LAUNCH_CHECK(ctx, "gemm_bf16_kernel");
     return MESSI_OK;
 }
 
@@ -106,18 +179,6 @@ __device__ __forceinline__ float dsilu(float z)
 {
     const float s = 1.f / (1.f + __expf(-z));
     return s * (1.f + z * (1.f - s));
-}
-
-__global__ void silu_kernel(const float* __restrict__ z, __nv_bfloat16* __restrict__ a, long long n)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] = __float2bfloat16(silu(z[i]));
-}
-
-__global__ void dsilu_kernel(const float* __restrict__ z, float* __restrict__ d, long long n)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) d[i] *= dsilu(z[i]);
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ s, __nv_bfloat16* __restrict__ d, long long n)
@@ -280,13 +341,14 @@ static int mlp_forward_dev(messi_ctx* ctx, messi_mlp* m, int Bn)
     const __nv_bfloat16* W3 = m->p16 + off[4];
     int rc;
     // z1 = x W1^T + b1 : A = x [B x in], B(k, n) = W1[n][k]
-    if ((rc = gemm(ctx, Bn, m->H, m->in, m->x, m->in, 1, W1, 1, m->in, m->p32 + off[1], m->z1, m->H, 0))) return rc;
-    silu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z1, m->a1, (long long)Bn * m->H);
-    LAUNCH_CHECK(ctx, "silu_kernel");
-    if ((rc = gemm(ctx, Bn, m->H, m->H, m->a1, m->H, 1, W2, 1, m->H, m->p32 + off[3], m->z2, m->H, 0))) return rc;
-    silu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z2, m->a2, (long long)Bn * m->H);
-    LAUNCH_CHECK(ctx, "silu_kernel");
-    return gemm(ctx, Bn, m->out, m->H, m->a2, m->H, 1, W3, 1, m->H, m->p32 + off[5], m->y, m->out, 0);
+    // (z1, a1) = (x W1^T + b1, silu); the same for layer 2; y = a2 W3^T + b3
+    if ((rc = gemm(ctx, Bn, m->H, m->in, m->x, m->in, 1, W1, 1, m->in, m->p32 + off[1], m->z1, m->H, kBiasSilu,
+                   nullptr, m->a1)))
+        return rc;
+    if ((rc = gemm(ctx, Bn, m->H, m->H, m->a1, m->H, 1, W2, 1, m->H, m->p32 + off[3], m->z2, m->H, kBiasSilu,
+                   nullptr, m->a2)))
+        return rc;
+    return gemm(ctx, Bn, m->out, m->H, m->a2, m->H, 1, W3, 1, m->H, m->p32 + off[5], m->y, m->out, kStoreBias);
 }
 
 // loss + gradients into m->grad (zeroed first); returns via m->loss
@@ -303,23 +365,25 @@ static int mlp_backward_dev(messi_ctx* ctx, messi_mlp* m, int Bn)
     LAUNCH_CHECK(ctx, "mixture_nll_kernel");
     int rc;
     // layer 3: dW3[o][h] = sum_b dy[b][o] a2[b][h]; db3 = colsum dy; d2 = dy W3
-    if ((rc = gemm(ctx, m->out, m->H, Bn, m->dy, 1, m->out, m->a2, m->H, 1, nullptr, m->grad + off[4], m->H, 1)))
+    if ((rc = gemm(ctx, m->out, m->H, Bn, m->dy, 1, m->out, m->a2, m->H, 1, nullptr, m->grad + off[4], m->H,
+                   kAccumulate)))
         return rc;
     colsum_kernel<<<blocks(m->out), 256, 0, ctx->stream>>>(m->dy, Bn, m->out, m->grad + off[5]);
     LAUNCH_CHECK(ctx, "colsum_kernel");
-    if ((rc = gemm(ctx, Bn, m->H, m->out, m->dy, m->out, 1, W3, m->H, 1, nullptr, m->d2, m->H, 0))) return rc;
-    dsilu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z2, m->d2, (long long)Bn * m->H);
-    LAUNCH_CHECK(ctx, "dsilu_kernel");
+    // d2 = (dy W3) * silu'(z2)
+    if ((rc = gemm(ctx, Bn, m->H, m->out, m->dy, m->out, 1, W3, m->H, 1, nullptr, m->d2, m->H, kDsilu, m->z2)))
+        return rc;
     // layer 2
-    if ((rc = gemm(ctx, m->H, m->H, Bn, m->d2, 1, m->H, m->a1, m->H, 1, nullptr, m->grad + off[2], m->H, 1)))
+    if ((rc = gemm(ctx, m->H, m->H, Bn, m->d2, 1, m->H, m->a1, m->H, 1, nullptr, m->grad + off[2], m->H,
+                   kAccumulate)))
         return rc;
     colsum_kernel<<<blocks(m->H), 256, 0, ctx->stream>>>(m->d2, Bn, m->H, m->grad + off[3]);
     LAUNCH_CHECK(ctx, "colsum_kernel");
-    if ((rc = gemm(ctx, Bn, m->H, m->H, m->d2, m->H, 1, W2, m->H, 1, nullptr, m->d1, m->H, 0))) return rc;
-    dsilu_kernel<<<blocks((long long)Bn * m->H), 256, 0, ctx->stream>>>(m->z1, m->d1, (long long)Bn * m->H);
-    LAUNCH_CHECK(ctx, "dsilu_kernel");
+    if ((rc = gemm(ctx, Bn, m->H, m->H, m->d2, m->H, 1, W2, m->H, 1, nullptr, m->d1, m->H, kDsilu, m->z1)))
+        return rc;
     // layer 1
-    if ((rc = gemm(ctx, m->H, m->in, Bn, m->d1, 1, m->H, m->x, m->in, 1, nullptr, m->grad + off[0], m->in, 1)))
+    if ((rc = gemm(ctx, m->H, m->in, Bn, m->d1, 1, m->H, m->x, m->in, 1, nullptr, m->grad + off[0], m->in,
+                   kAccumulate)))
         return rc;
     colsum_kernel<<<blocks(m->H), 256, 0, ctx->stream>>>(m->d1, Bn, m->H, m->grad + off[1]);
     LAUNCH_CHECK(ctx, "colsum_kernel");

@@ -250,7 +250,10 @@ int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8
     int64_t leaf_rows = 0;
     for (int v = 0; v < nn; v++)
         if (ds->children[2 * v] < 0) { ds->leaf_off[v] = leaf_rows; leaf_rows += ds->nunique[v]; }
-    std::vector<float> leaf((size_t)std::max<int64_t>(leaf_rows, 1) * 16, 0.f);
+    ds->leaf_rows = leaf_rows;
+    std::vector<float>& leaf = ds->leaf_host;
+    leaf.assign((size_t)std::max<int64_t>(leaf_rows, 1) * 16, 0.f);
+    ds->leafnode_host.assign((size_t)std::max<int64_t>(leaf_rows, 1), 0);
     for (int v = 0; v < nn; v++) {
         if (ds->children[2 * v] >= 0) continue;
         const uint8_t* row = &ds->masks[(size_t)ds->seqindex[v] * L];
@@ -258,6 +261,7 @@ int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8
             uint8_t mx = row[rep[v][2 * u]], my = row[rep[v][2 * u + 1]];
             float* o = &leaf[(size_t)(ds->leaf_off[v] + u) * 16];
             for (int a = 0; a < 16; a++) o[a] = (float)(((mx >> (a / 4)) & 1) * ((my >> (a % 4)) & 1));
+            ds->leafnode_host[ds->leaf_off[v] + u] = v;
         }
     }
 
@@ -318,6 +322,7 @@ int build_plan(messi_dataset* ds, const messi_alignment* aln, int W, const uint8
     UPLOAD(ds->d_bandidx, bandidx.data(), bandidx.size() * sizeof(int32_t));
     UPLOAD(ds->d_lr, lr.data(), lr.size() * sizeof(int32_t));
     UPLOAD(ds->d_leaf, leaf.data(), leaf.size() * sizeof(float));
+    UPLOAD(ds->d_leafnode, ds->leafnode_host.data(), ds->leafnode_host.size() * sizeof(int));
     UPLOAD(ds->d_masks, ds->masks.data(), ds->masks.size());
     UPLOAD(ds->d_tree, tree.data(), tree.size() * sizeof(int));
     UPLOAD(ds->d_post, ds->postorder.data(), ds->postorder.size() * sizeof(int));
@@ -352,7 +357,8 @@ cuda_error:
 }
 
 void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e, int64_t row_base, int64_t cstride,
-                           int node_base, int grp, NodeDev* out)
+                           float* leafmsg, int64_t leaf_base, int64_t leaf_cstride, int node_base, int grp,
+                           NodeDev* out)
 {
     for (int v = 0; v < ds->numnodes; v++) {
         NodeDev& d = out[v];
@@ -362,8 +368,7 @@ void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e
         d.li = ds->d_lr + ds->lr_off[v];
         d.ri = ds->d_lr + ds->lr_off[v] + ds->nunique[v];
         const int c0 = ds->children[2 * v], c1 = ds->children[2 * v + 1];
-        d.left = node_base + c0;
-        d.right = node_base + c1;
+        d.self = node_base + v;
         d.grp = grp;
         for (int side = 0; side < 2; side++) {
             const int c = side ? c1 : c0;
@@ -371,9 +376,9 @@ void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e
             const int* ex;
             long long cs;
             if (ds->children[2 * c] < 0) {
-                f = ds->d_leaf + (size_t)ds->leaf_off[c] * 16;
+                f = leafmsg + (size_t)(leaf_base + ds->leaf_off[c]) * 16;
                 ex = nullptr;
-                cs = 0;
+                cs = leaf_cstride;
             } else {
                 f = arena_f + (size_t)(row_base + ds->row_off[c]) * 16;
                 ex = arena_e + row_base + ds->row_off[c];
@@ -401,25 +406,30 @@ int allocate_arena(messi_dataset* ds, int C, std::string* err)
     cudaMemGetInfo(&freeb, &totalb);
     const size_t row_bytes = 16 * sizeof(float) + sizeof(int);
     size_t budget = freeb / 2;
+    const int64_t leaf_rows = std::max<int64_t>(ds->leaf_rows, 1);
     int chunk = C;
-    while (chunk > 1 && (size_t)chunk * ds->arena_rows * row_bytes > budget) chunk = (chunk + 1) / 2;
+    while (chunk > 1 && (size_t)chunk * (ds->arena_rows + leaf_rows) * row_bytes > budget) chunk = (chunk + 1) / 2;
     if (ds->chunk != chunk) {
         if (ds->d_arena_f) cudaFree(ds->d_arena_f);
         if (ds->d_arena_e) cudaFree(ds->d_arena_e);
+        if (ds->d_leafmsg) cudaFree(ds->d_leafmsg);
         ds->d_arena_f = nullptr;
         ds->d_arena_e = nullptr;
+        ds->d_leafmsg = nullptr;
         ds->chunk = 0;
         cudaError_t e = cudaMalloc((void**)&ds->d_arena_f, (size_t)chunk * ds->arena_rows * 16 * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc((void**)&ds->d_arena_e, (size_t)chunk * ds->arena_rows * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&ds->d_leafmsg, (size_t)chunk * leaf_rows * 16 * sizeof(float));
         if (e != cudaSuccess) {
-            *err = std::string("partial arena: ") + cudaGetErrorString(e);
+            *err = std::string("message arena: ") + cudaGetErrorString(e);
             return MESSI_ENOMEM;
         }
         ds->chunk = chunk;
     }
     ds->arena_gen++;
     ds->nodes_host.assign(ds->numnodes, NodeDev{});
-    fill_node_descriptors(ds, ds->d_arena_f, ds->d_arena_e, 0, ds->arena_rows, 0, 0, ds->nodes_host.data());
+    fill_node_descriptors(ds, ds->d_arena_f, ds->d_arena_e, 0, ds->arena_rows, ds->d_leafmsg, 0, leaf_rows, 0, 0,
+                          ds->nodes_host.data());
     const int nn = ds->numnodes;
     cudaError_t e = cudaMemcpy(ds->d_nodes, ds->nodes_host.data(), sizeof(NodeDev) * nn, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {

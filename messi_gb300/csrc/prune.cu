@@ -6,12 +6,22 @@
 // :135-151) with:
 //   * build_P16_kernel: P = exp(Qt) per (category, branch) in FP64 from the
 //     host eigensystem, stored as FP32 rows (row = parent state);
-//   * prune_mma_kernel: one launch per tree level and category pass; a warp
-//     owns 32 unique pairs of one node, gathers the child rows with cp.async
-//     (two categories in flight) and does both child mat-vecs on the tensor
-//     cores (3xTF32 mma.sync, operands split into hi/lo in registers).  Rows are rescaled by an exact power of two
-//     (exponent kept as an int), which computes the same likelihood as the
-//     reference's divide-by-max (felsenstein.cu:193-198);
+//   * message rows: what a node passes to its parent is its partial
+//     likelihood vector already multiplied by its own branch's matrix,
+//     m_v = P_v x_v, so every node update is x_v = m_left * m_right
+//     (elementwise) followed by ONE mat-vec, P_v x_v, done once per unique
+//     row at v instead of once per parent pair that reads the row (the
+//     reference applies both child matrices inside every parent update,
+//     felsenstein.cu:170-190); the root needs no mat-vec, only pi . x;
+//   * leaf_msg_kernel: the messages of the leaves (P_leaf x indicator rows)
+//     per category pass;
+//   * prune_msg_kernel: one launch per tree level and category pass; a warp
+//     owns 32 unique pairs of one node, gathers the two children's message
+//     rows with cp.async (two categories in flight) and does the mat-vec on
+//     the tensor cores (3xTF32 mma.sync, operands split into hi/lo in
+//     registers).  Rows are rescaled by an exact power of two (exponent kept
+//     as an int), which computes the same likelihood as the reference's
+//     divide-by-max (felsenstein.cu:193-198);
 //   * the root variant folds sumfinal and the category log-sum-exp into the
 //     same pass (FP64 log-likelihood reduction).
 // unpaired_site_kernel + unpaired_mix_kernel restate
@@ -103,16 +113,50 @@ __device__ __forceinline__ double lse_d(double a, double b)
 }
 
 // ---------------------------------------------------------------------------
+// Leaf messages: out[cc][r][a] = sum_d P[c0+cc][node(r)][a][d] * rows[r][d]
+// (16 threads per row, FP64 accumulation, one FP32 rounding).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) leaf_msg_kernel(const float* __restrict__ rows, const int* __restrict__ rownode,
+                                                       long long R, const float* __restrict__ P, int numnodes, int c0,
+                                                       float* __restrict__ out)
+{
+    const long long r = (long long)blockIdx.x * 16 + (threadIdx.x >> 4);
+    const int a = threadIdx.x & 15, cc = blockIdx.y;
+    if (r >= R) return;
+    const float* p = P + ((size_t)(c0 + cc) * numnodes + __ldg(rownode + r)) * 256 + a * 16;
+    const float* x = rows + r * 16;
+    double s = 0.0;
+#pragma unroll
+    for (int d = 0; d < 16; d++) s += (double)__ldg(p + d) * (double)__ldg(x + d);
+    out[((size_t)cc * R + r) * 16 + a] = (float)s;
+}
+
+int launch_leaf_messages(messi_ctx* ctx, const float* d_rows, const int* d_rownode, int64_t R, const float* d_P,
+                         int numnodes, int c0, int nc, float* d_out)
+{
+    if (R <= 0 || nc <= 0) return MESSI_OK;
+    leaf_msg_kernel<<<dim3((unsigned)((R + 15) / 16), nc), 256, 0, ctx->stream>>>(d_rows, d_rownode, R, d_P,
+                                                                                  numnodes, c0, d_out);
+    LAUNCH_CHECK(ctx, "leaf_msg_kernel");
+    return MESSI_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Tensor-core node update (3xTF32 mma.sync).  A warp owns 32 unique pairs of
-// one node; for each category the two child mat-vecs are the products
-// [32 pairs x 16] x [16 x 16]^T, done as m16n8k8 TF32 MMAs with both operands
-// split hi + lo (hi*hi + hi*lo + lo*hi: FP32-level accuracy; all operands are
-// non-negative, so no cancellation).  The contraction index d is permuted so
-// that lane (g, t) owns d = 4t..4t+3: its A fragment for pair row r is one
-// 16-byte load of child row r, and its B fragment is one 16-byte load of
-// P[8nt + g][4t..4t+3].  Lane (g, t) ends with states {2t, 2t+1, 8+2t, 9+2t}
-// of pairs g, g+8, g+16, g+24; lane t keeps the scalar bookkeeping (exponent,
-// mixture) of pair g + 8t.
+// one node.  For each category it forms x = m_left * m_right for its pairs
+// and, below the root, the product [32 pairs x 16] x [16 x 16]^T with P of
+// the node's own branch, as m16n8k8 TF32 MMAs with both operands split
+// hi + lo (hi*hi + hi*lo + lo*hi: FP32-level accuracy; all operands are
+// non-negative, so there is no cancellation).  The hi*hi products go to one
+// accumulator and the two small cross terms to another, added once at the
+// end: the tensor core's FP32 accumulation is not round-to-nearest, and this
+// keeps its error in the large sum to two accumulation steps per mat-vec.
+// The contraction index d is permuted so that lane (g, t) owns
+// d = 4t..4t+3: its A fragment for pair row r is one 16-byte load of each
+// child's row, and its B fragment one 16-byte load of P[8nt + g][4t..4t+3].
+// Lane (g, t) ends with states {2t, 2t+1, 8+2t, 9+2t} of pairs g, g+8,
+// g+16, g+24; lane t keeps the scalar bookkeeping (exponent, mixture) of pair
+// g + 8t.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float comp4(const float4& v, int k)
 {
@@ -132,8 +176,7 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
 // magnitude bits and truncating is round-to-nearest, ties away, the same as
 // cvt.rna for the finite values here) and lo = x - hi (exact in FP32), fed
 // without conversion: the tensor core reads the top 19 bits of lo, an error
-// below 2^-21 |x|.  Two integer operations and a subtraction per element
-// instead of two conversions: 3% faster pruning, same accuracy.
+// below 2^-21 |x| of either sign (lo is centred on zero).
 __device__ __forceinline__ void split_a(float x, uint32_t& hi, uint32_t& lo)
 {
     hi = (__float_as_uint(x) + 0x1000u) & 0xffffe000u;
@@ -153,9 +196,10 @@ __device__ __forceinline__ void split_b(const float4& p, float4& hi, float4& lo)
     lo = make_float4(__uint_as_float(l[0]), __uint_as_float(l[1]), __uint_as_float(l[2]), __uint_as_float(l[3]));
 }
 
-// D[mt][nt][4] += X (rows g + 8k, k = 0..3) x P^T for one child.
-__device__ __forceinline__ void child_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bl)[2],
-                                          float (&D)[2][2][4])
+// Dh[mt][nt] += Xh x Ph^T, Dx[mt][nt] += Xl x Ph^T + Xh x Pl^T for rows
+// g + 8k (k = 0..3).
+__device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bl)[2],
+                                        float (&Dh)[2][2][4], float (&Dx)[2][2][4])
 {
 #pragma unroll
     for (int mt = 0; mt < 2; mt++) {
@@ -170,9 +214,9 @@ __device__ __forceinline__ void child_mma(const float4 (&X)[4], const float4 (&B
             for (int nt = 0; nt < 2; nt++) {
                 const uint32_t bh0 = __float_as_uint(comp4(Bh[nt], 2 * ks)), bh1 = __float_as_uint(comp4(Bh[nt], 2 * ks + 1));
                 const uint32_t bl0 = __float_as_uint(comp4(Bl[nt], 2 * ks)), bl1 = __float_as_uint(comp4(Bl[nt], 2 * ks + 1));
-                mma_tf32(D[mt][nt], al, bh0, bh1);
-                mma_tf32(D[mt][nt], ah, bl0, bl1);
-                mma_tf32(D[mt][nt], ah, bh0, bh1);
+                mma_tf32(Dx[mt][nt], al, bh0, bh1);
+                mma_tf32(Dx[mt][nt], ah, bl0, bl1);
+                mma_tf32(Dh[mt][nt], ah, bh0, bh1);
             }
         }
     }
@@ -195,8 +239,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-
-
 // Exact power-of-two rescale of a row max m > 0: m * 2^-ex in [0.5, 1).
 __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
 {
@@ -216,11 +258,8 @@ __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
 
 // Pipeline shapes: STAGES categories in flight per warp (cp.async), MINB CTAs
 // of kTile = 128 threads per SM.  The default, 2 stages x 4 CTAs (16 warps,
-// 128 registers, 136 KB of stages per SM), leaves ~90 KB of the SM's L1 to
-// cache the gathered child rows, which parent pairs share heavily: on GB300
-// it prunes c2 in 9.2 ms against 11.4 ms for 3 CTAs of 8 warps (24 warps, 80
-// registers with spills, 204 KB of stages) and 20.3 ms with the row copies
-// bypassing L1.
+// 136 KB of stages per SM), leaves ~90 KB of the SM's L1 to cache the
+// gathered child rows, which parent pairs share heavily.
 
 // Per-warp staging of one category: 8 float4 per lane (child rows) + 2 exponents.
 struct WarpStage {
@@ -229,7 +268,7 @@ struct WarpStage {
 };
 
 template <bool ROOT, int STAGES, int MINB>
-__global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
+__global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
     const NodeDev* __restrict__ nodes, const int2* __restrict__ tiles, const float* __restrict__ P, int numnodes,
     int c0, int nc, int C, const float* __restrict__ pi16, const double* __restrict__ logw,
     const int* __restrict__ lam, int per_lambda)
@@ -290,47 +329,20 @@ __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
         cp_async_commit();
         cp_async_wait<STAGES - 1>();
         const WarpStage& st = stage[cc % STAGES];
-        float4 XL[4], XR[4];
+        // x = m_left * m_right: states 4t..4t+3 of pairs g + 8k
+        float4 X[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            XL[k] = st.x[k][lane];
-            XR[k] = st.x[4 + k][lane];
+            const float4 a = st.x[k][lane], b = st.x[4 + k][lane];
+            X[k] = make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
         }
         const int e = (le ? st.e[0][lane] : 0) + (re ? st.e[1][lane] : 0);
-        const float* ptl = P + ((size_t)(c0 + cc) * numnodes + nd.left) * 256;
-        const float* ptr = P + ((size_t)(c0 + cc) * numnodes + nd.right) * 256;
-        float4 Bh[2], Bl[2];
-        float DL[2][2][4], DR[2][2][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-            for (int nt = 0; nt < 2; nt++)
-#pragma unroll
-                for (int i = 0; i < 4; i++) { DL[mt][nt][i] = 0.f; DR[mt][nt][i] = 0.f; }
-#pragma unroll
-        for (int nt = 0; nt < 2; nt++) split_b(ldg4(ptl + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
-        child_mma(XL, Bh, Bl, DL);
-#pragma unroll
-        for (int nt = 0; nt < 2; nt++) split_b(ldg4(ptr + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
-        child_mma(XR, Bh, Bl, DR);
-        // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}
-        float V[4][4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int mt = k >> 1, h = k & 1;
-            V[k][0] = DL[mt][0][2 * h] * DR[mt][0][2 * h];
-            V[k][1] = DL[mt][0][2 * h + 1] * DR[mt][0][2 * h + 1];
-            V[k][2] = DL[mt][1][2 * h] * DR[mt][1][2 * h];
-            V[k][3] = DL[mt][1][2 * h + 1] * DR[mt][1][2 * h + 1];
-        }
         if (ROOT) {
-            const float* pc = pi16 + ((size_t)nd.grp * C + c0 + cc) * 16;
-            const float p0 = __ldg(pc + 2 * t), p1 = __ldg(pc + 2 * t + 1), p2 = __ldg(pc + 8 + 2 * t),
-                        p3 = __ldg(pc + 9 + 2 * t);
+            const float4 pc = __ldg(reinterpret_cast<const float4*>(pi16 + ((size_t)nd.grp * C + c0 + cc) * 16) + t);
             float dots[4];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                float dk = p0 * V[k][0] + p1 * V[k][1] + p2 * V[k][2] + p3 * V[k][3];
+                float dk = pc.x * X[k].x + pc.y * X[k].y + pc.z * X[k].z + pc.w * X[k].w;
                 dk += __shfl_xor_sync(0xffffffffu, dk, 1);
                 dk += __shfl_xor_sync(0xffffffffu, dk, 2);
                 dots[k] = dk;
@@ -359,6 +371,29 @@ __global__ void __launch_bounds__(kTile, MINB) prune_mma_kernel(
                     }
             }
         } else {
+            // m_v = P_v x (the node's own branch), then an exact power-of-two rescale
+            const float* pv = P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256;
+            float4 Bh[2], Bl[2];
+#pragma unroll
+            for (int nt = 0; nt < 2; nt++) split_b(ldg4(pv + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
+            float Dh[2][2][4], Dx[2][2][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 2; nt++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) { Dh[mt][nt][i] = 0.f; Dx[mt][nt][i] = 0.f; }
+            msg_mma(X, Bh, Bl, Dh, Dx);
+            // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}
+            float V[4][4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int mt = k >> 1, h = k & 1;
+                V[k][0] = Dh[mt][0][2 * h] + Dx[mt][0][2 * h];
+                V[k][1] = Dh[mt][0][2 * h + 1] + Dx[mt][0][2 * h + 1];
+                V[k][2] = Dh[mt][1][2 * h] + Dx[mt][1][2 * h];
+                V[k][3] = Dh[mt][1][2 * h + 1] + Dx[mt][1][2 * h + 1];
+            }
             int exk[4];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -405,21 +440,20 @@ static int launch_prune_shape(messi_ctx* ctx, const NodeDev* d_nodes, const int2
     static thread_local int smem_set_device = -1;
     const size_t smem = (size_t)(kTile / 32) * STAGES * sizeof(WarpStage);
     if (smem_set_device != ctx->device) {
-        cudaFuncSetAttribute(prune_mma_kernel<false, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(prune_msg_kernel<false, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-        cudaFuncSetAttribute(prune_mma_kernel<true, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(prune_msg_kernel<true, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-
         smem_set_device = ctx->device;
     }
     if (root) {
-        prune_mma_kernel<true, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
+        prune_msg_kernel<true, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
             d_nodes, d_tiles, d_P, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
-        LAUNCH_CHECK(ctx, "prune_mma_kernel<root>");
+        LAUNCH_CHECK(ctx, "prune_msg_kernel<root>");
     } else {
-        prune_mma_kernel<false, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
+        prune_msg_kernel<false, STAGES, MINB><<<nt, kTile, smem, ctx->stream>>>(
             d_nodes, d_tiles, d_P, numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda ? 1 : 0);
-        LAUNCH_CHECK(ctx, "prune_mma_kernel");
+        LAUNCH_CHECK(ctx, "prune_msg_kernel");
     }
     return MESSI_OK;
 }
@@ -429,8 +463,7 @@ int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_til
                        const double* d_logw, const int* d_lam, bool per_lambda)
 {
     if (nt <= 0) return MESSI_OK;
-    // MESSI_PRUNE_SHAPE=1 / 2: 3 stages x 3 CTAs, 2 stages x 3 CTAs (measured
-    // 6% and 5% slower on c2 and c4)
+    // shapes: 0 = 2 stages x 4 CTAs/SM, 1 = 3 stages x 3 CTAs, 2 = 2 stages x 3 CTAs
     switch (ctx->prune_shape) {
         case 1: return launch_prune_shape<3, 3>(ctx, d_nodes, d_tiles, nt, root, d_P, numnodes, c0, nc, C, d_pi16,
                                                 d_logw, d_lam, per_lambda);
@@ -448,6 +481,9 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
     const int chunk = ds->chunk;
     for (int c0 = 0; c0 < C; c0 += chunk) {
         const int nc = std::min(chunk, C - c0);
+        int rc = launch_leaf_messages(ctx, ds->d_leaf, ds->d_leafnode, ds->leaf_rows, d_P, ds->numnodes, c0, nc,
+                                      ds->d_leafmsg);
+        if (rc) return rc;
         for (int lv = 1; lv <= ds->H; lv++) {
             const int nt = ds->tile_cnt[lv];
             if (nt == 0) continue;
@@ -456,8 +492,8 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
                 for (int v : ds->level_nodes[lv]) units += (double)ds->nunique[v] * nc;
                 prof_begin(ctx, 0, units);
             }
-            int rc = launch_prune_tiles(ctx, ds->d_nodes, ds->d_tiles + ds->tile_off[lv], nt, lv == ds->H, d_P,
-                                        ds->numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda);
+            rc = launch_prune_tiles(ctx, ds->d_nodes, ds->d_tiles + ds->tile_off[lv], nt, lv == ds->H, d_P,
+                                    ds->numnodes, c0, nc, C, d_pi16, d_logw, d_lam, per_lambda);
             if (rc) return rc;
             prof_end(ctx);
         }

@@ -4,8 +4,11 @@ Same parameter layout and maths as messi_gb300/csrc/mlp.cu: three linear
 layers in -> H -> H -> out, SiLU after the first two, a K-component diagonal
 Gaussian-mixture head [K logits | K*D means | K*D log-sd (clamped to
 [-7, 5])] and the mean negative log-likelihood of targets.  With
-``bf16=True`` weights and activations are rounded to bfloat16 the way the GPU
-kernels store them, so the comparison isolates accumulation order.
+``bf16=True`` weights, activations and the gradient operands of the
+backward products are rounded to bfloat16 the way the GPU kernels stage them
+for the tensor cores (the bias gradients are column sums of the unrounded
+FP32 gradients, as on the GPU), so the comparison isolates accumulation
+order.
 """
 import numpy as np
 
@@ -84,14 +87,15 @@ def mixture_nll(y, tgt, K, D):
 def gradients(p, x, tgt, nin, H, K, D, bf16=True):
     nout = K + 2 * K * D
     f = forward(p, x, nin, H, nout, bf16)
+    r = to_bf16 if bf16 else (lambda a: np.asarray(a, np.float64))
     loss, dy = mixture_nll(f["y"], np.asarray(tgt, np.float64), K, D)
-    dW3 = dy.T @ f["a2"]
+    dW3 = r(dy).T @ f["a2"]
     db3 = dy.sum(0)
-    d2 = (dy @ f["W3"]) * dsilu(f["z2"])
-    dW2 = d2.T @ f["a1"]
+    d2 = (r(dy) @ f["W3"]) * dsilu(f["z2"])
+    dW2 = r(d2).T @ f["a1"]
     db2 = d2.sum(0)
-    d1 = (d2 @ f["W2"]) * dsilu(f["z1"])
-    dW1 = d1.T @ f["x"]
+    d1 = (r(d2) @ f["W2"]) * dsilu(f["z1"])
+    dW1 = r(d1).T @ f["x"]
     db1 = d1.sum(0)
     g = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dW3.ravel(), db3])
     return float(loss.mean()), g

@@ -79,6 +79,10 @@ def test_c2_pairs_Z_and_posteriors_against_fp64_chain(c2):
     u = api.computeunpairedlikelihoods(ds, params)
     mat, _ = api.felsensteincuda(ds, params, None, W)
     e_pair = _rel_err(mat, p_ref)
+    fin = np.isfinite(p_ref)
+    d = mat[fin] - p_ref[fin]
+    print(f"\nPARITY c2 pairs: signed error mean {d.mean():.3e}, sd {d.std():.3e}, fraction below the FP64 value "
+          f"{np.mean(d < 0):.3f}, max abs {np.abs(d).max():.3e} at |ref| {np.abs(p_ref[fin])[np.argmax(np.abs(d))]:.2f}")
     assert e_pair <= REL, f"c2 pair log-likelihoods: max relative error {e_pair:.3e}"
     np.testing.assert_allclose(u, u_ref, rtol=1e-11)
     assert int(np.isfinite(mat[np.triu_indices(L, 1)]).sum()) == 374750
