@@ -8,6 +8,7 @@ Matrices come back as Fortran-ordered numpy arrays (Julia's layout), so
 ``inside[X, i, j]`` and ``pairedlogprobs[x, y]`` index them like the
 reference's arrays (0-based).
 """
+import collections
 import ctypes
 import hashlib
 import threading
@@ -34,7 +35,7 @@ class Context:
         _lib.check(self.lib.messi_ctx_create(int(device), ctypes.byref(h)), "messi_ctx_create")
         self.handle = h
         self.device = device
-        self._datasets = {}
+        self._datasets = collections.OrderedDict()
 
     def close(self):
         for ds in list(self._datasets.values()):
@@ -89,10 +90,16 @@ class Context:
     def check(self, status, what):
         _lib.check(status, what, self.handle)
 
+    # dataset handles kept (each holds its pair plan and message arena on the device)
+    MAX_CACHED_DATASETS = 4
+
     def dataset(self, dataset, maxbasepairdistance=1000000, pairmask=None):
-        """Cached dataset handle (the reference caches its pair index in
-        process globals, src/FelsensteinCUDA.jl:206-238; here the cache key is
-        the dataset, the band and the pair mask)."""
+        """Cached dataset handle (the reference caches the pair index of its
+        last dataset in process globals, src/FelsensteinCUDA.jl:206-238; here
+        the cache key is the dataset, the band and the pair mask, and the
+        MAX_CACHED_DATASETS most recently used handles are kept: an evicted
+        handle is destroyed, so a loop over many alignments does not hold
+        every alignment's device arena)."""
         W = int(min(max(1, maxbasepairdistance), max(1, dataset.numcols - 1)))
         mkey = None if pairmask is None else hashlib.sha1(np.ascontiguousarray(pairmask, np.uint8)).hexdigest()
         key = (id(dataset), W, mkey)
@@ -100,8 +107,14 @@ class Context:
         if h is None or h.dataset is not dataset:
             if h is not None:  # id() reused by a new dataset object
                 h.close()
+                del self._datasets[key]
+            while len(self._datasets) >= self.MAX_CACHED_DATASETS:
+                _, old = self._datasets.popitem(last=False)
+                old.close()
             h = DatasetHandle(self, dataset, W, pairmask)
             self._datasets[key] = h
+        else:
+            self._datasets.move_to_end(key)
         return h
 
 

@@ -376,7 +376,7 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     const int* d_grp = (const int*)(base + o_grp);
     const uint8_t* d_gap = gapfrequency ? (const uint8_t*)(base + o_gap) : nullptr;
     void *pt, *p4;
-    if (grow(b->P16, (size_t)C * b->total_nodes * 256 * sizeof(float), &pt))
+    if (grow(b->P16, (size_t)3 * C * b->total_nodes * 256 * sizeof(float), &pt))
         return fail(ctx, MESSI_ENOMEM, "batch transition matrices");
     if (grow(b->P4, (size_t)nsite * b->total_nodes * 16 * sizeof(double), &p4))
         return fail(ctx, MESSI_ENOMEM, "batch unpaired transition matrices");
@@ -412,7 +412,7 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     for (int c0 = 0; c0 < C; c0 += b->chunk) {
         const int nc = std::min(b->chunk, C - c0);
         if ((rc = launch_leaf_messages(ctx, b->d_leafrows, b->d_leafnode, b->total_leaf_rows, d_P, b->total_nodes, c0,
-                                       nc, b->d_leafmsg)))
+                                       nc, C, b->d_leafmsg)))
             return rc;
         for (int lv = 1; lv <= b->H; lv++) {
             for (int root = 0; root < 2; root++) {

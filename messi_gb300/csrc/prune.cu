@@ -34,7 +34,21 @@
 
 namespace messi {
 
-// P[c][v][a][d] in FP32 (row = parent state), from the FP64 eigensystem.
+// TF32 rounding (to nearest) of a value, returned as the FP32 number the
+// tensor cores read without loss.
+__device__ __forceinline__ float tf32_rn(double v)
+{
+    const float f = (float)v;
+    return __uint_as_float((__float_as_uint(f) + 0x1000u) & 0xffffe000u);
+}
+
+// P[c][v][a][d] (row = parent state) from the FP64 eigensystem, stored as
+// three FP32 planes hi, mid, lo of TF32-exact values with hi + mid + lo = P
+// to about 2^-33 relative: hi = tf32(P), mid = tf32(P - hi),
+// lo = tf32(P - hi - mid).  A single FP32 copy of P would carry a rounding
+// error of up to 2^-24 per entry that is the same for every site pair, so
+// the pair log-likelihoods would all shift together (by ~1e-6 for a
+// 64-sequence tree); the three planes make that common error negligible.
 __global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl,
                                  const int* __restrict__ nodegrp, int numnodes, int C, float* __restrict__ P)
 {
@@ -50,19 +64,26 @@ __global__ void build_P16_kernel(const double* __restrict__ eig, const double* _
     }
     __syncthreads();
     const int a = t >> 4, d = t & 15;
-    float out;
+    double out;
     if (grp < 0) {
-        out = 0.f;  // a root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
+        out = 0.0;  // a root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
     } else if (tl == 0.0) {
-        out = (a == d) ? 1.f : 0.f;
+        out = (a == d) ? 1.0 : 0.0;
     } else {
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < 16; k++) s += U[a * 16 + k] * ex[k] * U[d * 16 + k];
         s *= sp[d] / sp[a];
-        out = (s <= 0.0) ? 0.f : (float)s;  // absmat clamp (1e-50 rounds to 0 in FP32)
+        out = (s <= 0.0) ? 0.0 : s;  // absmat clamp (1e-50 is below every plane's range)
     }
-    P[((size_t)c * numnodes + v) * 256 + t] = out;
+    const float hi = tf32_rn(out);
+    const double r1 = out - (double)hi;
+    const float mid = tf32_rn(r1);
+    const float lo = tf32_rn(r1 - (double)mid);
+    const size_t plane = (size_t)C * numnodes * 256, o = ((size_t)c * numnodes + v) * 256 + t;
+    P[o] = hi;
+    P[plane + o] = mid;
+    P[2 * plane + o] = lo;
 }
 
 __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl,
@@ -114,29 +135,33 @@ __device__ __forceinline__ double lse_d(double a, double b)
 
 // ---------------------------------------------------------------------------
 // Leaf messages: out[cc][r][a] = sum_d P[c0+cc][node(r)][a][d] * rows[r][d]
-// (16 threads per row, FP64 accumulation, one FP32 rounding).
+// (16 threads per row; P = the sum of its three planes, FP64 accumulation,
+// one FP32 rounding).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) leaf_msg_kernel(const float* __restrict__ rows, const int* __restrict__ rownode,
                                                        long long R, const float* __restrict__ P, int numnodes, int c0,
-                                                       float* __restrict__ out)
+                                                       int C, float* __restrict__ out)
 {
     const long long r = (long long)blockIdx.x * 16 + (threadIdx.x >> 4);
     const int a = threadIdx.x & 15, cc = blockIdx.y;
     if (r >= R) return;
+    const size_t plane = (size_t)C * numnodes * 256;
     const float* p = P + ((size_t)(c0 + cc) * numnodes + __ldg(rownode + r)) * 256 + a * 16;
     const float* x = rows + r * 16;
     double s = 0.0;
 #pragma unroll
-    for (int d = 0; d < 16; d++) s += (double)__ldg(p + d) * (double)__ldg(x + d);
+    for (int d = 0; d < 16; d++)
+        s += ((double)__ldg(p + d) + (double)__ldg(p + plane + d) + (double)__ldg(p + 2 * plane + d)) *
+             (double)__ldg(x + d);
     out[((size_t)cc * R + r) * 16 + a] = (float)s;
 }
 
 int launch_leaf_messages(messi_ctx* ctx, const float* d_rows, const int* d_rownode, int64_t R, const float* d_P,
-                         int numnodes, int c0, int nc, float* d_out)
+                         int numnodes, int c0, int nc, int C, float* d_out)
 {
     if (R <= 0 || nc <= 0) return MESSI_OK;
     leaf_msg_kernel<<<dim3((unsigned)((R + 15) / 16), nc), 256, 0, ctx->stream>>>(d_rows, d_rownode, R, d_P,
-                                                                                  numnodes, c0, d_out);
+                                                                                  numnodes, c0, C, d_out);
     LAUNCH_CHECK(ctx, "leaf_msg_kernel");
     return MESSI_OK;
 }
@@ -183,23 +208,10 @@ __device__ __forceinline__ void split_a(float x, uint32_t& hi, uint32_t& lo)
     lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
-// B operand (four entries of P) split the same way, in registers: one FP32
-// load per fragment instead of a hi and a lo load.
-__device__ __forceinline__ void split_b(const float4& p, float4& hi, float4& lo)
-{
-    uint32_t h[4], l[4];
-    split_a(p.x, h[0], l[0]);
-    split_a(p.y, h[1], l[1]);
-    split_a(p.z, h[2], l[2]);
-    split_a(p.w, h[3], l[3]);
-    hi = make_float4(__uint_as_float(h[0]), __uint_as_float(h[1]), __uint_as_float(h[2]), __uint_as_float(h[3]));
-    lo = make_float4(__uint_as_float(l[0]), __uint_as_float(l[1]), __uint_as_float(l[2]), __uint_as_float(l[3]));
-}
-
-// Dh[mt][nt] += Xh x Ph^T, Dx[mt][nt] += Xl x Ph^T + Xh x Pl^T for rows
-// g + 8k (k = 0..3).
-__device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bl)[2],
-                                        float (&Dh)[2][2][4], float (&Dx)[2][2][4])
+// Dh[mt][nt] += Xh x Ph^T, Dx[mt][nt] += Xl x Ph^T + Xh x Pm^T + Xh x Pl^T
+// for rows g + 8k (k = 0..3); P = Ph + Pm + Pl (the three planes).
+__device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bm)[2],
+                                        const float4 (&Bl)[2], float (&Dh)[2][2][4], float (&Dx)[2][2][4])
 {
 #pragma unroll
     for (int mt = 0; mt < 2; mt++) {
@@ -213,9 +225,11 @@ __device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)
 #pragma unroll
             for (int nt = 0; nt < 2; nt++) {
                 const uint32_t bh0 = __float_as_uint(comp4(Bh[nt], 2 * ks)), bh1 = __float_as_uint(comp4(Bh[nt], 2 * ks + 1));
+                const uint32_t bm0 = __float_as_uint(comp4(Bm[nt], 2 * ks)), bm1 = __float_as_uint(comp4(Bm[nt], 2 * ks + 1));
                 const uint32_t bl0 = __float_as_uint(comp4(Bl[nt], 2 * ks)), bl1 = __float_as_uint(comp4(Bl[nt], 2 * ks + 1));
-                mma_tf32(Dx[mt][nt], al, bh0, bh1);
                 mma_tf32(Dx[mt][nt], ah, bl0, bl1);
+                mma_tf32(Dx[mt][nt], al, bh0, bh1);
+                mma_tf32(Dx[mt][nt], ah, bm0, bm1);
                 mma_tf32(Dh[mt][nt], ah, bh0, bh1);
             }
         }
@@ -373,9 +387,14 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
         } else {
             // m_v = P_v x (the node's own branch), then an exact power-of-two rescale
             const float* pv = P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256;
-            float4 Bh[2], Bl[2];
+            const size_t plane = (size_t)C * numnodes * 256;
+            float4 Bh[2], Bm[2], Bl[2];
 #pragma unroll
-            for (int nt = 0; nt < 2; nt++) split_b(ldg4(pv + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
+            for (int nt = 0; nt < 2; nt++) {
+                Bh[nt] = ldg4(pv + (8 * nt + g) * 16 + 4 * t);
+                Bm[nt] = ldg4(pv + plane + (8 * nt + g) * 16 + 4 * t);
+                Bl[nt] = ldg4(pv + 2 * plane + (8 * nt + g) * 16 + 4 * t);
+            }
             float Dh[2][2][4], Dx[2][2][4];
 #pragma unroll
             for (int mt = 0; mt < 2; mt++)
@@ -383,7 +402,7 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
                 for (int nt = 0; nt < 2; nt++)
 #pragma unroll
                     for (int i = 0; i < 4; i++) { Dh[mt][nt][i] = 0.f; Dx[mt][nt][i] = 0.f; }
-            msg_mma(X, Bh, Bl, Dh, Dx);
+            msg_mma(X, Bh, Bm, Bl, Dh, Dx);
             // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}
             float V[4][4];
 #pragma unroll
@@ -481,7 +500,7 @@ int run_pairs(messi_ctx* ctx, messi_dataset* ds, const float* d_P, const float* 
     const int chunk = ds->chunk;
     for (int c0 = 0; c0 < C; c0 += chunk) {
         const int nc = std::min(chunk, C - c0);
-        int rc = launch_leaf_messages(ctx, ds->d_leaf, ds->d_leafnode, ds->leaf_rows, d_P, ds->numnodes, c0, nc,
+        int rc = launch_leaf_messages(ctx, ds->d_leaf, ds->d_leafnode, ds->leaf_rows, d_P, ds->numnodes, c0, nc, C,
                                       ds->d_leafmsg);
         if (rc) return rc;
         for (int lv = 1; lv <= ds->H; lv++) {
