@@ -86,6 +86,15 @@ int messi_ctx_last_launches(messi_ctx* ctx, int64_t* launches);
  * dataset, category layout and buffers; MESSI_GRAPHS=0 at context creation
  * turns graphs off). */
 int messi_ctx_graph_replays(messi_ctx* ctx, int64_t* replays);
+/* Launch shapes of the last likelihood evaluation (no counterpart in the
+ * reference): the pruning pipeline shape (0 = 2 stages x 4 CTAs per SM,
+ * 1 = 3 x 3, 2 = 2 x 3) and the wavefront CTA size (0 = chosen by band size),
+ * and how many workloads have finished autotuning.  The first four
+ * evaluations of a dataset (or batch) at a category count try candidate
+ * shapes, timed with CUDA events, and later ones use the fastest
+ * (MESSI_AUTOTUNE=0 at context creation turns this off; MESSI_PRUNE_SHAPE or
+ * MESSI_WAVE_THREADS fix one knob).  Results do not depend on the shapes. */
+int messi_ctx_launch_shapes(messi_ctx* ctx, int32_t* prune_shape, int32_t* wave_threads, int32_t* tuned);
 /* Text of the last error recorded on this context. */
 const char* messi_ctx_last_error(messi_ctx* ctx);
 /* Self-test of the bounded device waits (no counterpart in the reference):

@@ -51,6 +51,8 @@ _SIGS = {
     "messi_ctx_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "messi_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     "messi_ctx_graph_replays": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "messi_ctx_launch_shapes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "messi_ctx_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "messi_ctx_profile_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double)]),

@@ -61,6 +61,14 @@ class Context:
         _lib.check(self.lib.messi_ctx_last_launches(self.handle, ctypes.byref(n)), "messi_ctx_last_launches")
         return n.value
 
+    def launch_shapes(self):
+        """Shapes of the last likelihood evaluation and the number of
+        workloads whose autotuning has finished (messi_ctx_launch_shapes)."""
+        p, w, t = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self.check(self.lib.messi_ctx_launch_shapes(self.handle, ctypes.byref(p), ctypes.byref(w), ctypes.byref(t)),
+                   "messi_ctx_launch_shapes")
+        return {"prune_shape": p.value, "wave_threads": w.value, "tuned_workloads": t.value}
+
     def graph_replays(self):
         """messi_likelihood calls whose device work replayed a captured CUDA graph."""
         n = ctypes.c_int64()

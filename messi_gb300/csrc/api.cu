@@ -226,6 +226,66 @@ int finish(messi_ctx* ctx)
     return MESSI_OK;
 }
 
+void tune_begin(messi_ctx* ctx, const void* key, int C)
+{
+    ctx->tune_timing = false;
+    ctx->tune_saved[0] = ctx->prune_shape;
+    ctx->tune_saved[1] = ctx->wave_threads;
+    if (!ctx->autotune || (ctx->fixed_prune && ctx->fixed_wave) || ctx->profiling) return;
+    TuneSlot& s = ctx->tune[std::make_pair(key, C)];
+    if (s.done) {
+        if (!ctx->fixed_prune) ctx->prune_shape = s.prune_shape;
+        if (!ctx->fixed_wave) ctx->wave_threads = s.wave_threads;
+    } else {
+        if (!ctx->fixed_prune) ctx->prune_shape = s.k % kPruneShapes;
+        if (!ctx->fixed_wave) ctx->wave_threads = kWaveThreadCands[s.k % kWaveCands];
+        for (int i = 0; i < 4; i++)
+            if (!ctx->tev[i]) cudaEventCreate(&ctx->tev[i]);
+        ctx->tune_timing = true;
+    }
+}
+
+void tune_mark(messi_ctx* ctx, int i)
+{
+    if (ctx->tune_timing) cudaEventRecord(ctx->tev[i], ctx->stream);
+}
+
+void tune_end(messi_ctx* ctx, const void* key, int C)
+{
+    // the shapes of this workload apply to this call only
+    ctx->last_prune_shape = ctx->prune_shape;
+    ctx->last_wave_threads = ctx->wave_threads;
+    ctx->prune_shape = ctx->tune_saved[0];
+    ctx->wave_threads = ctx->tune_saved[1];
+    if (!ctx->tune_timing) return;
+    ctx->tune_timing = false;
+    TuneSlot& s = ctx->tune[std::make_pair(key, C)];
+    float p = 0.f, w = 0.f;
+    if (cudaEventElapsedTime(&p, ctx->tev[0], ctx->tev[1]) != cudaSuccess ||
+        cudaEventElapsedTime(&w, ctx->tev[2], ctx->tev[3]) != cudaSuccess) {
+        cudaGetLastError();
+        s.done = true;  // timing unavailable: keep the defaults
+        return;
+    }
+    s.prune_ms[s.k % kPruneShapes] = std::min(s.prune_ms[s.k % kPruneShapes], (double)p);
+    s.wave_ms[s.k % kWaveCands] = std::min(s.wave_ms[s.k % kWaveCands], (double)w);
+    if (++s.k < kTuneCalls) return;
+    s.done = true;
+    int bp = 0, bw = 0;
+    for (int i = 1; i < kPruneShapes; i++)
+        if (s.prune_ms[i] < s.prune_ms[bp]) bp = i;
+    for (int i = 1; i < kWaveCands; i++)
+        if (s.wave_ms[i] < s.wave_ms[bw]) bw = i;
+    s.prune_shape = (s.prune_ms[bp] < 0.98 * s.prune_ms[0]) ? bp : 0;
+    s.wave_threads = (s.wave_ms[bw] < 0.98 * s.wave_ms[0]) ? kWaveThreadCands[bw] : 0;
+}
+
+void tune_forget(messi_ctx* ctx, const void* key)
+{
+    for (auto it = ctx->tune.begin(); it != ctx->tune.end();)
+        it = (it->first.first == key) ? ctx->tune.erase(it) : std::next(it);
+}
+
 int begin(messi_ctx* ctx)
 {
     if (!ctx) return MESSI_EINVAL;
@@ -279,10 +339,15 @@ int enqueue_likelihood(messi_ctx* ctx, messi_dataset* ds, ModelDev& md, const Ba
             return rc;
         if ((rc = launch_baseline(ctx, t, 1.0))) return rc;
     }
+    tune_mark(ctx, 0);
     if ((rc = run_pairs(ctx, ds, md.P16, md.pi16, md.logw, md.lam, md.cat.C, md.cat.nlam, false))) return rc;
+    tune_mark(ctx, 1);
     if ((rc = join_side(ctx))) return rc;
     if ((rc = launch_bandprep_from_mix(ctx, ds, t, md.gapmask, 1.0, md.cat.logwF, md.logwF))) return rc;
-    return run_inside(ctx, t, 1.0);
+    tune_mark(ctx, 2);
+    if ((rc = run_inside(ctx, t, 1.0))) return rc;
+    tune_mark(ctx, 3);
+    return MESSI_OK;
 }
 
 // Capture enqueue_likelihood into ctx->lgraph (key: what its pointers and
@@ -404,14 +469,20 @@ int messi_ctx_create(int device, messi_ctx** out)
         const char* w = std::getenv("MESSI_WAVE_CTAS");
         if (w) ctx->wave_ctas = std::max(0, std::atoi(w));
         const char* wt = std::getenv("MESSI_WAVE_THREADS");
-        if (wt) ctx->wave_threads = std::atoi(wt);
+        if (wt) {
+            ctx->wave_threads = std::atoi(wt);
+            ctx->fixed_wave = true;
+        }
         const char* gr = std::getenv("MESSI_GRAPHS");
         if (gr && std::atoi(gr) == 0) ctx->graphs = false;
         const char* ps = std::getenv("MESSI_PRUNE_SHAPE");
         if (ps) {
             const int v = std::atoi(ps);
             ctx->prune_shape = (v >= 0 && v <= 2) ? v : 0;
+            ctx->fixed_prune = true;
         }
+        const char* at = std::getenv("MESSI_AUTOTUNE");
+        if (at && std::atoi(at) == 0) ctx->autotune = false;
     }
     *out = ctx;
     return MESSI_OK;
@@ -448,6 +519,8 @@ int messi_ctx_destroy(messi_ctx* ctx)
     cudaStreamSynchronize(ctx->stream);
     prof_collect(ctx);
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->tev)
+        if (e) cudaEventDestroy(e);
     for (auto& b : ctx->scratch)
         if (b.p) cudaFree(b.p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
@@ -488,6 +561,19 @@ int messi_selftest_bounded_wait(messi_ctx* ctx, int32_t* status)
     if ((rc = d2h(ctx, &flag, (unsigned int*)p + 2, sizeof(unsigned int)))) return rc;
     if ((rc = finish(ctx))) return rc;
     *status = flag ? MESSI_ETIMEOUT : MESSI_OK;
+    return MESSI_OK;
+}
+
+int messi_ctx_launch_shapes(messi_ctx* ctx, int32_t* prune_shape, int32_t* wave_threads, int32_t* tuned)
+{
+    if (!ctx) return MESSI_EINVAL;
+    if (prune_shape) *prune_shape = ctx->last_prune_shape;
+    if (wave_threads) *wave_threads = ctx->last_wave_threads;
+    if (tuned) {
+        int n = 0;
+        for (const auto& kv : ctx->tune) n += kv.second.done ? 1 : 0;
+        *tuned = n;
+    }
     return MESSI_OK;
 }
 
@@ -533,6 +619,7 @@ int messi_dataset_destroy(messi_dataset* ds)
             if (ctx->lgraph.exec) cudaGraphExecDestroy(ctx->lgraph.exec);
             ctx->lgraph = LikelihoodGraph{};
         }
+        tune_forget(ctx, ds);
     }
     void* bufs[] = {ds->d_bandidx, ds->d_lr, ds->d_leaf, ds->d_nodes, ds->d_tiles, ds->d_masks, ds->d_tree,
                     ds->d_post, ds->d_arena_f, ds->d_arena_e, ds->d_mix, ds->d_mixlam, ds->d_leafnode,
@@ -687,6 +774,7 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     Band t;
     const int Wb = std::max(0, std::min(ds->W, ds->L - 1));
     if ((rc = band_alloc(ctx, ds->L, Wb, false, &t))) return rc;
+    tune_begin(ctx, ds, md.cat.C);
     LikelihoodKey key;
     key.ds = ds;
     key.C = md.cat.C;
@@ -701,7 +789,7 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     key.wave_ctas = ctx->wave_ctas;
     key.wave_threads = ctx->wave_threads;
     key.prune_shape = ctx->prune_shape;
-    const bool graphs = ctx->graphs && !ctx->profiling;
+    const bool graphs = ctx->graphs && !ctx->profiling && !ctx->tune_timing;
     bool replay = graphs && ctx->lgraph.exec && ctx->lgraph.key == key;
     if (!replay && graphs && ctx->lgraph.seen == key) replay = capture_likelihood(ctx, ds, md, t, key);
     if (replay) {
@@ -715,7 +803,9 @@ int messi_likelihood(messi_ctx* ctx, messi_dataset* ds, const messi_model* model
     }
     if ((rc = d2h(ctx, Z, t.Zd, sizeof(double)))) return rc;
     if (unpaired && (rc = d2h(ctx, unpaired, t.u, (size_t)ds->L * sizeof(double)))) return rc;
-    return finish(ctx);
+    rc = finish(ctx);
+    tune_end(ctx, ds, md.cat.C);
+    return rc;
 }
 
 int messi_inside(messi_ctx* ctx, int32_t L, const double* unpaired, const double* paired, int32_t maxspan, double B,

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -157,6 +158,23 @@ struct LikelihoodKey {
                wave_ctas == o.wave_ctas && wave_threads == o.wave_threads && prune_shape == o.prune_shape;
     }
 };
+// Launch-shape autotuning of one workload (a dataset or a batch at a
+// category count): the first kTuneCalls evaluations run with candidate shapes
+// (pruning pipeline shape k % 3, wavefront CTA size k % 4) and time the
+// pruning and the inside pass with CUDA events; then the fastest of each is
+// kept (the default unless another is at least 2% faster).  Results do not
+// depend on the shapes.
+constexpr int kTuneCalls = 4;
+constexpr int kPruneShapes = 3;
+constexpr int kWaveCands = 4;
+constexpr int kWaveThreadCands[kWaveCands] = {0, 256, 512, 1024};  // 0: chosen by band size
+struct TuneSlot {
+    int k = 0;                       // evaluations timed so far
+    bool done = false;
+    double prune_ms[kPruneShapes] = {INFINITY, INFINITY, INFINITY};
+    double wave_ms[kWaveCands] = {INFINITY, INFINITY, INFINITY, INFINITY};
+    int prune_shape = 0, wave_threads = 0;  // chosen
+};
 struct LikelihoodGraph {
     cudaGraphExec_t exec = nullptr;
     LikelihoodKey key;      // of exec
@@ -201,6 +219,14 @@ struct messi_ctx {
     bool graphs = true;
     messi::LikelihoodGraph lgraph;
     int64_t graph_replays = 0;
+    // launch-shape autotuning (MESSI_AUTOTUNE=0 turns it off; an explicit
+    // MESSI_PRUNE_SHAPE or MESSI_WAVE_THREADS fixes that knob)
+    bool autotune = true, fixed_prune = false, fixed_wave = false;
+    std::map<std::pair<const void*, int>, messi::TuneSlot> tune;
+    cudaEvent_t tev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool tune_timing = false;        // record tev[] around the pruning and the inside pass of this call
+    int tune_saved[2] = {0, 0};      // context shapes restored after a tuned call
+    int last_prune_shape = 0, last_wave_threads = 0;
 };
 
 struct messi_dataset {
@@ -393,6 +419,15 @@ int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandB
 void bandbatch_free(BandBatch* bb);
 int launch_baseline_batch(messi_ctx* ctx, const BandBatch& bb, double B);
 int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B);
+// Autotuning around one evaluation of `key` with C categories (api.cu):
+// tune_begin sets the context's launch shapes for this call (a candidate, or
+// the chosen ones) and arms the timing events; tune_mark(i) records event i
+// (0/1 around the pruning, 2/3 around the inside pass) when armed;
+// tune_end reads the events after the call's stream synchronise.
+void tune_begin(messi_ctx* ctx, const void* key, int C);
+void tune_mark(messi_ctx* ctx, int i);
+void tune_end(messi_ctx* ctx, const void* key, int C);
+void tune_forget(messi_ctx* ctx, const void* key);
 // Queue a copy of the wavefront barrier status into ctx->status_host.
 int queue_status_readback(messi_ctx* ctx, const Band& t);
 
