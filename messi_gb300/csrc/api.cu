@@ -190,7 +190,7 @@ int upload_model(messi_ctx* ctx, messi_dataset* ds, const messi_model* m, bool p
     md->eig4 = (const double*)(base + o_eig4);
     if (pairs) {
         void* p;
-        if ((rc = ensure(ctx, kSlotP16, (size_t)3 * c.C * ds->numnodes * 256 * sizeof(float), &p))) return rc;
+        if ((rc = ensure(ctx, kSlotP16, (size_t)c.C * ds->numnodes * 256 * sizeof(float), &p))) return rc;
         md->P16 = (float*)p;
     }
     if (unpaired) {

@@ -566,7 +566,7 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     const void* old_P = b->P16.p;
     const void* old_P4 = b->P4.p;
     if (grow(b->stage, st.host.size(), &dev)) return fail(ctx, MESSI_ENOMEM, "batch model staging");
-    if (grow(b->P16, (size_t)3 * C * b->total_nodes * 256 * sizeof(float), &pt))
+    if (grow(b->P16, (size_t)C * b->total_nodes * 256 * sizeof(float), &pt))
         return fail(ctx, MESSI_ENOMEM, "batch transition matrices");
     if (grow(b->P4, (size_t)nsite * b->total_nodes * 16 * sizeof(double), &p4))
         return fail(ctx, MESSI_ENOMEM, "batch unpaired transition matrices");

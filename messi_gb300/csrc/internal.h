@@ -319,15 +319,15 @@ void fill_node_descriptors(const messi_dataset* ds, float* arena_f, int* arena_e
 // ---- pruning kernels (prune.cu) ----
 // nodegrp: [numnodes] model group of each node, -1 for a root (nullptr: one
 // tree, root = node 0, group 0).  Category tables are [group][C][...].
-// d_P: [3][C][numnodes][256] FP32: the hi, mid and lo TF32 planes of every
-// transition matrix (their sum is P to ~2^-33).
+// d_P: FP32 matrices [C][numnodes][256] (the pruning kernel splits them into
+// TF32 hi/lo parts in registers).
 int launch_build_P16(messi_ctx* ctx, const double* d_eig, const double* d_bl, const int* d_nodegrp, int numnodes,
                      int C, float* d_P);
 int launch_build_P4(messi_ctx* ctx, const double* d_eig4, const double* d_bl, const int* d_nodegrp, int numnodes,
                     int nsite, double* d_P4);
 // Leaf messages of categories c0 .. c0+nc-1: out[cc][r] = P[c0+cc][rownode[r]]
 // x rows[r] for the R leaf rows (FP64 accumulation, stored FP32); d_P holds
-// the three planes of C categories.
+// C categories.
 int launch_leaf_messages(messi_ctx* ctx, const float* d_rows, const int* d_rownode, int64_t R, const float* d_P,
                          int numnodes, int c0, int nc, int C, float* d_out);
 // The tensor-core node update over `nt` tiles of one level (root tiles when root).

@@ -34,21 +34,7 @@
 
 namespace messi {
 
-// TF32 rounding (to nearest) of a value, returned as the FP32 number the
-// tensor cores read without loss.
-__device__ __forceinline__ float tf32_rn(double v)
-{
-    const float f = (float)v;
-    return __uint_as_float((__float_as_uint(f) + 0x1000u) & 0xffffe000u);
-}
-
-// P[c][v][a][d] (row = parent state) from the FP64 eigensystem, stored as
-// three FP32 planes hi, mid, lo of TF32-exact values with hi + mid + lo = P
-// to about 2^-33 relative: hi = tf32(P), mid = tf32(P - hi),
-// lo = tf32(P - hi - mid).  A single FP32 copy of P would carry a rounding
-// error of up to 2^-24 per entry that is the same for every site pair, so
-// the pair log-likelihoods would all shift together (by ~1e-6 for a
-// 64-sequence tree); the three planes make that common error negligible.
+// P[c][v][a][d] in FP32 (row = parent state), from the FP64 eigensystem.
 __global__ void build_P16_kernel(const double* __restrict__ eig, const double* __restrict__ bl,
                                  const int* __restrict__ nodegrp, int numnodes, int C, float* __restrict__ P)
 {
@@ -64,26 +50,19 @@ __global__ void build_P16_kernel(const double* __restrict__ eig, const double* _
     }
     __syncthreads();
     const int a = t >> 4, d = t & 15;
-    double out;
+    float out;
     if (grp < 0) {
-        out = 0.0;  // a root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
+        out = 0.f;  // a root has no branch (gettransitionmatriceslist, src/FARCE.jl:416)
     } else if (tl == 0.0) {
-        out = (a == d) ? 1.0 : 0.0;
+        out = (a == d) ? 1.f : 0.f;
     } else {
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < 16; k++) s += U[a * 16 + k] * ex[k] * U[d * 16 + k];
         s *= sp[d] / sp[a];
-        out = (s <= 0.0) ? 0.0 : s;  // absmat clamp (1e-50 is below every plane's range)
+        out = (s <= 0.0) ? 0.f : (float)s;  // absmat clamp (1e-50 rounds to 0 in FP32)
     }
-    const float hi = tf32_rn(out);
-    const double r1 = out - (double)hi;
-    const float mid = tf32_rn(r1);
-    const float lo = tf32_rn(r1 - (double)mid);
-    const size_t plane = (size_t)C * numnodes * 256, o = ((size_t)c * numnodes + v) * 256 + t;
-    P[o] = hi;
-    P[plane + o] = mid;
-    P[2 * plane + o] = lo;
+    P[((size_t)c * numnodes + v) * 256 + t] = out;
 }
 
 __global__ void build_P4_kernel(const double* __restrict__ eig4, const double* __restrict__ bl,
@@ -135,8 +114,7 @@ __device__ __forceinline__ double lse_d(double a, double b)
 
 // ---------------------------------------------------------------------------
 // Leaf messages: out[cc][r][a] = sum_d P[c0+cc][node(r)][a][d] * rows[r][d]
-// (16 threads per row; P = the sum of its three planes, FP64 accumulation,
-// one FP32 rounding).
+// (16 threads per row, FP64 accumulation, one FP32 rounding).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) leaf_msg_kernel(const float* __restrict__ rows, const int* __restrict__ rownode,
                                                        long long R, const float* __restrict__ P, int numnodes, int c0,
@@ -145,14 +123,12 @@ __global__ void __launch_bounds__(256) leaf_msg_kernel(const float* __restrict__
     const long long r = (long long)blockIdx.x * 16 + (threadIdx.x >> 4);
     const int a = threadIdx.x & 15, cc = blockIdx.y;
     if (r >= R) return;
-    const size_t plane = (size_t)C * numnodes * 256;
+    (void)C;
     const float* p = P + ((size_t)(c0 + cc) * numnodes + __ldg(rownode + r)) * 256 + a * 16;
     const float* x = rows + r * 16;
     double s = 0.0;
 #pragma unroll
-    for (int d = 0; d < 16; d++)
-        s += ((double)__ldg(p + d) + (double)__ldg(p + plane + d) + (double)__ldg(p + 2 * plane + d)) *
-             (double)__ldg(x + d);
+    for (int d = 0; d < 16; d++) s += (double)__ldg(p + d) * (double)__ldg(x + d);
     out[((size_t)cc * R + r) * 16 + a] = (float)s;
 }
 
@@ -172,10 +148,17 @@ int launch_leaf_messages(messi_ctx* ctx, const float* d_rows, const int* d_rowno
 // and, below the root, the product [32 pairs x 16] x [16 x 16]^T with P of
 // the node's own branch, as m16n8k8 TF32 MMAs with both operands split
 // hi + lo (hi*hi + hi*lo + lo*hi: FP32-level accuracy; all operands are
-// non-negative, so there is no cancellation).  The hi*hi products go to one
-// accumulator and the two small cross terms to another, added once at the
-// end: the tensor core's FP32 accumulation is not round-to-nearest, and this
-// keeps its error in the large sum to two accumulation steps per mat-vec.
+// non-negative, so there is no cancellation).
+// Rounding.  The tensor core rounds each MMA's FP32 result toward zero
+// (measured on GB300: 99.9% of outputs equal the truncation of the exact
+// sum, mean error -0.44 ulp), so a chain of MMAs loses about half an ulp per
+// result, always downwards; over the 62 mat-vecs of a 64-leaf tree that
+// shifted every pair log-likelihood by about -1.2e-6.  Each of the two
+// k-steps therefore accumulates into its own registers (small cross terms
+// first, so their truncation is negligible), the two halves are added in
+// FP32 (round to nearest), and half an ulp of the sum is added back, again
+// rounded to nearest: a tie, which rounds up or down on the last mantissa
+// bit, so the truncation bias of the two halves is returned on average.
 // The contraction index d is permuted so that lane (g, t) owns
 // d = 4t..4t+3: its A fragment for pair row r is one 16-byte load of each
 // child's row, and its B fragment one 16-byte load of P[8nt + g][4t..4t+3].
@@ -208,10 +191,31 @@ __device__ __forceinline__ void split_a(float x, uint32_t& hi, uint32_t& lo)
     lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
-// Dh[mt][nt] += Xh x Ph^T, Dx[mt][nt] += Xl x Ph^T + Xh x Pm^T + Xh x Pl^T
-// for rows g + 8k (k = 0..3); P = Ph + Pm + Pl (the three planes).
-__device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bm)[2],
-                                        const float4 (&Bl)[2], float (&Dh)[2][2][4], float (&Dx)[2][2][4])
+// B operand (four entries of P) split the same way, in registers: one FP32
+// load per fragment instead of a hi and a lo load.
+__device__ __forceinline__ void split_b(const float4& p, float4& hi, float4& lo)
+{
+    uint32_t h[4], l[4];
+    split_a(p.x, h[0], l[0]);
+    split_a(p.y, h[1], l[1]);
+    split_a(p.z, h[2], l[2]);
+    split_a(p.w, h[3], l[3]);
+    hi = make_float4(__uint_as_float(h[0]), __uint_as_float(h[1]), __uint_as_float(h[2]), __uint_as_float(h[3]));
+    lo = make_float4(__uint_as_float(l[0]), __uint_as_float(l[1]), __uint_as_float(l[2]), __uint_as_float(l[3]));
+}
+
+// v + half an ulp of v, rounded to nearest (ties to even): v or v + ulp,
+// each for half of the mantissas.  v >= 0.
+__device__ __forceinline__ float add_half_ulp(float v)
+{
+    const int e = (int)(__float_as_uint(v) & 0x7f800000u) - (24 << 23);
+    return v + __int_as_float(max(e, 0));
+}
+
+// D0[mt][nt] += X x P^T over states k-step 0 (d = 4t, 4t+1), D1 over k-step 1
+// (d = 4t+2, 4t+3), each as lo*hi + hi*lo + hi*hi, for rows g + 8k (k = 0..3).
+__device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)[2], const float4 (&Bl)[2],
+                                        float (&D0)[2][2][4], float (&D1)[2][2][4])
 {
 #pragma unroll
     for (int mt = 0; mt < 2; mt++) {
@@ -225,12 +229,11 @@ __device__ __forceinline__ void msg_mma(const float4 (&X)[4], const float4 (&Bh)
 #pragma unroll
             for (int nt = 0; nt < 2; nt++) {
                 const uint32_t bh0 = __float_as_uint(comp4(Bh[nt], 2 * ks)), bh1 = __float_as_uint(comp4(Bh[nt], 2 * ks + 1));
-                const uint32_t bm0 = __float_as_uint(comp4(Bm[nt], 2 * ks)), bm1 = __float_as_uint(comp4(Bm[nt], 2 * ks + 1));
                 const uint32_t bl0 = __float_as_uint(comp4(Bl[nt], 2 * ks)), bl1 = __float_as_uint(comp4(Bl[nt], 2 * ks + 1));
-                mma_tf32(Dx[mt][nt], ah, bl0, bl1);
-                mma_tf32(Dx[mt][nt], al, bh0, bh1);
-                mma_tf32(Dx[mt][nt], ah, bm0, bm1);
-                mma_tf32(Dh[mt][nt], ah, bh0, bh1);
+                float (&D)[4] = ks ? D1[mt][nt] : D0[mt][nt];
+                mma_tf32(D, al, bh0, bh1);
+                mma_tf32(D, ah, bl0, bl1);
+                mma_tf32(D, ah, bh0, bh1);
             }
         }
     }
@@ -387,31 +390,27 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
         } else {
             // m_v = P_v x (the node's own branch), then an exact power-of-two rescale
             const float* pv = P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256;
-            const size_t plane = (size_t)C * numnodes * 256;
-            float4 Bh[2], Bm[2], Bl[2];
+            float4 Bh[2], Bl[2];
 #pragma unroll
-            for (int nt = 0; nt < 2; nt++) {
-                Bh[nt] = ldg4(pv + (8 * nt + g) * 16 + 4 * t);
-                Bm[nt] = ldg4(pv + plane + (8 * nt + g) * 16 + 4 * t);
-                Bl[nt] = ldg4(pv + 2 * plane + (8 * nt + g) * 16 + 4 * t);
-            }
-            float Dh[2][2][4], Dx[2][2][4];
+            for (int nt = 0; nt < 2; nt++) split_b(ldg4(pv + (8 * nt + g) * 16 + 4 * t), Bh[nt], Bl[nt]);
+            float D0[2][2][4], D1[2][2][4];
 #pragma unroll
             for (int mt = 0; mt < 2; mt++)
 #pragma unroll
                 for (int nt = 0; nt < 2; nt++)
 #pragma unroll
-                    for (int i = 0; i < 4; i++) { Dh[mt][nt][i] = 0.f; Dx[mt][nt][i] = 0.f; }
-            msg_mma(X, Bh, Bm, Bl, Dh, Dx);
-            // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}
+                    for (int i = 0; i < 4; i++) { D0[mt][nt][i] = 0.f; D1[mt][nt][i] = 0.f; }
+            msg_mma(X, Bh, Bl, D0, D1);
+            // V[k][j]: pair g + 8k, states {2t, 2t+1, 8+2t, 9+2t}; the two
+            // k-step halves added, then their truncation returned on average
             float V[4][4];
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 const int mt = k >> 1, h = k & 1;
-                V[k][0] = Dh[mt][0][2 * h] + Dx[mt][0][2 * h];
-                V[k][1] = Dh[mt][0][2 * h + 1] + Dx[mt][0][2 * h + 1];
-                V[k][2] = Dh[mt][1][2 * h] + Dx[mt][1][2 * h];
-                V[k][3] = Dh[mt][1][2 * h + 1] + Dx[mt][1][2 * h + 1];
+                V[k][0] = add_half_ulp(D0[mt][0][2 * h] + D1[mt][0][2 * h]);
+                V[k][1] = add_half_ulp(D0[mt][0][2 * h + 1] + D1[mt][0][2 * h + 1]);
+                V[k][2] = add_half_ulp(D0[mt][1][2 * h] + D1[mt][1][2 * h]);
+                V[k][3] = add_half_ulp(D0[mt][1][2 * h + 1] + D1[mt][1][2 * h + 1]);
             }
             int exk[4];
 #pragma unroll

@@ -169,6 +169,9 @@ def test_c4_fp64_chain_and_posteriors():
     u = api.computeunpairedlikelihoods(ds, params)
     Zg, single, pair = api.computeposteriors(u, mat, maxspan=W)
     e_post = _post_err(single, pair, s_ref, up_ref, lo_ref, W)
+    del s_ref, up_ref, lo_ref
+    _, s_same, up_same, lo_same = co.posteriors_banded(u, mat, W)
+    e_post_same = _post_err(single, pair, s_same, up_same, lo_same, W)
     print(f"\nPARITY c4: pairs max rel {e_pair:.3e}; Z (fused) rel {e_Z:.3e}; posteriors max abs {e_post:.3e} "
-          f"(vs FP64 chain)")
+          f"(vs FP64 chain), {e_post_same:.3e} (same scores)")
     assert e_post <= POST_TOL

@@ -155,6 +155,7 @@ def test_likelihood_graph_replay_equals_eager(c1, monkeypatch):
         p[0:3] *= np.exp(rng.normal(0, 0.1, 3))
         p[14] = min(0.9, max(0.1, p[14] + rng.normal(0, 0.05)))  # lambda-zero weight: the factorised term
         p15s.append(p)
+    monkeypatch.setenv("MESSI_AUTOTUNE", "0")  # graphs from the second call (tuning calls run eagerly)
     ctx = api.Context(0)
     try:
         Zg = [api.computestructureintegratedlikelihood(ds, M.getparams(p, ds.branchlengths), c1.W, ctx=ctx)
@@ -174,7 +175,7 @@ def test_likelihood_graph_replay_equals_eager(c1, monkeypatch):
     assert replays >= 3, replays
 
 
-def test_likelihood_graph_dropped_with_its_dataset(c1):
+def test_likelihood_graph_dropped_with_its_dataset(c1, monkeypatch):
     """A captured likelihood graph holds its dataset's device pointers:
     destroying the dataset drops it, so a dataset created afterwards (which
     may reuse the host address) starts with eager calls and replays only its
@@ -183,6 +184,7 @@ def test_likelihood_graph_dropped_with_its_dataset(c1):
     from messi_gb300 import model as M
     ds = c1.dataset
     params = M.getparams(c1.params15, ds.branchlengths)
+    monkeypatch.setenv("MESSI_AUTOTUNE", "0")
     ctx = api.Context(0)
     handles = []
     try:
@@ -250,3 +252,30 @@ def test_inside_kernels_and_grids_bit_identical(env, monkeypatch):
     assert Z1 == Z0
     for a, b in zip(post1, post0):
         np.testing.assert_array_equal(a, b)
+
+
+def test_autotuner_tries_candidates_then_keeps_one_with_identical_results(c1):
+    """The first evaluations of a dataset time candidate launch shapes (the
+    pruning pipeline shape and the wavefront CTA size); then the chosen
+    shapes are kept, the step is captured and replayed, and every call gives
+    the same bits whatever shape ran it."""
+    from messi_gb300 import api
+    from messi_gb300 import model as M
+    ds = c1.dataset
+    params = M.getparams(c1.params15, ds.branchlengths)
+    ctx = api.Context(0)
+    try:
+        shapes, Z = [], []
+        for _ in range(8):
+            Z.append(api.computestructureintegratedlikelihood(ds, params, c1.W, ctx=ctx))
+            shapes.append(ctx.launch_shapes())
+        assert len(set(Z)) == 1, Z
+        # tuning calls cycle through the candidates (pruning shapes 0, 1, 2, 0;
+        # CTA sizes automatic, 256, 512, 1024)
+        assert [s["prune_shape"] for s in shapes[:4]] == [0, 1, 2, 0]
+        assert [s["wave_threads"] for s in shapes[:4]] == [0, 256, 512, 1024]
+        assert shapes[3]["tuned_workloads"] == 1
+        assert all(s == shapes[4] for s in shapes[4:])
+        assert ctx.graph_replays() >= 2
+    finally:
+        ctx.close()
