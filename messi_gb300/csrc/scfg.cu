@@ -300,8 +300,124 @@ int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_de
 // inside
 // ---------------------------------------------------------------------------
 // Ssuf[i] for spans beyond the band (i < T = L-1-Wb), descending i:
-// Ssuf[i] = r1 + LSE_{k=0..Wb} (Lrow[i][k] + Ssuf[i+k+1]).
-__device__ void inside_suffix_body(const Band& t, const Rules& R)
+// Ssuf[i] = r1 + LSE_{k=0..Wb} (Lrow[i][k] + Ssuf[i+k+1]), a recurrence
+// whose every cell waits for the Wb+1 cells after it.  One CTA, blocks of 32
+// cells from the top.  Every cell keeps a running log-sum-exp (m, s) of the
+// terms whose S cell is already final, in shared memory over a window of
+// cells (slot c % win): first the terms into the band's last column (j >= T),
+// then, each time a block is final, its 32 values are pushed into the cells
+// that reference them.  Warp 0 pushes into the next block's cells, in
+// registers, and solves that block's in-block triangle by column-oriented
+// substitution; meanwhile the other warps push into the farther cells; one
+// CTA barrier per block.  (The former form pulled each block's Wb+1 terms
+// per cell from global memory after the block above was final: about 10 us
+// per block, 2.7 ms for the 8,199 suffix cells of a 9,000-column alignment
+// with span 800.)
+constexpr int kSuffixMaxWindow = 24576;  // cells of the shared-memory window (192 KB)
+
+__host__ __device__ inline int suffix_window(int Wb) { return Wb + 64; }
+
+__device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, float* as, int win)
+{
+    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    const int T = L - 1 - Wb;
+    if (T <= 0) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __shared__ float tri[32][33];
+    // finished block values, double-buffered: the far pushes of one block may
+    // still read them while warp 0 solves the next block
+    __shared__ float vals2[2][32];
+    int parity = 0;
+    for (int c = threadIdx.x; c < win; c += blockDim.x) {
+        am[c] = -INFINITY;
+        as[c] = 0.f;
+    }
+    __syncthreads();
+    // terms into the band's last column: cells T-1 down to T-1-Wb
+    const int c_first = max(0, T - 1 - Wb);
+    for (int c = T - 1 - w; c >= c_first; c -= nw) {
+        float m = -INFINITY, s = 0.f;
+        const float* lrow = t.Lrow + (size_t)c * RS;
+        const int k1 = min(L - 1, c + Wb + 1) - c - 1;
+        for (int k = (T - c - 1) + lane; k <= k1; k += 32) lse_add(m, s, __ldg(lrow + k) + t.Ssuf[c + k + 1]);
+        group_reduce<32>(m, s);
+        if (lane == 0) {
+            am[c % win] = m;
+            as[c % win] = s;
+        }
+    }
+    __syncthreads();
+    int i0 = T - 1, lo = max(0, i0 - 31);
+    float cm = -INFINITY, cs = 0.f;  // warp 0: accumulator of cell i0 - lane
+    if (w == 0) {
+        const int c = i0 - lane;
+        if (c >= lo) {
+            cm = am[c % win];
+            cs = as[c % win];
+        }
+        for (int k = 0; k < 32; k++) tri[lane][k] = (c >= lo && k <= Wb) ? __ldg(t.Lrow + (size_t)c * RS + k) : -INFINITY;
+        __syncwarp();
+    }
+    for (;;) {
+        const int nb = i0 - lo + 1;
+        float* vals = vals2[parity];
+        parity ^= 1;
+        if (w == 0) {
+            float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
+            for (int l = 0; l < nb; l++) {
+                const float sv = __shfl_sync(0xffffffffu, R.r[0] + lse_val(m, s), l);
+                if (lane == 0) {
+                    t.Ssuf[i0 - l] = sv;
+                    vals[l] = sv;
+                }
+                const int k = lane - l - 1;
+                if (lane > l && lane < nb && k <= Wb) lse_add(m, s, tri[lane][k] + sv);
+            }
+        }
+        __syncthreads();
+        if (lo == 0) break;
+        // push the block [lo, i0] into the cells lo-1 .. lo-1-Wb (a cell's first
+        // push starts it afresh unless the band already gave it terms)
+        const int nlo = max(0, lo - 32);
+        if (w == 0) {
+            const int c = lo - 1 - lane;
+            if (c >= nlo) {
+                const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
+                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
+                const float* lrow = t.Lrow + (size_t)c * RS;
+                for (int q = 0; q < nb; q++) {
+                    const int k = i0 - q - c - 1;
+                    if (k <= Wb) lse_add(m, s, __ldg(lrow + k) + vals[q]);
+                }
+                cm = m;
+                cs = s;
+                for (int k = 0; k < 32; k++) tri[lane][k] = (k <= Wb) ? __ldg(lrow + k) : -INFINITY;
+            } else {
+                cm = -INFINITY;
+                cs = 0.f;
+            }
+            __syncwarp();
+        } else {
+            for (int c = nlo - 1 - (threadIdx.x - 32); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 32) {
+                const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
+                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
+                const float* lrow = t.Lrow + (size_t)c * RS;
+                for (int q = 0; q < nb; q++) {
+                    const int k = i0 - q - c - 1;
+                    if (k <= Wb) lse_add(m, s, __ldg(lrow + k) + vals[q]);
+                }
+                am[c % win] = m;
+                as[c % win] = s;
+            }
+        }
+        i0 = lo - 1;
+        lo = nlo;
+    }
+}
+
+// Blocks of 32 cells pulled from global memory (bands wider than the
+// shared-memory window of the pushing form).
+__device__ void inside_suffix_body_pull(const Band& t, const Rules& R)
 {
     const int T = t.L - 1 - t.Wb;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -339,13 +455,54 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R)
     }
 }
 
-__global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R) { inside_suffix_body(t, R); }
+__device__ void inside_suffix_any(const Band& t, const Rules& R, float* smem, int win)
+{
+    if (suffix_window(t.Wb) <= win) inside_suffix_body(t, R, smem, smem + win, win);
+    else inside_suffix_body_pull(t, R);
+}
+
+// win: cells of the dynamic shared-memory window (2 * win floats)
+__global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R, int win)
+{
+    extern __shared__ float suffix_smem[];
+    inside_suffix_any(t, R, suffix_smem, win);
+}
 
 // one block per alignment of a batch (alignments whose band reaches the last column skip)
-__global__ void __launch_bounds__(1024) inside_suffix_batch_kernel(const Band* __restrict__ bands, Rules R)
+__global__ void __launch_bounds__(1024) inside_suffix_batch_kernel(const Band* __restrict__ bands, Rules R, int win)
 {
+    extern __shared__ float suffix_smem[];
     const Band t = bands[blockIdx.x];
-    if (t.L - 1 > t.Wb) inside_suffix_body(t, R);
+    if (t.L - 1 > t.Wb) inside_suffix_any(t, R, suffix_smem, win);
+}
+
+// Window for the largest band that needs a suffix (0: none fits, the pull form runs).
+static int suffix_launch_window(int maxWb)
+{
+    const int win = suffix_window(maxWb);
+    return (win <= kSuffixMaxWindow) ? win : 0;
+}
+
+// The window for a batch: the widest band among those that take the pushing
+// form (a band too wide for any window takes the pull form in a single call
+// too, so both paths give the same bits).
+static int suffix_batch_window(const BandBatch& bb)
+{
+    int win = 0;
+    for (const Band& t : bb.host)
+        if (t.L - 1 > t.Wb && suffix_window(t.Wb) <= kSuffixMaxWindow) win = std::max(win, suffix_window(t.Wb));
+    return win;
+}
+
+static cudaError_t suffix_smem_attr(int win)
+{
+    const int bytes = 2 * win * (int)sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(inside_suffix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         std::max(bytes, 0));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(inside_suffix_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 std::max(bytes, 0));
+    return e;
 }
 
 __global__ void finish_Z_kernel(Band t)
@@ -1084,7 +1241,10 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
         prof_begin(ctx, 2, (double)(t.L - 1 - t.Wb));
-        inside_suffix_kernel<<<1, 1024, 0, ctx->stream>>>(t, R);
+        const int win = suffix_launch_window(t.Wb);
+        cudaError_t e = suffix_smem_attr(win);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_suffix_kernel attributes");
+        inside_suffix_kernel<<<1, 1024, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
         LAUNCH_CHECK(ctx, "inside_suffix_kernel");
         prof_end(ctx);
     }
@@ -1223,7 +1383,10 @@ int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
     if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_wave_batch_kernel");
     prof_end(ctx);
     prof_begin(ctx, 2, 0.0);
-    inside_suffix_batch_kernel<<<n, 1024, 0, ctx->stream>>>(bands, R);
+    const int win = suffix_batch_window(bb);
+    e = suffix_smem_attr(win);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_suffix_batch_kernel attributes");
+    inside_suffix_batch_kernel<<<n, 1024, (size_t)2 * win * sizeof(float), ctx->stream>>>(bands, R, win);
     LAUNCH_CHECK(ctx, "inside_suffix_batch_kernel");
     prof_end(ctx);
     finish_Z_batch_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(bands, n, sync, bb.d_Z);
@@ -1238,7 +1401,95 @@ int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
 // ---------------------------------------------------------------------------
 // Osuf[i] for spans beyond the band on the last column, ascending i:
 // Osuf[0] = 0;  Osuf[i] = r1 + LSE_{k=0..Wb, i-k-1>=0} (Osuf[i-k-1] + Lcol[i-1][k]).
-__global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
+// Osuf[i] (outside of S(i, L-1) beyond the band, i < T = L-1-Wb), ascending
+// i: Osuf[0] = 0, Osuf[i] = r1 + LSE_{k=0..min(Wb, i-1)} (Osuf[i-k-1] +
+// Lcol[i-1][k]).  The mirror of the inside suffix: blocks of 32 cells from
+// the bottom, every finished block pushed into the next Wb+1 cells'
+// shared-memory accumulators (warp 0 into the next block and its triangle,
+// the other warps into the farther cells, one barrier per block).
+__device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, float* as, int win)
+{
+    const int Wb = t.Wb, RS = t.RS;
+    const int T = t.L - 1 - Wb;
+    if (T <= 0) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ float tri[32][33];  // Lcol[c - 1][k], k < 32, for the block's cells c
+    __shared__ float vals2[2][32];
+    int parity = 0;
+    for (int c = threadIdx.x; c < win; c += blockDim.x) {
+        am[c] = -INFINITY;
+        as[c] = 0.f;
+    }
+    int i0 = 0, hi = min(T - 1, 31);
+    float cm = -INFINITY, cs = 0.f;
+    if (w == 0) {
+        const int c = i0 + lane;
+        for (int k = 0; k < 32; k++)
+            tri[lane][k] = (c <= hi && c >= 1 && k <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + k) : -INFINITY;
+        __syncwarp();
+    }
+    __syncthreads();
+    for (;;) {
+        const int nb = hi - i0 + 1;
+        float* vals = vals2[parity];
+        parity ^= 1;
+        if (w == 0) {
+            float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
+            for (int l = 0; l < nb; l++) {
+                const int ic = i0 + l;
+                const float fin = (ic == 0) ? 0.f : R.r[0] + lse_val(m, s);
+                const float sv = __shfl_sync(0xffffffffu, fin, l);
+                if (lane == 0) {
+                    t.Osuf[ic] = sv;
+                    vals[l] = sv;
+                }
+                const int k = lane - l - 1;
+                if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1) lse_add(m, s, tri[lane][k] + sv);
+            }
+        }
+        __syncthreads();
+        if (hi == T - 1) break;
+        // push the block [i0, hi] into the cells hi+1 .. hi+1+Wb; a cell's first
+        // push (from the block holding its smallest referenced cell) starts it afresh
+        const int nhi = min(T - 1, hi + 32);
+        if (w == 0) {
+            const int c = hi + 1 + lane;
+            if (c <= nhi) {
+                const bool fresh = i0 <= max(0, c - 1 - Wb);
+                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
+                const float* lcol = t.Lcol + (size_t)(c - 1) * RS;
+                for (int q = 0; q < nb; q++) {
+                    const int k = c - (i0 + q) - 1;
+                    if (k <= Wb) lse_add(m, s, vals[q] + __ldg(lcol + k));
+                }
+                cm = m;
+                cs = s;
+                for (int k = 0; k < 32; k++) tri[lane][k] = (k <= Wb) ? __ldg(lcol + k) : -INFINITY;
+            } else {
+                cm = -INFINITY;
+                cs = 0.f;
+            }
+            __syncwarp();
+        } else {
+            for (int c = nhi + 1 + (threadIdx.x - 32); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 32) {
+                const bool fresh = i0 <= max(0, c - 1 - Wb);
+                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
+                const float* lcol = t.Lcol + (size_t)(c - 1) * RS;
+                for (int q = 0; q < nb; q++) {
+                    const int k = c - (i0 + q) - 1;
+                    if (k <= Wb) lse_add(m, s, vals[q] + __ldg(lcol + k));
+                }
+                am[c % win] = m;
+                as[c % win] = s;
+            }
+        }
+        i0 = hi + 1;
+        hi = nhi;
+    }
+}
+
+// Blocks of 32 cells pulled from global memory (bands wider than the window).
+__device__ void outside_suffix_body_pull(const Band& t, const Rules& R)
 {
     const int T = t.L - 1 - t.Wb;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1280,11 +1531,22 @@ __global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R)
     }
 }
 
+__global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R, int win)
+{
+    extern __shared__ float suffix_smem[];
+    if (suffix_window(t.Wb) <= win) outside_suffix_body(t, R, suffix_smem, suffix_smem + win, win);
+    else outside_suffix_body_pull(t, R);
+}
+
 int run_outside(messi_ctx* ctx, const Band& t, double B)
 {
     Rules R = make_rules(B);
     if (t.L - 1 > t.Wb) {
-        outside_suffix_kernel<<<1, 1024, 0, ctx->stream>>>(t, R);
+        const int win = suffix_launch_window(t.Wb);
+        cudaError_t e = cudaFuncSetAttribute(outside_suffix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             2 * win * (int)sizeof(float));
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "outside_suffix_kernel attributes");
+        outside_suffix_kernel<<<1, 1024, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
         LAUNCH_CHECK(ctx, "outside_suffix_kernel");
     }
     Band tt = t;

