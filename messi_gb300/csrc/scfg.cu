@@ -315,6 +315,25 @@ int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_de
 // with span 800.)
 constexpr int kSuffixMaxWindow = 24576;  // cells of the shared-memory window (192 KB)
 
+// Adds the terms x[q] = row[kbase - q] + vals[q] for q < nb (and row index
+// <= Wb) to (m, s): the 32 loads are issued together, then summed in blocks
+// of eight.
+__device__ __forceinline__ void suffix_push_terms(float& m, float& s, const float* __restrict__ row, int kbase,
+                                                  int dk, const float* vals, int nb, int Wb)
+{
+    float x[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) {
+        const int k = kbase + dk * q;
+        x[q] = (q < nb && k >= 0 && k <= Wb) ? __ldg(row + k) + vals[q] : -INFINITY;
+    }
+#pragma unroll
+    for (int q = 0; q < 32; q += 8) {
+        const float y[8] = {x[q], x[q + 1], x[q + 2], x[q + 3], x[q + 4], x[q + 5], x[q + 6], x[q + 7]};
+        lse_add8(m, s, y);
+    }
+}
+
 __host__ __device__ inline int suffix_window(int Wb) { return Wb + 64; }
 
 __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, float* as, int win)
@@ -339,7 +358,15 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         float m = -INFINITY, s = 0.f;
         const float* lrow = t.Lrow + (size_t)c * RS;
         const int k1 = min(L - 1, c + Wb + 1) - c - 1;
-        for (int k = (T - c - 1) + lane; k <= k1; k += 32) lse_add(m, s, __ldg(lrow + k) + t.Ssuf[c + k + 1]);
+        for (int k = (T - c - 1) + lane; k <= k1; k += 256) {
+            float x[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int kq = k + 32 * q;
+                x[q] = (kq <= k1) ? __ldg(lrow + kq) + t.Ssuf[c + kq + 1] : -INFINITY;
+            }
+            lse_add8(m, s, x);
+        }
         group_reduce<32>(m, s);
         if (lane == 0) {
             am[c % win] = m;
@@ -385,10 +412,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
                 const float* lrow = t.Lrow + (size_t)c * RS;
-                for (int q = 0; q < nb; q++) {
-                    const int k = i0 - q - c - 1;
-                    if (k <= Wb) lse_add(m, s, __ldg(lrow + k) + vals[q]);
-                }
+                suffix_push_terms(m, s, lrow, i0 - c - 1, -1, vals, nb, Wb);
                 cm = m;
                 cs = s;
                 for (int k = 0; k < 32; k++) tri[lane][k] = (k <= Wb) ? __ldg(lrow + k) : -INFINITY;
@@ -402,10 +426,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
                 const float* lrow = t.Lrow + (size_t)c * RS;
-                for (int q = 0; q < nb; q++) {
-                    const int k = i0 - q - c - 1;
-                    if (k <= Wb) lse_add(m, s, __ldg(lrow + k) + vals[q]);
-                }
+                suffix_push_terms(m, s, lrow, i0 - c - 1, -1, vals, nb, Wb);
                 am[c % win] = m;
                 as[c % win] = s;
             }
@@ -1458,10 +1479,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
                 const float* lcol = t.Lcol + (size_t)(c - 1) * RS;
-                for (int q = 0; q < nb; q++) {
-                    const int k = c - (i0 + q) - 1;
-                    if (k <= Wb) lse_add(m, s, vals[q] + __ldg(lcol + k));
-                }
+                suffix_push_terms(m, s, lcol, c - i0 - 1, -1, vals, nb, Wb);
                 cm = m;
                 cs = s;
                 for (int k = 0; k < 32; k++) tri[lane][k] = (k <= Wb) ? __ldg(lcol + k) : -INFINITY;
@@ -1475,10 +1493,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
                 const float* lcol = t.Lcol + (size_t)(c - 1) * RS;
-                for (int q = 0; q < nb; q++) {
-                    const int k = c - (i0 + q) - 1;
-                    if (k <= Wb) lse_add(m, s, vals[q] + __ldg(lcol + k));
-                }
+                suffix_push_terms(m, s, lcol, c - i0 - 1, -1, vals, nb, Wb);
                 am[c % win] = m;
                 as[c % win] = s;
             }
