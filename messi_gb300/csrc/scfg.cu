@@ -306,35 +306,40 @@ int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_de
 // terms whose S cell is already final, in shared memory over a window of
 // cells (slot c % win): first the terms into the band's last column (j >= T),
 // then, each time a block is final, its 32 values are pushed into the cells
-// that reference them.  Warp 0 pushes into the next block's cells, in
-// registers, and solves that block's in-block triangle by column-oriented
-// substitution; meanwhile the other warps push into the farther cells; one
-// CTA barrier per block.  (The former form pulled each block's Wb+1 terms
-// per cell from global memory after the block above was final: about 10 us
-// per block, 2.7 ms for the 8,199 suffix cells of a 9,000-column alignment
-// with span 800.)
+// that reference them.  A push of S cell j into cell c adds L(c, j-1) +
+// Ssuf[j]; for fixed j, L(c, j-1) = Lcol[j-1][j-1-c] is contiguous in c, so
+// threads that own consecutive cells load consecutive words.  Warp 0 pushes
+// into the next block's cells and solves that block's in-block triangle by
+// column-oriented substitution; meanwhile the other warps push into the
+// farther cells; one CTA barrier per block.  (The former form pulled each
+// block's Wb+1 terms per cell from global memory after the block above was
+// final: 2.7 ms for the 8,199 suffix cells of a 9,000-column alignment with
+// span 800.)
 constexpr int kSuffixMaxWindow = 24576;  // cells of the shared-memory window (192 KB)
 
-// Adds the terms x[q] = row[kbase - q] + vals[q] for q < nb (and row index
-// <= Wb) to (m, s): the 32 loads are issued together, then summed in blocks
-// of eight.
-__device__ __forceinline__ void suffix_push_terms(float& m, float& s, const float* __restrict__ row, int kbase,
-                                                  int dk, const float* vals, int nb, int Wb)
+__host__ __device__ inline int suffix_window(int Wb) { return Wb + 64; }
+
+// Adds to (m, s) the terms col[u] + vals[u] for the block's values u < nb,
+// where col[u] = tab[(jbase + dj*u) * RS + kbase + dk*u] (the L cell that
+// joins this thread's cell to value u; skipped when its band offset is
+// outside 0..Wb): the 32 loads are issued together, then summed in blocks of
+// eight.
+__device__ __forceinline__ void suffix_push_terms(float& m, float& s, const float* __restrict__ tab, int RS,
+                                                  int jbase, int dj, int kbase, int dk, const float* vals, int nb,
+                                                  int Wb)
 {
     float x[32];
 #pragma unroll
-    for (int q = 0; q < 32; q++) {
-        const int k = kbase + dk * q;
-        x[q] = (q < nb && k >= 0 && k <= Wb) ? __ldg(row + k) + vals[q] : -INFINITY;
+    for (int u = 0; u < 32; u++) {
+        const int k = kbase + dk * u;
+        x[u] = (u < nb && k >= 0 && k <= Wb) ? __ldg(tab + (size_t)(jbase + dj * u) * RS + k) + vals[u] : -INFINITY;
     }
 #pragma unroll
-    for (int q = 0; q < 32; q += 8) {
-        const float y[8] = {x[q], x[q + 1], x[q + 2], x[q + 3], x[q + 4], x[q + 5], x[q + 6], x[q + 7]};
+    for (int u = 0; u < 32; u += 8) {
+        const float y[8] = {x[u], x[u + 1], x[u + 2], x[u + 3], x[u + 4], x[u + 5], x[u + 6], x[u + 7]};
         lse_add8(m, s, y);
     }
 }
-
-__host__ __device__ inline int suffix_window(int Wb) { return Wb + 64; }
 
 __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, float* as, int win)
 {
@@ -342,7 +347,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     const int T = L - 1 - Wb;
     if (T <= 0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    __shared__ float tri[32][33];
+    __shared__ float tri[32][33];  // tri[q][k] = Lrow[i0 - q][k]: the in-block terms of the block's cells
     // finished block values, double-buffered: the far pushes of one block may
     // still read them while warp 0 solves the next block
     __shared__ float vals2[2][32];
@@ -352,7 +357,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         as[c] = 0.f;
     }
     __syncthreads();
-    // terms into the band's last column: cells T-1 down to T-1-Wb
+    // terms into the band's last column: cells T-1 down to T-1-Wb, a warp per cell
     const int c_first = max(0, T - 1 - Wb);
     for (int c = T - 1 - w; c >= c_first; c -= nw) {
         float m = -INFINITY, s = 0.f;
@@ -373,17 +378,15 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
             as[c % win] = s;
         }
     }
-    __syncthreads();
     int i0 = T - 1, lo = max(0, i0 - 31);
+    if (w == 0)
+        for (int q = 0; q < 32; q++)
+            tri[q][lane] = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
+    __syncthreads();
     float cm = -INFINITY, cs = 0.f;  // warp 0: accumulator of cell i0 - lane
-    if (w == 0) {
-        const int c = i0 - lane;
-        if (c >= lo) {
-            cm = am[c % win];
-            cs = as[c % win];
-        }
-        for (int k = 0; k < 32; k++) tri[lane][k] = (c >= lo && k <= Wb) ? __ldg(t.Lrow + (size_t)c * RS + k) : -INFINITY;
-        __syncwarp();
+    if (w == 0 && i0 - lane >= lo) {
+        cm = am[(i0 - lane) % win];
+        cs = as[(i0 - lane) % win];
     }
     for (;;) {
         const int nb = i0 - lo + 1;
@@ -403,30 +406,31 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         }
         __syncthreads();
         if (lo == 0) break;
-        // push the block [lo, i0] into the cells lo-1 .. lo-1-Wb (a cell's first
-        // push starts it afresh unless the band already gave it terms)
+        // push the block [lo, i0] (value u = S cell i0 - u) into the cells
+        // lo-1 .. lo-1-Wb; a cell's first push starts it afresh unless the
+        // band already gave it terms
         const int nlo = max(0, lo - 32);
         if (w == 0) {
             const int c = lo - 1 - lane;
+            cm = -INFINITY;
+            cs = 0.f;
             if (c >= nlo) {
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
-                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
-                const float* lrow = t.Lrow + (size_t)c * RS;
-                suffix_push_terms(m, s, lrow, i0 - c - 1, -1, vals, nb, Wb);
-                cm = m;
-                cs = s;
-                for (int k = 0; k < 32; k++) tri[lane][k] = (k <= Wb) ? __ldg(lrow + k) : -INFINITY;
-            } else {
-                cm = -INFINITY;
-                cs = 0.f;
+                if (!fresh) {
+                    cm = am[c % win];
+                    cs = as[c % win];
+                }
+                suffix_push_terms(cm, cs, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, -1, vals, nb, Wb);
             }
+            for (int q = 0; q < 32; q++)
+                tri[q][lane] = (lo - 1 - q >= nlo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane)
+                                                                 : -INFINITY;
             __syncwarp();
         } else {
             for (int c = nlo - 1 - (threadIdx.x - 32); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 32) {
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
-                const float* lrow = t.Lrow + (size_t)c * RS;
-                suffix_push_terms(m, s, lrow, i0 - c - 1, -1, vals, nb, Wb);
+                suffix_push_terms(m, s, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, -1, vals, nb, Wb);
                 am[c % win] = m;
                 as[c % win] = s;
             }
@@ -1434,7 +1438,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
     const int T = t.L - 1 - Wb;
     if (T <= 0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __shared__ float tri[32][33];  // Lcol[c - 1][k], k < 32, for the block's cells c
+    __shared__ float tri[32][33];  // tri[q][k] = Lcol[i0 + q - 1][k] for the block's cells i0 + q
     __shared__ float vals2[2][32];
     int parity = 0;
     for (int c = threadIdx.x; c < win; c += blockDim.x) {
@@ -1442,14 +1446,13 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
         as[c] = 0.f;
     }
     int i0 = 0, hi = min(T - 1, 31);
-    float cm = -INFINITY, cs = 0.f;
-    if (w == 0) {
-        const int c = i0 + lane;
-        for (int k = 0; k < 32; k++)
-            tri[lane][k] = (c <= hi && c >= 1 && k <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + k) : -INFINITY;
-        __syncwarp();
-    }
+    if (w == 0)
+        for (int q = 0; q < 32; q++) {
+            const int c = i0 + q;
+            tri[q][lane] = (c <= hi && c >= 1 && lane <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + lane) : -INFINITY;
+        }
     __syncthreads();
+    float cm = -INFINITY, cs = 0.f;
     for (;;) {
         const int nb = hi - i0 + 1;
         float* vals = vals2[parity];
@@ -1470,30 +1473,33 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
         }
         __syncthreads();
         if (hi == T - 1) break;
-        // push the block [i0, hi] into the cells hi+1 .. hi+1+Wb; a cell's first
-        // push (from the block holding its smallest referenced cell) starts it afresh
+        // push the block [i0, hi] (value u = cell i0 + u) into the cells
+        // hi+1 .. hi+1+Wb: L(i0 + u, c - 1) = Lrow[i0 + u][c - 1 - i0 - u],
+        // contiguous in c; a cell's first push (from the block holding its
+        // smallest referenced cell) starts it afresh
         const int nhi = min(T - 1, hi + 32);
         if (w == 0) {
             const int c = hi + 1 + lane;
+            cm = -INFINITY;
+            cs = 0.f;
             if (c <= nhi) {
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
-                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
-                const float* lcol = t.Lcol + (size_t)(c - 1) * RS;
-                suffix_push_terms(m, s, lcol, c - i0 - 1, -1, vals, nb, Wb);
-                cm = m;
-                cs = s;
-                for (int k = 0; k < 32; k++) tri[lane][k] = (k <= Wb) ? __ldg(lcol + k) : -INFINITY;
-            } else {
-                cm = -INFINITY;
-                cs = 0.f;
+                if (!fresh) {
+                    cm = am[c % win];
+                    cs = as[c % win];
+                }
+                suffix_push_terms(cm, cs, t.Lrow, RS, i0, 1, c - 1 - i0, -1, vals, nb, Wb);
+            }
+            for (int q = 0; q < 32; q++) {
+                const int cq = hi + 1 + q;
+                tri[q][lane] = (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
             }
             __syncwarp();
         } else {
             for (int c = nhi + 1 + (threadIdx.x - 32); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 32) {
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
-                const float* lcol = t.Lcol + (size_t)(c - 1) * RS;
-                suffix_push_terms(m, s, lcol, c - i0 - 1, -1, vals, nb, Wb);
+                suffix_push_terms(m, s, t.Lrow, RS, i0, 1, c - 1 - i0, -1, vals, nb, Wb);
                 am[c % win] = m;
                 as[c % win] = s;
             }
