@@ -11,12 +11,13 @@
 // forward/backward kernels read); activations are BF16, and so are the
 // gradient operands of the backward GEMMs (rounded while a tile is staged);
 // every product is accumulated in FP32.  Every GEMM runs on the tensor cores
-// (gemm_bf16_kernel: 64 x 64 CTA tiles, four warps of 32 x 32, BF16
+// (gemm_bf16_kernel: 32 x 32 CTA tiles, four warps of 16 x 16, BF16
 // mma.sync m16n8k16 with FP32 accumulators) with its epilogue fused: bias,
 // bias + SiLU (writing the FP32 pre-activation and the BF16 activation), or
 // the SiLU derivative of the backward pass.  The network is small (batch a
-// few hundred, width 256), so a GEMM is a few CTAs and latency bound; the
-// fused epilogues remove the elementwise launches between the GEMMs.
+// few hundred, width 256), so a GEMM is latency bound: small tiles for more
+// CTAs, a 256-wide K chunk staged per barrier, and the fused epilogues
+// remove the elementwise launches between the GEMMs.
 //
 // Head per sample: [K logits | K*D means | K*D log-sd]; the loss is the
 // negative log-likelihood of a target vector under the mixture.
@@ -58,7 +59,11 @@ __device__ __forceinline__ float dsilu(float z);
 __device__ __forceinline__ __nv_bfloat16 to_bf(float v) { return __float2bfloat16(v); }
 __device__ __forceinline__ __nv_bfloat16 to_bf(__nv_bfloat16 v) { return v; }
 
-constexpr int kBM = 64, kBN = 64, kBK = 32, kPad = 8;  // CTA tile, k step, row padding (bf16)
+// CTA tile 32 x 32 (four warps of 16 x 16), the K extent staged in chunks of
+// kBK: the GEMMs of this network are a few hundred rows, so the CTA count,
+// not the per-CTA rate, bounds them; a whole chunk's loads are issued before
+// the one CTA barrier, so a chunk costs one memory round trip.
+constexpr int kBM = 32, kBN = 32, kBK = 256, kPad = 8;
 
 // GEMM epilogues
 enum GemmMode {
@@ -79,8 +84,8 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 
 // C[m][n] (row stride scm) = epilogue(sum_k A(m, k) * B(k, n)) with
 // A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn]; operands are rounded
-// to BF16 as the tile is staged in shared memory ([row][k], k contiguous,
-// rows padded by 8 so the fragment loads hit 32 distinct banks).
+// to BF16 as they are staged in shared memory ([row][k], k contiguous, rows
+// padded by 8 so the fragment loads hit 32 distinct banks).
 template <typename TA, typename TB>
 __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, const TA* __restrict__ A, long long sam,
                                                         long long sak, const TB* __restrict__ B, long long sbk,
@@ -92,74 +97,71 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, con
     __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kBK + kPad];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int wm = (warp >> 1) * 16, wn = (warp & 1) * 16;
     const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-    float acc[2][4][4];
+    float acc[2][4];
 #pragma unroll
-    for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
 #pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
+        for (int q = 0; q < 4; q++) acc[j][q] = 0.f;
     // consecutive threads walk the operand's unit-stride index (coalesced)
     const bool a_k_fast = (sak == 1), b_k_fast = (sbk == 1);
     for (int k0 = 0; k0 < K; k0 += kBK) {
+        const int kc = min(kBK, K - k0);
+        const int kc16 = (kc + 15) & ~15;  // chunk rounded up to whole k16 steps (zero padded)
+        if (k0 > 0) __syncthreads();
+#pragma unroll 8
         for (int e = tid; e < kBM * kBK; e += 128) {
             const int r = a_k_fast ? e / kBK : e % kBM, c = a_k_fast ? e % kBK : e / kBM;
-            const int m = m0 + r, k = k0 + c;
-            As[r][c] = (m < M && k < K) ? to_bf(A[m * sam + k * sak]) : __float2bfloat16(0.f);
+            if (c < kc16) {
+                const int m = m0 + r, k = k0 + c;
+                As[r][c] = (m < M && c < kc) ? to_bf(A[m * sam + k * sak]) : __float2bfloat16(0.f);
+            }
             const int r2 = b_k_fast ? e / kBK : e % kBN, c2 = b_k_fast ? e % kBK : e / kBN;
-            const int n = n0 + r2, kk = k0 + c2;
-            Bs[r2][c2] = (n < N && kk < K) ? to_bf(B[kk * sbk + n * sbn]) : __float2bfloat16(0.f);
+            if (c2 < kc16) {
+                const int n = n0 + r2, kk = k0 + c2;
+                Bs[r2][c2] = (n < N && c2 < kc) ? to_bf(B[kk * sbk + n * sbn]) : __float2bfloat16(0.f);
+            }
         }
         __syncthreads();
+        for (int ks = 0; ks < kc16; ks += 16) {
+            uint32_t af[4], bf[2][2];
+            const int r = wm + g;
+            af[0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t]);
+            af[1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t]);
+            af[2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t + 8]);
+            af[3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t + 8]);
 #pragma unroll
-        for (int ks = 0; ks < kBK; ks += 16) {
-            uint32_t af[2][4], bf[4][2];
-#pragma unroll
-            for (int mt = 0; mt < 2; mt++) {
-                const int r = wm + mt * 16 + g;
-                af[mt][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t]);
-                af[mt][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t]);
-                af[mt][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t + 8]);
-                af[mt][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t + 8]);
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
+            for (int nt = 0; nt < 2; nt++) {
                 const int c = wn + nt * 8 + g;
                 bf[nt][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * t]);
                 bf[nt][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * t + 8]);
             }
 #pragma unroll
-            for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-                for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
+            for (int nt = 0; nt < 2; nt++) mma_bf16(acc[nt], af, bf[nt][0], bf[nt][1]);
         }
-        __syncthreads();
     }
 #pragma unroll
-    for (int mt = 0; mt < 2; mt++)
+    for (int nt = 0; nt < 2; nt++)
 #pragma unroll
-        for (int nt = 0; nt < 4; nt++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int m = m0 + wm + mt * 16 + g + 8 * (q >> 1);
-                const int n = n0 + wn + nt * 8 + 2 * t + (q & 1);
-                if (m >= M || n >= N) continue;
-                const long long o = m * scm + n;
-                const float v = acc[mt][nt][q];
-                if (mode == kStoreBias) {
-                    C[o] = v + (bias ? bias[n] : 0.f);
-                } else if (mode == kAccumulate) {
-                    C[o] += v;
-                } else if (mode == kBiasSilu) {
-                    const float zz = v + (bias ? bias[n] : 0.f);
-                    C[o] = zz;
-                    act[o] = __float2bfloat16(silu(zz));
-                } else {
-                    C[o] = v * dsilu(z[o]);
-                }
+        for (int q = 0; q < 4; q++) {
+            const int m = m0 + wm + g + 8 * (q >> 1);
+            const int n = n0 + wn + nt * 8 + 2 * t + (q & 1);
+            if (m >= M || n >= N) continue;
+            const long long o = m * scm + n;
+            const float v = acc[nt][q];
+            if (mode == kStoreBias) {
+                C[o] = v + (bias ? bias[n] : 0.f);
+            } else if (mode == kAccumulate) {
+                C[o] += v;
+            } else if (mode == kBiasSilu) {
+                const float zz = v + (bias ? bias[n] : 0.f);
+                C[o] = zz;
+                act[o] = __float2bfloat16(silu(zz));
+            } else {
+                C[o] = v * dsilu(z[o]);
             }
+        }
 }
 
 template <typename TA, typename TB>

@@ -316,6 +316,9 @@ int launch_bandprep_from_dense(messi_ctx* ctx, const Band& t, const double* d_de
 // final: 2.7 ms for the 8,199 suffix cells of a 9,000-column alignment with
 // span 800.)
 constexpr int kSuffixMaxWindow = 24576;  // cells of the shared-memory window (192 KB)
+// threads of a suffix CTA (16 warps: 128 registers each, so warp 0 keeps its
+// 32 prefetched terms in registers across the triangle)
+constexpr int kSuffixThreads = 512;
 
 __host__ __device__ inline int suffix_window(int Wb) { return Wb + 64; }
 
@@ -347,11 +350,13 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     const int T = L - 1 - Wb;
     if (T <= 0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    __shared__ float tri[32][33];  // tri[q][k] = Lrow[i0 - q][k]: the in-block terms of the block's cells
+    // tri[q][k] = Lrow[i0 - q][k]: the in-block terms of the block's cells,
+    // double-buffered (warp 1 stages the next block's while warp 0 solves)
+    __shared__ float tri2[2][32][33];
     // finished block values, double-buffered: the far pushes of one block may
     // still read them while warp 0 solves the next block
     __shared__ float vals2[2][32];
-    int parity = 0;
+    int parity = 0, tb = 0;
     for (int c = threadIdx.x; c < win; c += blockDim.x) {
         am[c] = -INFINITY;
         as[c] = 0.f;
@@ -363,14 +368,17 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         float m = -INFINITY, s = 0.f;
         const float* lrow = t.Lrow + (size_t)c * RS;
         const int k1 = min(L - 1, c + Wb + 1) - c - 1;
-        for (int k = (T - c - 1) + lane; k <= k1; k += 256) {
-            float x[8];
+        for (int k = (T - c - 1) + lane; k <= k1; k += 512) {
+            float x[16];
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
+            for (int q = 0; q < 16; q++) {
                 const int kq = k + 32 * q;
                 x[q] = (kq <= k1) ? __ldg(lrow + kq) + t.Ssuf[c + kq + 1] : -INFINITY;
             }
-            lse_add8(m, s, x);
+            const float y0[8] = {x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7]};
+            const float y1[8] = {x[8], x[9], x[10], x[11], x[12], x[13], x[14], x[15]};
+            lse_add8(m, s, y0);
+            lse_add8(m, s, y1);
         }
         group_reduce<32>(m, s);
         if (lane == 0) {
@@ -379,9 +387,9 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         }
     }
     int i0 = T - 1, lo = max(0, i0 - 31);
-    if (w == 0)
+    if (w == 1)
         for (int q = 0; q < 32; q++)
-            tri[q][lane] = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
+            tri2[0][q][lane] = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
     __syncthreads();
     float cm = -INFINITY, cs = 0.f;  // warp 0: accumulator of cell i0 - lane
     if (w == 0 && i0 - lane >= lo) {
@@ -390,9 +398,21 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     }
     for (;;) {
         const int nb = i0 - lo + 1;
+        const int nlo = max(0, lo - 32);
         float* vals = vals2[parity];
         parity ^= 1;
+        float x[32];  // warp 0: L values joining its next-block cell to this block's cells
         if (w == 0) {
+            // issue the next push's loads first: they do not need this block's
+            // values, and they arrive while the triangle runs
+            const int c = lo - 1 - lane;
+#pragma unroll
+            for (int u = 0; u < 32; u++) {
+                const int k = i0 - 1 - c - u;
+                x[u] = (lo > 0 && c >= nlo && u < nb && k <= Wb) ? __ldg(t.Lcol + (size_t)(i0 - 1 - u) * RS + k)
+                                                                 : -INFINITY;
+            }
+            float (&tri)[32][33] = tri2[tb];
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
             for (int l = 0; l < nb; l++) {
                 const float sv = __shfl_sync(0xffffffffu, R.r[0] + lse_val(m, s), l);
@@ -403,13 +423,17 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 const int k = lane - l - 1;
                 if (lane > l && lane < nb && k <= Wb) lse_add(m, s, tri[lane][k] + sv);
             }
+        } else if (w == 1 && lo > 0) {
+            for (int q = 0; q < 32; q++)
+                tri2[tb ^ 1][q][lane] = (lo - 1 - q >= nlo && lane <= Wb)
+                                            ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane)
+                                            : -INFINITY;
         }
         __syncthreads();
         if (lo == 0) break;
         // push the block [lo, i0] (value u = S cell i0 - u) into the cells
         // lo-1 .. lo-1-Wb; a cell's first push starts it afresh unless the
         // band already gave it terms
-        const int nlo = max(0, lo - 32);
         if (w == 0) {
             const int c = lo - 1 - lane;
             cm = -INFINITY;
@@ -420,14 +444,16 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                     cm = am[c % win];
                     cs = as[c % win];
                 }
-                suffix_push_terms(cm, cs, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, -1, vals, nb, Wb);
+#pragma unroll
+                for (int u = 0; u < 32; u += 8) {
+                    const float y[8] = {x[u] + vals[u], x[u + 1] + vals[u + 1], x[u + 2] + vals[u + 2],
+                                        x[u + 3] + vals[u + 3], x[u + 4] + vals[u + 4], x[u + 5] + vals[u + 5],
+                                        x[u + 6] + vals[u + 6], x[u + 7] + vals[u + 7]};
+                    lse_add8(cm, cs, y);
+                }
             }
-            for (int q = 0; q < 32; q++)
-                tri[q][lane] = (lo - 1 - q >= nlo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane)
-                                                                 : -INFINITY;
-            __syncwarp();
-        } else {
-            for (int c = nlo - 1 - (threadIdx.x - 32); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 32) {
+        } else if (w >= 2) {
+            for (int c = nlo - 1 - (threadIdx.x - 64); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 64) {
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
                 suffix_push_terms(m, s, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, -1, vals, nb, Wb);
@@ -435,6 +461,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 as[c % win] = s;
             }
         }
+        tb ^= 1;
         i0 = lo - 1;
         lo = nlo;
     }
@@ -487,14 +514,15 @@ __device__ void inside_suffix_any(const Band& t, const Rules& R, float* smem, in
 }
 
 // win: cells of the dynamic shared-memory window (2 * win floats)
-__global__ void __launch_bounds__(1024) inside_suffix_kernel(Band t, Rules R, int win)
+__global__ void __launch_bounds__(kSuffixThreads) inside_suffix_kernel(Band t, Rules R, int win)
 {
     extern __shared__ float suffix_smem[];
     inside_suffix_any(t, R, suffix_smem, win);
 }
 
 // one block per alignment of a batch (alignments whose band reaches the last column skip)
-__global__ void __launch_bounds__(1024) inside_suffix_batch_kernel(const Band* __restrict__ bands, Rules R, int win)
+__global__ void __launch_bounds__(kSuffixThreads) inside_suffix_batch_kernel(const Band* __restrict__ bands, Rules R,
+                                                                           int win)
 {
     extern __shared__ float suffix_smem[];
     const Band t = bands[blockIdx.x];
@@ -1269,7 +1297,7 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
         const int win = suffix_launch_window(t.Wb);
         cudaError_t e = suffix_smem_attr(win);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_suffix_kernel attributes");
-        inside_suffix_kernel<<<1, 1024, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
+        inside_suffix_kernel<<<1, kSuffixThreads, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
         LAUNCH_CHECK(ctx, "inside_suffix_kernel");
         prof_end(ctx);
     }
@@ -1411,7 +1439,7 @@ int run_inside_batch(messi_ctx* ctx, const BandBatch& bb, double B)
     const int win = suffix_batch_window(bb);
     e = suffix_smem_attr(win);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "inside_suffix_batch_kernel attributes");
-    inside_suffix_batch_kernel<<<n, 1024, (size_t)2 * win * sizeof(float), ctx->stream>>>(bands, R, win);
+    inside_suffix_batch_kernel<<<n, kSuffixThreads, (size_t)2 * win * sizeof(float), ctx->stream>>>(bands, R, win);
     LAUNCH_CHECK(ctx, "inside_suffix_batch_kernel");
     prof_end(ctx);
     finish_Z_batch_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(bands, n, sync, bb.d_Z);
@@ -1438,26 +1466,39 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
     const int T = t.L - 1 - Wb;
     if (T <= 0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __shared__ float tri[32][33];  // tri[q][k] = Lcol[i0 + q - 1][k] for the block's cells i0 + q
+    // tri[q][k] = Lcol[i0 + q - 1][k] for the block's cells i0 + q, double-buffered
+    __shared__ float tri2[2][32][33];
     __shared__ float vals2[2][32];
-    int parity = 0;
+    int parity = 0, tb = 0;
     for (int c = threadIdx.x; c < win; c += blockDim.x) {
         am[c] = -INFINITY;
         as[c] = 0.f;
     }
     int i0 = 0, hi = min(T - 1, 31);
-    if (w == 0)
+    if (w == 1)
         for (int q = 0; q < 32; q++) {
             const int c = i0 + q;
-            tri[q][lane] = (c <= hi && c >= 1 && lane <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + lane) : -INFINITY;
+            tri2[0][q][lane] =
+                (c <= hi && c >= 1 && lane <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + lane) : -INFINITY;
         }
     __syncthreads();
     float cm = -INFINITY, cs = 0.f;
     for (;;) {
         const int nb = hi - i0 + 1;
+        const int nhi = min(T - 1, hi + 32);
         float* vals = vals2[parity];
         parity ^= 1;
+        float x[32];  // warp 0: L values joining its next-block cell to this block's cells
         if (w == 0) {
+            const int c = hi + 1 + lane;
+#pragma unroll
+            for (int u = 0; u < 32; u++) {
+                const int k = c - 1 - i0 - u;
+                x[u] = (hi < T - 1 && c <= nhi && u < nb && k >= 0 && k <= Wb)
+                           ? __ldg(t.Lrow + (size_t)(i0 + u) * RS + k)
+                           : -INFINITY;
+            }
+            float (&tri)[32][33] = tri2[tb];
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
             for (int l = 0; l < nb; l++) {
                 const int ic = i0 + l;
@@ -1470,6 +1511,12 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 const int k = lane - l - 1;
                 if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1) lse_add(m, s, tri[lane][k] + sv);
             }
+        } else if (w == 1 && hi < T - 1) {
+            for (int q = 0; q < 32; q++) {
+                const int cq = hi + 1 + q;
+                tri2[tb ^ 1][q][lane] =
+                    (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
+            }
         }
         __syncthreads();
         if (hi == T - 1) break;
@@ -1477,7 +1524,6 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
         // hi+1 .. hi+1+Wb: L(i0 + u, c - 1) = Lrow[i0 + u][c - 1 - i0 - u],
         // contiguous in c; a cell's first push (from the block holding its
         // smallest referenced cell) starts it afresh
-        const int nhi = min(T - 1, hi + 32);
         if (w == 0) {
             const int c = hi + 1 + lane;
             cm = -INFINITY;
@@ -1488,15 +1534,16 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                     cm = am[c % win];
                     cs = as[c % win];
                 }
-                suffix_push_terms(cm, cs, t.Lrow, RS, i0, 1, c - 1 - i0, -1, vals, nb, Wb);
+#pragma unroll
+                for (int u = 0; u < 32; u += 8) {
+                    const float y[8] = {x[u] + vals[u], x[u + 1] + vals[u + 1], x[u + 2] + vals[u + 2],
+                                        x[u + 3] + vals[u + 3], x[u + 4] + vals[u + 4], x[u + 5] + vals[u + 5],
+                                        x[u + 6] + vals[u + 6], x[u + 7] + vals[u + 7]};
+                    lse_add8(cm, cs, y);
+                }
             }
-            for (int q = 0; q < 32; q++) {
-                const int cq = hi + 1 + q;
-                tri[q][lane] = (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
-            }
-            __syncwarp();
-        } else {
-            for (int c = nhi + 1 + (threadIdx.x - 32); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 32) {
+        } else if (w >= 2) {
+            for (int c = nhi + 1 + (threadIdx.x - 64); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 64) {
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
                 suffix_push_terms(m, s, t.Lrow, RS, i0, 1, c - 1 - i0, -1, vals, nb, Wb);
@@ -1504,6 +1551,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 as[c % win] = s;
             }
         }
+        tb ^= 1;
         i0 = hi + 1;
         hi = nhi;
     }
@@ -1552,7 +1600,7 @@ __device__ void outside_suffix_body_pull(const Band& t, const Rules& R)
     }
 }
 
-__global__ void __launch_bounds__(1024) outside_suffix_kernel(Band t, Rules R, int win)
+__global__ void __launch_bounds__(kSuffixThreads) outside_suffix_kernel(Band t, Rules R, int win)
 {
     extern __shared__ float suffix_smem[];
     if (suffix_window(t.Wb) <= win) outside_suffix_body(t, R, suffix_smem, suffix_smem + win, win);
@@ -1567,7 +1615,7 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
         cudaError_t e = cudaFuncSetAttribute(outside_suffix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              2 * win * (int)sizeof(float));
         if (e != cudaSuccess) return cuda_fail(ctx, e, "outside_suffix_kernel attributes");
-        outside_suffix_kernel<<<1, 1024, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
+        outside_suffix_kernel<<<1, kSuffixThreads, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
         LAUNCH_CHECK(ctx, "outside_suffix_kernel");
     }
     Band tt = t;
