@@ -59,11 +59,81 @@ __device__ __forceinline__ float dsilu(float z);
 __device__ __forceinline__ __nv_bfloat16 to_bf(float v) { return __float2bfloat16(v); }
 __device__ __forceinline__ __nv_bfloat16 to_bf(__nv_bfloat16 v) { return v; }
 
+
 // CTA tile 32 x 32 (four warps of 16 x 16), the K extent staged in chunks of
 // kBK: the GEMMs of this network are a few hundred rows, so the CTA count,
 // not the per-CTA rate, bounds them; a whole chunk's loads are issued before
 // the one CTA barrier, so a chunk costs one memory round trip.
 constexpr int kBM = 32, kBN = 32, kBK = 256, kPad = 8;
+
+// Four consecutive elements (16 B of FP32 or 8 B of BF16), rounded to BF16.
+__device__ __forceinline__ void load4_bf(const float* p, __nv_bfloat16 (&o)[4])
+{
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = __float2bfloat16(v.x);
+    o[1] = __float2bfloat16(v.y);
+    o[2] = __float2bfloat16(v.z);
+    o[3] = __float2bfloat16(v.w);
+}
+__device__ __forceinline__ void load4_bf(const __nv_bfloat16* p, __nv_bfloat16 (&o)[4])
+{
+    const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+    const __nv_bfloat16* b = reinterpret_cast<const __nv_bfloat16*>(&v);
+    o[0] = b[0];
+    o[1] = b[1];
+    o[2] = b[2];
+    o[3] = b[3];
+}
+
+// Stage rows r0.. of one operand tile, [rows][k] in shared memory (rows of
+// kBK + kPad): X(r, k) = X[r*srow + k*sk].  With vec (unit stride along the
+// fast index, the other stride a multiple of 4, the base aligned), four
+// consecutive elements of the fast index come in one load.
+template <int ROWS, typename T>
+__device__ __forceinline__ void stage_tile(__nv_bfloat16 (*dst)[kBK + 8], const T* __restrict__ X, long long srow,
+                                           long long sk, int r0, int nrows, int k0, int kc, int kc16, bool vec)
+{
+    const bool k_fast = (sk == 1);
+    if (vec) {
+        for (int e = threadIdx.x; e < ROWS * kBK / 4; e += blockDim.x) {
+            // groups of four along the fast index
+            const int r = k_fast ? e / (kBK / 4) : 4 * (e % (ROWS / 4));
+            const int c = k_fast ? 4 * (e % (kBK / 4)) : e / (ROWS / 4);
+            if (c >= kc16) continue;
+            __nv_bfloat16 v[4];
+            const int rr = r0 + r, kk = k0 + c;
+            if (k_fast) {
+                if (rr < nrows && c + 3 < kc) load4_bf(X + rr * srow + kk, v);
+                else
+                    for (int q = 0; q < 4; q++)
+                        v[q] = (rr < nrows && c + q < kc) ? to_bf(X[rr * srow + kk + q]) : __float2bfloat16(0.f);
+                for (int q = 0; q < 4; q++) dst[r][c + q] = v[q];
+            } else {
+                if (rr + 3 < nrows && c < kc) load4_bf(X + rr + kk * sk, v);
+                else
+                    for (int q = 0; q < 4; q++)
+                        v[q] = (rr + q < nrows && c < kc) ? to_bf(X[(rr + q) + kk * sk]) : __float2bfloat16(0.f);
+                for (int q = 0; q < 4; q++) dst[r + q][c] = v[q];
+            }
+        }
+    } else {
+        for (int e = threadIdx.x; e < ROWS * kBK; e += blockDim.x) {
+            const int r = k_fast ? e / kBK : e % ROWS, c = k_fast ? e % kBK : e / ROWS;
+            if (c >= kc16) continue;
+            const int rr = r0 + r, kk = k0 + c;
+            dst[r][c] = (rr < nrows && c < kc) ? to_bf(X[rr * srow + kk * sk]) : __float2bfloat16(0.f);
+        }
+    }
+}
+
+template <typename T>
+__host__ __device__ inline bool vec_ok(const T* p, long long srow, long long sk)
+{
+    const size_t align = sizeof(T) * 4;
+    const bool unit = (srow == 1) != (sk == 1) && (srow == 1 || sk == 1);
+    const long long other = (sk == 1) ? srow : sk;
+    return unit && other % 4 == 0 && (reinterpret_cast<size_t>(p) % align) == 0;
+}
 
 // GEMM epilogues
 enum GemmMode {
@@ -105,24 +175,13 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, con
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[j][q] = 0.f;
     // consecutive threads walk the operand's unit-stride index (coalesced)
-    const bool a_k_fast = (sak == 1), b_k_fast = (sbk == 1);
+    const bool va = vec_ok(A, sam, sak), vb = vec_ok(B, sbn, sbk);
     for (int k0 = 0; k0 < K; k0 += kBK) {
         const int kc = min(kBK, K - k0);
         const int kc16 = (kc + 15) & ~15;  // chunk rounded up to whole k16 steps (zero padded)
         if (k0 > 0) __syncthreads();
-#pragma unroll 8
-        for (int e = tid; e < kBM * kBK; e += 128) {
-            const int r = a_k_fast ? e / kBK : e % kBM, c = a_k_fast ? e % kBK : e / kBM;
-            if (c < kc16) {
-                const int m = m0 + r, k = k0 + c;
-                As[r][c] = (m < M && c < kc) ? to_bf(A[m * sam + k * sak]) : __float2bfloat16(0.f);
-            }
-            const int r2 = b_k_fast ? e / kBK : e % kBN, c2 = b_k_fast ? e % kBK : e / kBN;
-            if (c2 < kc16) {
-                const int n = n0 + r2, kk = k0 + c2;
-                Bs[r2][c2] = (n < N && c2 < kc) ? to_bf(B[kk * sbk + n * sbn]) : __float2bfloat16(0.f);
-            }
-        }
+        stage_tile<kBM>(As, A, sam, sak, m0, M, k0, kc, kc16, va);
+        stage_tile<kBN>(Bs, B, sbn, sbk, n0, N, k0, kc, kc16, vb);
         __syncthreads();
         for (int ks = 0; ks < kc16; ks += 16) {
             uint32_t af[4], bf[2][2];
