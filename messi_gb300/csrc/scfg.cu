@@ -110,6 +110,17 @@ __device__ __forceinline__ float lse2f(float a, float b)
     return m + __logf(__expf(a - m) + __expf(b - m));
 }
 
+// Adds sl * exp(x0) to the log-sum-exp (m, s) without branches (x0, m may
+// be -inf): the serial triangle of the suffix recurrences, where a branch
+// would split the warp on every step.
+__device__ __forceinline__ void lse_add_scaled(float& m, float& s, float x0, float sl)
+{
+    const float mx = fmaxf(m, x0);
+    const float base = (mx == -INFINITY) ? 0.f : mx;
+    s = s * __expf(m - base) + sl * __expf(x0 - base);
+    m = mx;
+}
+
 template <int G>
 __device__ __forceinline__ void group_reduce(float& m, float& s)
 {
@@ -412,16 +423,21 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 x[u] = (lo > 0 && c >= nlo && u < nb && k <= Wb) ? __ldg(t.Lcol + (size_t)(i0 - 1 - u) * RS + k)
                                                                  : -INFINITY;
             }
+            // column-oriented substitution: lane q owns cell i0 - q; once cell
+            // l is final its (m, s) is broadcast and every later cell adds
+            // L(cell, i0 - l - 1) + r1 + m_l weighted by s_l (no log on the
+            // serial path)
             float (&tri)[32][33] = tri2[tb];
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
             for (int l = 0; l < nb; l++) {
-                const float sv = __shfl_sync(0xffffffffu, R.r[0] + lse_val(m, s), l);
+                const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
+                const int k = lane - l - 1;
+                if (lane > l && lane < nb && k <= Wb) lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
                 if (lane == 0) {
+                    const float sv = R.r[0] + lse_val(ml, sl);
                     t.Ssuf[i0 - l] = sv;
                     vals[l] = sv;
                 }
-                const int k = lane - l - 1;
-                if (lane > l && lane < nb && k <= Wb) lse_add(m, s, tri[lane][k] + sv);
             }
         } else if (w == 1 && lo > 0) {
             for (int q = 0; q < 32; q++)
@@ -1498,18 +1514,24 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                            ? __ldg(t.Lrow + (size_t)(i0 + u) * RS + k)
                            : -INFINITY;
             }
+            // column-oriented substitution (lane q owns cell i0 + q); Osuf[0]
+            // = 0 is (m, s) = (-r1, 1), so every value is r1 + m + log s
             float (&tri)[32][33] = tri2[tb];
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
+            if (i0 + lane == 0) {
+                m = -R.r[0];
+                s = 1.f;
+            }
             for (int l = 0; l < nb; l++) {
-                const int ic = i0 + l;
-                const float fin = (ic == 0) ? 0.f : R.r[0] + lse_val(m, s);
-                const float sv = __shfl_sync(0xffffffffu, fin, l);
+                const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
+                const int k = lane - l - 1;
+                if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1)
+                    lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
                 if (lane == 0) {
-                    t.Osuf[ic] = sv;
+                    const float sv = (i0 + l == 0) ? 0.f : R.r[0] + lse_val(ml, sl);
+                    t.Osuf[i0 + l] = sv;
                     vals[l] = sv;
                 }
-                const int k = lane - l - 1;
-                if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1) lse_add(m, s, tri[lane][k] + sv);
             }
         } else if (w == 1 && hi < T - 1) {
             for (int q = 0; q < 32; q++) {
