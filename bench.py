@@ -697,6 +697,12 @@ def run_structures(args):
     (e, sm), t_dec = timed(lambda: api.computeposteriordecodingcuda(single, pair, 2.0, ctx=ctx), args.steps)
     cons, t_cons = timed(lambda: api.consensusstructure(u, mat, ctx=ctx), args.steps)
     post, t_post = timed(lambda: api.computeposteriors(u, mat, ctx=ctx), args.steps)
+    # device time of the posterior chain's passes (CUDA events around each launch)
+    ctx.profile(True)
+    api.computeposteriors(u, mat, ctx=ctx)
+    post_kernels = {name: ctx.profile_read(k)[0] for k, name in ((1, "inside_wavefront_ms"), (2, "inside_suffix_ms"),
+                                                                 (3, "outside_wavefront_ms"))}
+    ctx.profile(False)
     (S, pri), t_samp = timed(lambda: api.samplestructures(u, mat, nsamp, seed=3, ctx=ctx), args.steps)
     fx, t_fix = timed(lambda: api._structure_call(ds, prm, paired1, ctx), args.steps)
     band, t_band = timed(lambda: api.computestructureintegratedlikelihood(ds, prm, W, ctx=ctx), args.steps)
@@ -716,7 +722,7 @@ def run_structures(args):
             "steps": args.steps, "warmup": args.warmup,
             "posterior_decoding_ms": t_dec, "decoding_cells": L * (L - 1) // 2,
             "reference_decoding": ref,
-            "posteriors_ms": t_post, "consensus_chain_ms": t_cons,
+            "posteriors_ms": t_post, "posterior_chain_kernels": post_kernels, "consensus_chain_ms": t_cons,
             "consensus_pairs": int(np.count_nonzero(cons) // 2),
             "sampling_ms": t_samp, "structures_per_s": nsamp / (t_samp / 1e3), "samples": nsamp,
             "fixed_structure_ms": t_fix, "fixed_structure_pairs": npairs_struct,

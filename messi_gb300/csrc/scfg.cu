@@ -440,10 +440,13 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 }
             }
         } else if (w == 1 && lo > 0) {
+            // all 32 loads first, then the stores: one memory round trip
+            float v[32];
+#pragma unroll
             for (int q = 0; q < 32; q++)
-                tri2[tb ^ 1][q][lane] = (lo - 1 - q >= nlo && lane <= Wb)
-                                            ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane)
-                                            : -INFINITY;
+                v[q] = (lo - 1 - q >= nlo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane) : -INFINITY;
+#pragma unroll
+            for (int q = 0; q < 32; q++) tri2[tb ^ 1][q][lane] = v[q];
         }
         __syncthreads();
         if (lo == 0) break;
@@ -1534,11 +1537,15 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 }
             }
         } else if (w == 1 && hi < T - 1) {
+            // all 32 loads first, then the stores: one memory round trip
+            float v[32];
+#pragma unroll
             for (int q = 0; q < 32; q++) {
                 const int cq = hi + 1 + q;
-                tri2[tb ^ 1][q][lane] =
-                    (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
+                v[q] = (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
             }
+#pragma unroll
+            for (int q = 0; q < 32; q++) tri2[tb ^ 1][q][lane] = v[q];
         }
         __syncthreads();
         if (hi == T - 1) break;
