@@ -38,6 +38,7 @@ WORKLOAD = "c2"
 WORKLOAD_TEXT = {"c2": "c2: 64 seqs x 1,000 nt, max pair span 500",
                  "c2p": "c2p: 64 seqs x 600 nt, max pair span 300",
                  "c4": "c4: 30 seqs x 9,000 nt, max pair span 800",
+                 "c4p": "c4p: 8 seqs x 9,000 nt, max pair span 800",
                  "c1": "c1: 16 seqs x 120 nt, all pairs"}
 BYTES_PER_UPDATE = 212  # algorithmic bytes of one node update (2 child rows + exps + indices in, 1 row out)
 # DRAM bytes (read + write) per node update of the pruning kernel from one ncu

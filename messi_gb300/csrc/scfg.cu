@@ -639,7 +639,7 @@ struct CellPartial {
     float m, s, pbv;
 };
 
-template <int NLO, int NHI>
+template <int NLO, int NHI, bool WIDE>
 __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int d, bool valid, int lane, int G)
 {
     const int RS = t.RS;
@@ -649,10 +649,34 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
     if (valid && kend > NLO) {
         const float* lrow = t.Lrow + (size_t)i * RS;
         const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
-        // blocks of eight split points per lane, the sixteen loads of a block
-        // issued together (a lane has at most eight points up to span 256);
-        // points past the end are -inf, which lse_add8 skips exactly
-        for (int k = NLO + lane; k < kend; k += 8 * G) {
+        // blocks of eight split points per lane, summed in order.  WIDE: while
+        // a lane has more than eight points left, two blocks' 32 loads are
+        // issued together (one L2 round trip for sixteen points: long spans
+        // have up to 47 points per lane); the narrow form keeps 16 loads in
+        // flight for kernels without the registers.  Points past the end are
+        // -inf, which lse_add8 skips exactly, so both forms give the same bits.
+        int k = NLO + lane;
+        if (WIDE) {
+            for (; k + 8 * G < kend; k += 16 * G) {
+                float a[16], b[16];
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int kq = k + q * G;
+                    const bool on = kq < kend;
+                    a[q] = on ? __ldcg(lrow + kq) : -INFINITY;
+                    b[q] = on ? __ldcg(scol - kq) : -INFINITY;
+                }
+                float x0[8], x1[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    x0[q] = a[q] + b[q];
+                    x1[q] = a[8 + q] + b[8 + q];
+                }
+                lse_add8(c.m, c.s, x0);
+                lse_add8(c.m, c.s, x1);
+            }
+        }
+        for (; k < kend; k += 8 * G) {
             float x[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) {
@@ -804,9 +828,10 @@ __device__ __forceinline__ void cell_finish_t(const Band& t, int i, int d, bool 
     cell_write_t<NLO, NHI>(t, i, d, c, outer_load<NLO, NHI>(t, i, d, false), R);
 }
 
+template <bool WIDE>
 __device__ __forceinline__ CellPartial inside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G)
 {
-    return (d & 1) ? cell_partial_t<2, 2>(t, i, d, valid, lane, G) : cell_partial_t<3, 3>(t, i, d, valid, lane, G);
+    return (d & 1) ? cell_partial_t<2, 2, WIDE>(t, i, d, valid, lane, G) : cell_partial_t<3, 3, WIDE>(t, i, d, valid, lane, G);
 }
 
 __device__ __forceinline__ void inside_cell_finish(const Band& t, int i, int d, bool valid, int lane, CellPartial c,
@@ -816,9 +841,10 @@ __device__ __forceinline__ void inside_cell_finish(const Band& t, int i, int d, 
     else cell_finish_t<3, 3>(t, i, d, valid, lane, c, R);
 }
 
+template <bool WIDE>
 __device__ __forceinline__ void inside_cell(const Band& t, int i, int d, bool valid, int lane, int G, const Rules& R)
 {
-    inside_cell_finish(t, i, d, valid, lane, inside_cell_partial(t, i, d, valid, lane, G), R);
+    inside_cell_finish(t, i, d, valid, lane, inside_cell_partial<WIDE>(t, i, d, valid, lane, G), R);
 }
 
 // The cells of one diagonal that a CTA owns (rows [r0, end)), computed by the
@@ -838,6 +864,7 @@ struct WarpSet {
     }
 };
 
+template <bool WIDE>
 __device__ __forceinline__ RowsPart rows_partial(const Band& t, int d, int r0, int end, WarpSet ws)
 {
     RowsPart p;
@@ -848,11 +875,12 @@ __device__ __forceinline__ RowsPart rows_partial(const Band& t, int d, int r0, i
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int i = r0 + g + it * gpb;
-        p.c[it] = inside_cell_partial(t, i, d, i < end, lane, G);
+        p.c[it] = inside_cell_partial<WIDE>(t, i, d, i < end, lane, G);
     }
     return p;
 }
 
+template <bool WIDE>
 __device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int end, const RowsPart& p, const Rules& R,
                                             WarpSet ws)
 {
@@ -866,7 +894,7 @@ __device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int en
     }
     for (int base = r0 + 2 * gpb; base < end; base += gpb) {
         const int i = base + g;
-        inside_cell(t, i, d, i < end, lane, G, R);
+        inside_cell<WIDE>(t, i, d, i < end, lane, G, R);
     }
 }
 
@@ -892,12 +920,14 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_kernel(Band t, Ru
         const int eB = eA + 1;
         const int endA = min(r0 + rows + 1, L - eA);
         const int endB = (eB <= t.Wb) ? min(r0 + rows, L - eB) : r0;
-        const RowsPart pa = rows_partial(t, eA, r0, endA, all);
-        const RowsPart pb = rows_partial(t, eB, r0, endB, all);
+        const RowsPart pa = rows_partial<true>(t, eA, r0, endA, all);
+        const RowsPart pb = rows_partial<true>(t, eB, r0, endB, all);
         if (!grid_wait(t.sync, gen)) return;
-        rows_finish(t, eA, r0, endA, pa, R, all);
+        // further rows (short spans only) in the narrow form: the wide one
+        // would spill beside the partial sums held across the wait
+        rows_finish<false>(t, eA, r0, endA, pa, R, all);
         __syncthreads();  // diagonal 2p-1 of this CTA's rows before diagonal 2p reads it
-        rows_finish(t, eB, r0, endB, pb, R, all);
+        rows_finish<false>(t, eB, r0, endB, pb, R, all);
         grid_arrive(t.sync);
     }
 }
@@ -1037,14 +1067,14 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
         const bool v0 = gid0 < ncell;
         const int b0 = v0 ? batch_band(cumL, nact, d, gid0) : 0;
         const int i0 = v0 ? (int)(gid0 - (cumL[b0] - (long long)d * b0)) : 0;
-        const CellPartial c = inside_cell_partial(bands[b0], i0, d, v0, lane, G);
+        const CellPartial c = inside_cell_partial<true>(bands[b0], i0, d, v0, lane, G);
         if (!grid_wait(sync, gen)) return;
         inside_cell_finish(bands[b0], i0, d, v0, lane, c, R);
         for (long long base = total; base < ncell; base += total) {
             const long long it = base + gid0;
             const bool valid = it < ncell;
             const int b = valid ? batch_band(cumL, nact, d, it) : 0;
-            inside_cell(bands[b], valid ? (int)(it - (cumL[b] - (long long)d * b)) : 0, d, valid, lane, G, R);
+            inside_cell<true>(bands[b], valid ? (int)(it - (cumL[b] - (long long)d * b)) : 0, d, valid, lane, G, R);
         }
         grid_arrive(sync);
     }
@@ -1052,150 +1082,187 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
 
 // Outside cell (i, j = i+d) in two parts, as the inside cells: the parent
 // sums run over q of OS/OF(i, j+1+q) * S(j+1, j+1+q) (L) and of
-// OS/OF(i-1-q, j) * L(i-1-q, i-1) (S), spans d+1+q.  outside_cell_partial
-// sums q >= 1 (spans >= d+2), the suffix-column terms and the F value (span
-// d+2) and reduces them over the group; outside_cell_finish adds the q = 0
-// terms, which read the diagonal d+1 finished just before, and writes the
-// cell (lane 0).
+// OS/OF(i-1-q, j) * L(i-1-q, i-1) (S), spans d+1+q.  The partial part sums
+// q >= Q and the suffix-column terms, the L and S sums side by side (the 24
+// loads of a step, four points of each sum, in flight together), reduces them
+// over the group and loads the enclosing pair's score; the finishing part
+// (lane 0) adds q = 0 .. Q-1 in ascending order, forms the F value from the
+// enclosing pair (i-1, j+1) (span d+2) and writes the cell.  Diagonals go
+// two per barrier, (e, e-1), with Q = 2 for e and Q = 3 for e-1: the partial
+// sums then read spans >= e+3 only, which are complete before the wait that
+// completes e+2 and e+1.  A cell's bits do not depend on which CTA or warp
+// computes it.
 struct OutPartial {
-    float mL, sL, mS, sS, oF;
+    float mL, sL, mS, sS, pp;
 };
 
-__device__ __forceinline__ OutPartial outside_cell_partial(const Band& t, int i, int d, bool valid, int lane, int G,
-                                                           const Rules& R)
+template <int Q>
+__device__ __forceinline__ OutPartial outside_partial_t(const Band& t, int i, int d, bool valid, int lane, int G,
+                                                        const Rules& R)
 {
     const int L = t.L, Wb = t.Wb, RS = t.RS;
     const int j = i + d;
     OutPartial c{-INFINITY, 0.f, -INFINITY, 0.f, -INFINITY};
     if (valid) {
-        const int nL = min(i + Wb, L - 1) - j;
+        const bool hasL = j + 1 <= L - 1, hasS = i >= 1;
+        const int nL = hasL ? min(i + Wb, L - 1) - j : 0;
+        const int nS = hasS ? i - max(0, j - Wb) : 0;
         const float* osr = t.OSrow + (size_t)i * RS + d + 1;
         const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
-        if (j + 1 <= L - 1) {
-            const float* srw = t.Srow + (size_t)(j + 1) * RS;
-            int q = 1 + lane;
-            for (; q + 3 * G < nL; q += 4 * G) {
-                float x[8];
+        const float* srw = t.Srow + (size_t)min(j + 1, L - 1) * RS;
+        const float* lcol = t.Lcol + (size_t)max(i - 1, 0) * RS;
+        const float* osc = t.OScol + (size_t)j * RS + d + 1;
+        const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
+        const int n = max(nL, nS);
+        for (int q = Q + lane; q < n; q += 4 * G) {
+            float xl[8], xs[8];
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const float sib = srw[q + u * G];
-                    x[2 * u] = R.r[0] + __ldcg(osr + q + u * G) + sib;
-                    x[2 * u + 1] = R.r[4] + __ldcg(ofr + q + u * G) + sib;
-                }
-                lse_add8(c.mL, c.sL, x);
+            for (int u = 0; u < 4; u++) {
+                const int qq = q + u * G;
+                const bool onL = qq < nL, onS = qq < nS;
+                const float sib = onL ? srw[qq] : 0.f;
+                const float osl = onL ? __ldcg(osr + qq) : -INFINITY;
+                const float ofl = onL ? __ldcg(ofr + qq) : -INFINITY;
+                const float lft = onS ? lcol[qq] : 0.f;
+                const float oss = onS ? __ldcg(osc + qq) : -INFINITY;
+                const float ofs = onS ? __ldcg(ofc + qq) : -INFINITY;
+                xl[2 * u] = R.r[0] + osl + sib;
+                xl[2 * u + 1] = R.r[4] + ofl + sib;
+                xs[2 * u] = R.r[0] + oss + lft;
+                xs[2 * u + 1] = R.r[4] + ofs + lft;
             }
-            for (; q + G < nL; q += 2 * G) {
-                const float sib0 = srw[q], sib1 = srw[q + G];
-                lse_add4(c.mL, c.sL, R.r[0] + __ldcg(osr + q) + sib0, R.r[4] + __ldcg(ofr + q) + sib0,
-                         R.r[0] + __ldcg(osr + q + G) + sib1, R.r[4] + __ldcg(ofr + q + G) + sib1);
-            }
-            for (; q < nL; q += G) {
-                const float sib = srw[q];
-                lse_add(c.mL, c.sL, R.r[0] + __ldcg(osr + q) + sib);
-                lse_add(c.mL, c.sL, R.r[4] + __ldcg(ofr + q) + sib);
-            }
-            if (lane == 0 && L - 1 > i + Wb) lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
+            lse_add8(c.mL, c.sL, xl);
+            lse_add8(c.mS, c.sS, xs);
         }
-        if (i >= 1) {
-            const int ip0 = max(0, j - Wb);
-            const int nS = i - ip0;
-            const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
-            const float* osc = t.OScol + (size_t)j * RS + d + 1;
-            const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
-            int q = 1 + lane;
-            for (; q + 3 * G < nS; q += 4 * G) {
-                float x[8];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const float lft = lcol[q + u * G];
-                    x[2 * u] = R.r[0] + __ldcg(osc + q + u * G) + lft;
-                    x[2 * u + 1] = R.r[4] + __ldcg(ofc + q + u * G) + lft;
-                }
-                lse_add8(c.mS, c.sS, x);
-            }
-            for (; q + G < nS; q += 2 * G) {
-                const float l0 = lcol[q], l1 = lcol[q + G];
-                lse_add4(c.mS, c.sS, R.r[0] + __ldcg(osc + q) + l0, R.r[4] + __ldcg(ofc + q) + l0,
-                         R.r[0] + __ldcg(osc + q + G) + l1, R.r[4] + __ldcg(ofc + q + G) + l1);
-            }
-            for (; q < nS; q += G) {
-                const float lft = lcol[q];
-                lse_add(c.mS, c.sS, R.r[0] + __ldcg(osc + q) + lft);
-                lse_add(c.mS, c.sS, R.r[4] + __ldcg(ofc + q) + lft);
-            }
-            if (j == L - 1) {
-                const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
-                for (int ip = a + lane; ip <= bnd; ip += G) lse_add(c.mS, c.sS, R.r[0] + __ldcg(t.Osuf + ip) + lcol[i - 1 - ip]);
-            }
+        if (lane == 0 && hasL && L - 1 > i + Wb) lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
+        if (hasS && j == L - 1) {
+            const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
+            for (int ip = a + lane; ip <= bnd; ip += G) lse_add(c.mS, c.sS, R.r[0] + __ldcg(t.Osuf + ip) + lcol[i - 1 - ip]);
         }
-        if (lane == 0 && i >= 1 && j <= L - 2 && d + 2 <= Wb) {
-            const size_t pr = (size_t)(i - 1) * RS + d + 2;
-            const float pp = t.pb[pr];
-            if (pp != -INFINITY) {
-                float m = -INFINITY, s = 0.f;
-                lse_add(m, s, R.r[2] + pp + __ldcg(t.OSrow + pr));
-                lse_add(m, s, R.r[3] + pp + __ldcg(t.OFrow + pr));
-                lse_add(m, s, R.r[6] + pp + __ldcg(t.OLrow + pr));
-                c.oF = lse_val(m, s);
-            }
-        }
+        if (lane == 0 && hasS && j <= L - 2 && d + 2 <= Wb) c.pp = t.pb[(size_t)(i - 1) * RS + d + 2];
     }
     group_reduce_rt(c.mL, c.sL, G);
     group_reduce_rt(c.mS, c.sS, G);
     return c;
 }
 
-__device__ __forceinline__ void outside_cell_finish(const Band& t, int i, int d, bool valid, int lane, OutPartial c,
-                                                    const Rules& R)
+template <int Q>
+__device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, bool valid, int lane, OutPartial c,
+                                                 const Rules& R)
 {
     if (!(valid && lane == 0)) return;
     const int L = t.L, Wb = t.Wb, RS = t.RS;
     const int j = i + d;
-    if (min(i + Wb, L - 1) - j >= 1) {  // q = 0 of the L sum: OS/OF(i, j+1) * S(j+1, j+1)
-        const float sib = t.Srow[(size_t)(j + 1) * RS];
-        const size_t o = (size_t)i * RS + d + 1;
-        lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.OSrow + o) + sib);
-        lse_add(c.mL, c.sL, R.r[4] + __ldcg(t.OFrow + o) + sib);
+    const bool hasL = j + 1 <= L - 1, hasS = i >= 1;
+    const int nL = hasL ? min(i + Wb, L - 1) - j : 0;
+    const int nS = hasS ? i - max(0, j - Wb) : 0;
+    // every operand first (one round trip), then the sums in ascending q
+    float sib[Q], osl[Q], ofl[Q], lft[Q], oss[Q], ofs[Q];
+    const size_t orow = (size_t)i * RS + d + 1, ocol = (size_t)j * RS + d + 1;
+    const size_t srow = (size_t)min(j + 1, L - 1) * RS, lc = (size_t)max(i - 1, 0) * RS;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const bool onL = q < nL, onS = q < nS;
+        sib[q] = onL ? t.Srow[srow + q] : 0.f;
+        osl[q] = onL ? __ldcg(t.OSrow + orow + q) : -INFINITY;
+        ofl[q] = onL ? __ldcg(t.OFrow + orow + q) : -INFINITY;
+        lft[q] = onS ? t.Lcol[lc + q] : 0.f;
+        oss[q] = onS ? __ldcg(t.OScol + ocol + q) : -INFINITY;
+        ofs[q] = onS ? __ldcg(t.OFcol + ocol + q) : -INFINITY;
     }
-    if (i >= 1 && i - max(0, j - Wb) >= 1) {  // q = 0 of the S sum: OS/OF(i-1, j) * L(i-1, i-1)
-        const float lft = t.Lcol[(size_t)(i - 1) * RS];
-        const size_t o = (size_t)j * RS + d + 1;
-        lse_add(c.mS, c.sS, R.r[0] + __ldcg(t.OScol + o) + lft);
-        lse_add(c.mS, c.sS, R.r[4] + __ldcg(t.OFcol + o) + lft);
+    float oF = -INFINITY;
+    if (c.pp != -INFINITY) {
+        const size_t pr = (size_t)(i - 1) * RS + d + 2;
+        const float a = __ldcg(t.OSrow + pr), b = __ldcg(t.OFrow + pr), e = __ldcg(t.OLrow + pr);
+        float m = -INFINITY, s = 0.f;
+        lse_add(m, s, R.r[2] + c.pp + a);
+        lse_add(m, s, R.r[3] + c.pp + b);
+        lse_add(m, s, R.r[6] + c.pp + e);
+        oF = lse_val(m, s);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        lse_add(c.mL, c.sL, R.r[0] + osl[q] + sib[q]);
+        lse_add(c.mL, c.sL, R.r[4] + ofl[q] + sib[q]);
+        lse_add(c.mS, c.sS, R.r[0] + oss[q] + lft[q]);
+        lse_add(c.mS, c.sS, R.r[4] + ofs[q] + lft[q]);
     }
     const float oL = lse_val(c.mL, c.sL);
     float oS = lse_val(c.mS, c.sS);
     if (i == 0 && j == L - 1) oS = 0.f;
     t.OSrow[(size_t)i * RS + d] = oS;
     t.OScol[(size_t)j * RS + d] = oS;
-    t.OFrow[(size_t)i * RS + d] = c.oF;
-    t.OFcol[(size_t)j * RS + d] = c.oF;
+    t.OFrow[(size_t)i * RS + d] = oF;
+    t.OFcol[(size_t)j * RS + d] = oF;
     t.OLrow[(size_t)i * RS + d] = oL;
     if (j == L - 1) t.Osuf[i] = oS;
 }
 
-// All band diagonals of the outside pass, descending spans; the partial sums
-// of a CTA's first cells of diagonal d are computed between its arrival at
-// the barrier of diagonal d+1 and its wait there.
+// The outside cells of one diagonal with rows [start, end), by all warps of
+// the CTA: partial sums of the first two rows of every group, then (after the
+// caller's wait) their finishing parts and any further rows whole.
+struct OutRows {
+    OutPartial c[2];
+};
+
+template <int Q>
+__device__ __forceinline__ OutRows out_rows_partial(const Band& t, int d, int start, int end, const Rules& R)
+{
+    OutRows p;
+    const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const int i = start + g + it * gpb;
+        p.c[it] = outside_partial_t<Q>(t, i, d, i < end, lane, G, R);
+    }
+    return p;
+}
+
+template <int Q>
+__device__ __forceinline__ void out_rows_finish(const Band& t, int d, int start, int end, const OutRows& p,
+                                                const Rules& R)
+{
+    const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const int i = start + g + it * gpb;
+        outside_finish_t<Q>(t, i, d, i < end, lane, p.c[it], R);
+    }
+    for (int base = start + 2 * gpb; base < end; base += gpb) {
+        const int i = base + g;
+        outside_finish_t<Q>(t, i, d, i < end, lane, outside_partial_t<Q>(t, i, d, i < end, lane, G, R), R);
+    }
+}
+
+// All band diagonals of the outside pass, descending spans, two per grid
+// barrier.  CTA b owns rows [b*R, (b+1)*R) of every diagonal (R = ceil(L /
+// CTAs)).  For the pair (e, e-1) it computes diagonal e for its rows plus row
+// b*R - 1 (which the previous CTA also computes, to the same bits) and then,
+// after a CTA barrier, diagonal e-1, whose cells read diagonal e only at rows
+// i and i-1.  The partial sums of both diagonals read spans >= e+3 and are
+// computed between the CTA's arrival at the barrier that completes e+1 and its
+// wait there.
 __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, Rules R)
 {
     unsigned int gen = 0;
     const int L = t.L, Wb = t.Wb;
+    const int rows = (L + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * rows;
     grid_arrive(t.sync);  // the suffix column was written by the previous launch
-    for (int d = Wb; d >= 0; d--) {
-        const int G = group_width(2 * (Wb - d) + 2);
-        const int gpb = blockDim.x / G;
-        const int total = gridDim.x * gpb;
-        const int lane = threadIdx.x & (G - 1);
-        const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
-        const int ncell = L - d;
-        const OutPartial c = outside_cell_partial(t, gid0, d, gid0 < ncell, lane, G, R);
+    for (int eA = Wb; eA >= 0; eA -= 2) {
+        const int eB = eA - 1;
+        const int sA = max(r0 - 1, 0), endA = min(r0 + rows, L - eA);
+        const int endB = (eB >= 0) ? min(r0 + rows, L - eB) : r0;
+        const OutRows pa = out_rows_partial<2>(t, eA, sA, endA, R);
+        OutRows pb;
+        if (eB >= 0) pb = out_rows_partial<3>(t, eB, r0, endB, R);
         if (!grid_wait(t.sync, gen)) return;
-        outside_cell_finish(t, gid0, d, gid0 < ncell, lane, c, R);
-        for (int base = total; base < ncell; base += total) {
-            const int i = base + gid0;
-            const bool valid = i < ncell;
-            outside_cell_finish(t, i, d, valid, lane, outside_cell_partial(t, i, d, valid, lane, G, R), R);
+        out_rows_finish<2>(t, eA, sA, endA, pa, R);
+        if (eB >= 0) {
+            __syncthreads();  // diagonal e of rows r0-1 .. before diagonal e-1 reads it
+            out_rows_finish<3>(t, eB, r0, endB, pb, R);
         }
         grid_arrive(t.sync);
     }

@@ -33,6 +33,9 @@ WORKLOADS = {
     "c4": dict(numseqs=30, numcols=9000, W=800, paired=0.20, mean_bl=0.05),
     # profiling-sized case of the c2 shape (about 2 GB of partials)
     "c2p": dict(numseqs=64, numcols=600, W=300, paired=0.30, mean_bl=0.10),
+    # profiling-sized case with the c4 band (the same inside/outside passes,
+    # 8 sequences so that the pair pruning holds little memory)
+    "c4p": dict(numseqs=8, numcols=9000, W=800, paired=0.20, mean_bl=0.05),
 }
 
 
