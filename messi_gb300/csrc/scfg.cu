@@ -333,6 +333,25 @@ constexpr int kSuffixThreads = 512;
 
 __host__ __device__ inline int suffix_window(int Wb) { return Wb + 64; }
 
+// Asks L2 to fetch rows [r0, r1] of a band table (RS floats per row) from
+// DRAM, `nlines` 128-byte lines from the start of each row, by threads tid
+// of nthr; rows outside [0, L) are skipped.  The suffix recurrences walk the
+// band tables one 32-row block at a time, and when the inside wavefront's
+// tables exceed L2 each block's rows would otherwise arrive at DRAM latency
+// on the single CTA's critical path.
+__device__ __forceinline__ void prefetch_rows_l2(const float* tab, int RS, int L, int r0, int r1, int nlines, int tid,
+                                                 int nthr)
+{
+    r0 = max(r0, 0);
+    r1 = min(r1, L - 1);
+    if (r1 < r0) return;
+    const int n = (r1 - r0 + 1) * nlines;
+    for (int x = tid; x < n; x += nthr) {
+        const float* p = tab + (size_t)(r0 + x / nlines) * RS + (size_t)(x % nlines) * 32;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+    }
+}
+
 // Adds to (m, s) the terms col[u] + vals[u] for the block's values u < nb,
 // where col[u] = tab[(jbase + dj*u) * RS + kbase + dk*u] (the L cell that
 // joins this thread's cell to value u; skipped when its band offset is
@@ -398,6 +417,10 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         }
     }
     int i0 = T - 1, lo = max(0, i0 - 31);
+    // the first two blocks' pushes (Lcol rows lo-33 .. i0-1) and the second
+    // block's in-block terms (first line of Lrow rows lo-32 .. lo-1)
+    prefetch_rows_l2(t.Lcol, RS, L, lo - 33, i0 - 1, RS / 32, threadIdx.x, blockDim.x);
+    prefetch_rows_l2(t.Lrow, RS, L, lo - 32, lo - 1, 1, threadIdx.x, blockDim.x);
     if (w == 1)
         for (int q = 0; q < 32; q++)
             tri2[0][q][lane] = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
@@ -447,6 +470,11 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 v[q] = (lo - 1 - q >= nlo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane) : -INFINITY;
 #pragma unroll
             for (int q = 0; q < 32; q++) tri2[tb ^ 1][q][lane] = v[q];
+        } else if (w >= 2) {
+            // the block after the next one: its pushes read Lcol rows
+            // lo-65 .. lo-34, its in-block terms Lrow rows lo-64 .. lo-33
+            prefetch_rows_l2(t.Lcol, RS, L, lo - 65, lo - 34, RS / 32, threadIdx.x - 64, blockDim.x - 64);
+            prefetch_rows_l2(t.Lrow, RS, L, lo - 64, lo - 33, 1, threadIdx.x - 64, blockDim.x - 64);
         }
         __syncthreads();
         if (lo == 0) break;
@@ -1200,17 +1228,20 @@ __device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, bo
 
 // The outside cells of one diagonal with rows [start, end), by all warps of
 // the CTA: partial sums of the first two rows of every group, then (after the
-// caller's wait) their finishing parts and any further rows whole.
+// caller's wait) their finishing parts and any further rows whole.  Row
+// start + r goes to group (first + r) mod (groups per CTA), so that the
+// second diagonal of a pair starts on the groups the first one leaves idle.
 struct OutRows {
     OutPartial c[2];
 };
 
 template <int Q>
-__device__ __forceinline__ OutRows out_rows_partial(const Band& t, int d, int start, int end, const Rules& R)
+__device__ __forceinline__ OutRows out_rows_partial(const Band& t, int d, int start, int end, int first,
+                                                    const Rules& R)
 {
     OutRows p;
     const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
-    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+    const int lane = threadIdx.x & (G - 1), g = (threadIdx.x / G + gpb - first % gpb) % gpb;
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int i = start + g + it * gpb;
@@ -1220,11 +1251,11 @@ __device__ __forceinline__ OutRows out_rows_partial(const Band& t, int d, int st
 }
 
 template <int Q>
-__device__ __forceinline__ void out_rows_finish(const Band& t, int d, int start, int end, const OutRows& p,
-                                                const Rules& R)
+__device__ __forceinline__ void out_rows_finish(const Band& t, int d, int start, int end, int first,
+                                                const OutRows& p, const Rules& R)
 {
     const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
-    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+    const int lane = threadIdx.x & (G - 1), g = (threadIdx.x / G + gpb - first % gpb) % gpb;
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const int i = start + g + it * gpb;
@@ -1255,14 +1286,15 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
         const int eB = eA - 1;
         const int sA = max(r0 - 1, 0), endA = min(r0 + rows, L - eA);
         const int endB = (eB >= 0) ? min(r0 + rows, L - eB) : r0;
-        const OutRows pa = out_rows_partial<2>(t, eA, sA, endA, R);
+        const int firstB = max(endA - sA, 0);  // diagonal e-1 after diagonal e's rows
+        const OutRows pa = out_rows_partial<2>(t, eA, sA, endA, 0, R);
         OutRows pb;
-        if (eB >= 0) pb = out_rows_partial<3>(t, eB, r0, endB, R);
+        if (eB >= 0) pb = out_rows_partial<3>(t, eB, r0, endB, firstB, R);
         if (!grid_wait(t.sync, gen)) return;
-        out_rows_finish<2>(t, eA, sA, endA, pa, R);
+        out_rows_finish<2>(t, eA, sA, endA, 0, pa, R);
         if (eB >= 0) {
             __syncthreads();  // diagonal e of rows r0-1 .. before diagonal e-1 reads it
-            out_rows_finish<3>(t, eB, r0, endB, pb, R);
+            out_rows_finish<3>(t, eB, r0, endB, firstB, pb, R);
         }
         grid_arrive(t.sync);
     }
@@ -1561,6 +1593,10 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
         as[c] = 0.f;
     }
     int i0 = 0, hi = min(T - 1, 31);
+    // the first two blocks' pushes (Lrow rows i0 .. hi+32) and the second
+    // block's in-block terms (first line of Lcol rows hi .. hi+31)
+    prefetch_rows_l2(t.Lrow, RS, t.L, i0, hi + 32, RS / 32, threadIdx.x, blockDim.x);
+    prefetch_rows_l2(t.Lcol, RS, t.L, hi, hi + 31, 1, threadIdx.x, blockDim.x);
     if (w == 1)
         for (int q = 0; q < 32; q++) {
             const int c = i0 + q;
@@ -1613,6 +1649,11 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
             }
 #pragma unroll
             for (int q = 0; q < 32; q++) tri2[tb ^ 1][q][lane] = v[q];
+        } else if (w >= 2) {
+            // the block after the next one: its pushes read Lrow rows
+            // hi+33 .. hi+64, its in-block terms Lcol rows hi+32 .. hi+63
+            prefetch_rows_l2(t.Lrow, RS, t.L, hi + 33, hi + 64, RS / 32, threadIdx.x - 64, blockDim.x - 64);
+            prefetch_rows_l2(t.Lcol, RS, t.L, hi + 32, hi + 63, 1, threadIdx.x - 64, blockDim.x - 64);
         }
         __syncthreads();
         if (hi == T - 1) break;
@@ -1717,8 +1758,10 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
     Band tt = t;
     void* args[] = {&tt, &R};
     prof_begin(ctx, 3, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
+    // paired: a CTA's two diagonals of a pair (2 x rows + 1 cells) in one
+    // pass of its warps where the CTA can grow to hold them
     int rc = launch_wave(ctx, (const void*)outside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
-                         "outside_wave_kernel");
+                         "outside_wave_kernel", true);
     if (rc) return rc;
     prof_end(ctx);
     return queue_status_readback(ctx, t);
