@@ -667,6 +667,32 @@ struct CellPartial {
     float m, s, pbv;
 };
 
+// Sixteen split points of a lane that are all in range (two blocks of eight,
+// summed in order): no predicates, and with the group width a constant the
+// 32 loads take immediate offsets from two base addresses.  Long spans spend
+// most of their points here; the integer pipe (addresses, range checks,
+// selects) was the busiest one in the predicated form.
+template <int GS>
+__device__ __forceinline__ void split_full16(float& m, float& s, const float* lrow, const float* scol, int k)
+{
+    const float* pa = lrow + k;
+    const float* pb = scol - k;
+    float a[16], b[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        a[q] = __ldcg(pa + q * GS);
+        b[q] = __ldcg(pb - q * GS);
+    }
+    float x0[8], x1[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        x0[q] = a[q] + b[q];
+        x1[q] = a[8 + q] + b[8 + q];
+    }
+    lse_add8(m, s, x0);
+    lse_add8(m, s, x1);
+}
+
 template <int NLO, int NHI, bool WIDE>
 __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int d, bool valid, int lane, int G)
 {
@@ -684,6 +710,8 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
         // flight for kernels without the registers.  Points past the end are
         // -inf, which lse_add8 skips exactly, so both forms give the same bits.
         int k = NLO + lane;
+        if (WIDE && G == 32)  // warp-uniform: one cell per warp
+            for (; k + 15 * 32 < kend; k += 16 * 32) split_full16<32>(c.m, c.s, lrow, scol, k);
         if (WIDE) {
             for (; k + 8 * G < kend; k += 16 * G) {
                 float a[16], b[16];
@@ -915,10 +943,18 @@ __device__ __forceinline__ void rows_finish(const Band& t, int d, int r0, int en
     if (!ws.mine()) return;
     const int G = group_width(d), gpb = ws.nw * (32 / G);
     const int lane = threadIdx.x & (G - 1), g = (threadIdx.x - 32 * ws.w0) / G;
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
+    if (G >= 2) {
+        // every lane of a group holds both reduced partial sums: lanes 0 and 1
+        // finish the group's two cells side by side
+        const int it = lane & 1;
         const int i = r0 + g + it * gpb;
-        inside_cell_finish(t, i, d, i < end, lane, p.c[it], R);
+        inside_cell_finish(t, i, d, lane < 2 && i < end, 0, it ? p.c[1] : p.c[0], R);
+    } else {
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+            const int i = r0 + g + it * gpb;
+            inside_cell_finish(t, i, d, i < end, lane, p.c[it], R);
+        }
     }
     for (int base = r0 + 2 * gpb; base < end; base += gpb) {
         const int i = base + g;
@@ -1256,10 +1292,17 @@ __device__ __forceinline__ void out_rows_finish(const Band& t, int d, int start,
 {
     const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
     const int lane = threadIdx.x & (G - 1), g = (threadIdx.x / G + gpb - first % gpb) % gpb;
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
+    if (G >= 2) {
+        // lanes 0 and 1 of a group finish its two cells side by side
+        const int it = lane & 1;
         const int i = start + g + it * gpb;
-        outside_finish_t<Q>(t, i, d, i < end, lane, p.c[it], R);
+        outside_finish_t<Q>(t, i, d, lane < 2 && i < end, 0, it ? p.c[1] : p.c[0], R);
+    } else {
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+            const int i = start + g + it * gpb;
+            outside_finish_t<Q>(t, i, d, i < end, lane, p.c[it], R);
+        }
     }
     for (int base = start + 2 * gpb; base < end; base += gpb) {
         const int i = base + g;
