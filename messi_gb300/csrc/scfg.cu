@@ -452,15 +452,20 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
             // serial path)
             float (&tri)[32][33] = tri2[tb];
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
-            for (int l = 0; l < nb; l++) {
-                const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
-                const int k = lane - l - 1;
-                if (lane > l && lane < nb && k <= Wb) lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
-                if (lane == 0) {
-                    const float sv = R.r[0] + lse_val(ml, sl);
-                    t.Ssuf[i0 - l] = sv;
-                    vals[l] = sv;
+#pragma unroll
+            for (int l = 0; l < 32; l++) {
+                if (l < nb) {
+                    const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
+                    const int k = lane - l - 1;
+                    if (lane > l && lane < nb && k <= Wb) lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
                 }
+            }
+            // lane q's (m, s) is final from step q on: the block's values are
+            // formed and stored by all lanes at once, off the serial path
+            if (lane < nb) {
+                const float sv = R.r[0] + lse_val(m, s);
+                t.Ssuf[i0 - lane] = sv;
+                vals[lane] = sv;
             }
         } else if (w == 1 && lo > 0) {
             // all 32 loads first, then the stores: one memory round trip
@@ -1671,16 +1676,20 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 m = -R.r[0];
                 s = 1.f;
             }
-            for (int l = 0; l < nb; l++) {
-                const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
-                const int k = lane - l - 1;
-                if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1)
-                    lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
-                if (lane == 0) {
-                    const float sv = (i0 + l == 0) ? 0.f : R.r[0] + lse_val(ml, sl);
-                    t.Osuf[i0 + l] = sv;
-                    vals[l] = sv;
+#pragma unroll
+            for (int l = 0; l < 32; l++) {
+                if (l < nb) {
+                    const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
+                    const int k = lane - l - 1;
+                    if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1)
+                        lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
                 }
+            }
+            // lane q's (m, s) is final from step q on (values stored by all lanes)
+            if (lane < nb) {
+                const float sv = (i0 + lane == 0) ? 0.f : R.r[0] + lse_val(m, s);
+                t.Osuf[i0 + lane] = sv;
+                vals[lane] = sv;
             }
         } else if (w == 1 && hi < T - 1) {
             // all 32 loads first, then the stores: one memory round trip
