@@ -97,6 +97,7 @@ struct Band {
     float *Lrow, *Lcol, *Srow, *Scol, *Frow, *pb, *Ssuf;
     float *OSrow, *OScol, *OFrow, *OFcol, *OLrow, *Osuf;
     float *PP, *SL, *nrm;
+    float* OSlast;  // suffix-column terms of the outside S sums of the last column's band cells
     double *b, *cb, *u, *Zd;
     int* maxspan;
     unsigned int* sync;  // kSyncWords grid-barrier words of the wavefront kernels

@@ -156,7 +156,7 @@ extern "C" int messi_inside_noalloc(void* stream, int32_t L, const double* d_unp
     t.Zd = d_Z;
     t.maxspan = s->maxspan;
     t.sync = s->sync;
-    t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = nullptr;
+    t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = t.OSlast = nullptr;
     if ((rc = launch_baseline(&local, t, B))) return rc;
     if ((rc = launch_bandprep_from_dense(&local, t, d_paired, B))) return rc;
     if ((rc = run_inside(&local, t, B))) return rc;

@@ -166,11 +166,12 @@ int band_alloc(messi_ctx* ctx, int L, int Wb, bool outside, Band* t)
             if ((rc = ensure(ctx, 8 + k, tab, &p))) return rc;
             *out_tabs[k] = (float*)p;
         }
-        if ((rc = ensure(ctx, 14, (size_t)2 * L * sizeof(float), &p))) return rc;
+        if ((rc = ensure(ctx, 14, (size_t)3 * L * sizeof(float), &p))) return rc;
         t->SL = (float*)p;
         t->nrm = t->SL + L;
+        t->OSlast = t->nrm + L;
     } else {
-        t->OSrow = t->OScol = t->OFrow = t->OFcol = t->OLrow = t->PP = t->SL = t->nrm = nullptr;
+        t->OSrow = t->OScol = t->OFrow = t->OFcol = t->OLrow = t->PP = t->SL = t->nrm = t->OSlast = nullptr;
     }
     return MESSI_OK;
 }
@@ -703,7 +704,8 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
 {
     const int RS = t.RS;
     CellPartial c{-INFINITY, 0.f, -INFINITY};
-    if (valid && lane == 0 && d >= 2) c.pbv = t.pb[(size_t)i * RS + d];
+    // lanes 0 and 1: either may finish the cell (rows_finish)
+    if (valid && lane < 2 && d >= 2) c.pbv = t.pb[(size_t)i * RS + d];
     const int kend = d - NHI;
     if (valid && kend > NLO) {
         const float* lrow = t.Lrow + (size_t)i * RS;
@@ -1204,11 +1206,10 @@ __device__ __forceinline__ OutPartial outside_partial_t(const Band& t, int i, in
             lse_add8(c.mS, c.sS, xs);
         }
         if (lane == 0 && hasL && L - 1 > i + Wb) lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
-        if (hasS && j == L - 1) {
-            const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
-            for (int ip = a + lane; ip <= bnd; ip += G) lse_add(c.mS, c.sS, R.r[0] + __ldcg(t.Osuf + ip) + lcol[i - 1 - ip]);
-        }
-        if (lane == 0 && hasS && j <= L - 2 && d + 2 <= Wb) c.pp = t.pb[(size_t)(i - 1) * RS + d + 2];
+        // the last column's parents beyond the band, summed before the launch
+        if (lane == 0 && hasS && j == L - 1) lse_add(c.mS, c.sS, t.OSlast[i]);
+        // lanes 0 and 1: either may finish the cell (out_rows_finish)
+        if (lane < 2 && hasS && j <= L - 2 && d + 2 <= Wb) c.pp = t.pb[(size_t)(i - 1) * RS + d + 2];
     }
     group_reduce_rt(c.mL, c.sL, G);
     group_reduce_rt(c.mS, c.sS, G);
@@ -1313,6 +1314,35 @@ __device__ __forceinline__ void out_rows_finish(const Band& t, int d, int start,
         const int i = base + g;
         outside_finish_t<Q>(t, i, d, i < end, lane, outside_partial_t<Q>(t, i, d, i < end, lane, G, R), R);
     }
+}
+
+// Suffix-column terms of the outside S sums of the last column's band cells:
+// cell (i, L-1) has the parents (ip, L-1) beyond the band, ip = max(0, i-1-Wb)
+// .. L-2-Wb, each adding r1 + OS(ip, L-1) + L(ip, i-1).  They read only the
+// suffix column and the inside tables, so one launch before the wavefront
+// sums them for every row, a warp per row: inside the wavefront the cell of
+// diagonal d has d+1 of them, summed by the single lane group of a long
+// diagonal while every other CTA waited at the next barrier.
+__global__ void outside_lastcol_kernel(Band t, Rules R)
+{
+    const int L = t.L, Wb = t.Wb, RS = t.RS;
+    const int lane = threadIdx.x & 31;
+    const int i = max(1, L - 1 - Wb) + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (i > L - 1) return;  // warp-uniform
+    const int a = max(0, i - 1 - Wb), bnd = min(i - 1, L - 2 - Wb);
+    const float* lcol = t.Lcol + (size_t)(i - 1) * RS;
+    float m = -INFINITY, s = 0.f;
+    for (int ip = a + lane; ip <= bnd; ip += 256) {
+        float x[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int iq = ip + 32 * q;
+            x[q] = (iq <= bnd) ? R.r[0] + t.Osuf[iq] + lcol[i - 1 - iq] : -INFINITY;
+        }
+        lse_add8(m, s, x);
+    }
+    group_reduce<32>(m, s);
+    if (lane == 0) t.OSlast[i] = lse_val(m, s);
 }
 
 // All band diagonals of the outside pass, descending spans, two per grid
@@ -1540,7 +1570,7 @@ int bandbatch_alloc(const std::vector<int>& L, const std::vector<int>& Wb, BandB
         t.Zd = t.u + t.L;
         t.maxspan = nullptr;
         t.sync = bb->d_sync;
-        t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = nullptr;
+        t.OSrow = t.OScol = t.OFrow = t.OFcol = t.OLrow = t.PP = t.SL = t.nrm = t.OSlast = nullptr;
         cum[k + 1] = cum[k] + t.L;
         wbs[k] = t.Wb;
     }
@@ -1806,6 +1836,13 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
         if (e != cudaSuccess) return cuda_fail(ctx, e, "outside_suffix_kernel attributes");
         outside_suffix_kernel<<<1, kSuffixThreads, (size_t)2 * win * sizeof(float), ctx->stream>>>(t, R, win);
         LAUNCH_CHECK(ctx, "outside_suffix_kernel");
+    }
+    {
+        const int rows = t.L - std::max(1, t.L - 1 - t.Wb);  // last-column band cells with i >= 1
+        if (rows > 0) {
+            outside_lastcol_kernel<<<(rows + 7) / 8, 256, 0, ctx->stream>>>(t, R);
+            LAUNCH_CHECK(ctx, "outside_lastcol_kernel");
+        }
     }
     Band tt = t;
     void* args[] = {&tt, &R};
