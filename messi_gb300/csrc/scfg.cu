@@ -1151,76 +1151,106 @@ __global__ void __launch_bounds__(kWaveMaxThreads) inside_wave_batch_kernel(cons
     }
 }
 
-// Outside cell (i, j = i+d) in two parts, as the inside cells: the parent
-// sums run over q of OS/OF(i, j+1+q) * S(j+1, j+1+q) (L) and of
-// OS/OF(i-1-q, j) * L(i-1-q, i-1) (S), spans d+1+q.  The partial part sums
-// q >= Q and the suffix-column terms, the L and S sums side by side (the 24
-// loads of a step, four points of each sum, in flight together), reduces them
-// over the group and loads the enclosing pair's score; the finishing part
-// (lane 0) adds q = 0 .. Q-1 in ascending order, forms the F value from the
-// enclosing pair (i-1, j+1) (span d+2) and writes the cell.  Diagonals go
-// two per barrier, (e, e-1), with Q = 2 for e and Q = 3 for e-1: the partial
-// sums then read spans >= e+3 only, which are complete before the wait that
-// completes e+2 and e+1.  A cell's bits do not depend on which CTA or warp
-// computes it.
-struct OutPartial {
-    float mL, sL, mS, sS, pp;
+// Outside cell (i, j = i+d): the parent sums run over q of OS/OF(i, j+1+q) *
+// S(j+1, j+1+q) (side 0, "L") and of OS/OF(i-1-q, j) * L(i-1-q, i-1) (side
+// 1, "S"), spans d+1+q.  Each sum is computed apart, by its own lane group
+// (outside_sum_t: q >= Q and the suffix-column terms, reduced over the
+// group); the finishing part (outside_finish_t, one thread) adds q = 0 ..
+// Q-1 of both sums in ascending order, forms the F value from the enclosing
+// pair (i-1, j+1) (span d+2) and writes the cell.  Diagonals go two per
+// barrier, (e, e-1), with Q = 2 for e and Q = 3 for e-1: the sums then read
+// spans >= e+3 only, which are complete before the wait that completes e+2
+// and e+1.  A cell's bits depend only on its span (the group width), not on
+// which CTA, warp or thread computes it.
+struct SumPartial {
+    float m, s;
 };
 
+// Eight points of one sum that are all in range (two blocks of four points,
+// eight terms each, summed in order): no range checks, and with the group
+// width a constant the 24 loads take immediate offsets.
+template <int GS>
+__device__ __forceinline__ void outside_full8(float& m, float& s, const float* o1, const float* o2, const float* in,
+                                              int q, const Rules& R)
+{
+    const float* p1 = o1 + q;
+    const float* p2 = o2 + q;
+    const float* p3 = in + q;
+    float a[8], b[8], v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        a[u] = __ldcg(p1 + u * GS);
+        b[u] = __ldcg(p2 + u * GS);
+        v[u] = p3[u * GS];
+    }
+    float x0[8], x1[8];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        x0[2 * u] = R.r[0] + a[u] + v[u];
+        x0[2 * u + 1] = R.r[4] + b[u] + v[u];
+        x1[2 * u] = R.r[0] + a[4 + u] + v[4 + u];
+        x1[2 * u + 1] = R.r[4] + b[4 + u] + v[4 + u];
+    }
+    lse_add8(m, s, x0);
+    lse_add8(m, s, x1);
+}
+
 template <int Q>
-__device__ __forceinline__ OutPartial outside_partial_t(const Band& t, int i, int d, bool valid, int lane, int G,
-                                                        const Rules& R)
+__device__ __forceinline__ SumPartial outside_sum_t(const Band& t, int i, int d, int side, bool valid, int lane,
+                                                    int G, const Rules& R)
 {
     const int L = t.L, Wb = t.Wb, RS = t.RS;
     const int j = i + d;
-    OutPartial c{-INFINITY, 0.f, -INFINITY, 0.f, -INFINITY};
+    SumPartial c{-INFINITY, 0.f};
     if (valid) {
-        const bool hasL = j + 1 <= L - 1, hasS = i >= 1;
-        const int nL = hasL ? min(i + Wb, L - 1) - j : 0;
-        const int nS = hasS ? i - max(0, j - Wb) : 0;
-        const float* osr = t.OSrow + (size_t)i * RS + d + 1;
-        const float* ofr = t.OFrow + (size_t)i * RS + d + 1;
-        const float* srw = t.Srow + (size_t)min(j + 1, L - 1) * RS;
-        const float* lcol = t.Lcol + (size_t)max(i - 1, 0) * RS;
-        const float* osc = t.OScol + (size_t)j * RS + d + 1;
-        const float* ofc = t.OFcol + (size_t)j * RS + d + 1;
-        const int n = max(nL, nS);
-        for (int q = Q + lane; q < n; q += 4 * G) {
-            float xl[8], xs[8];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int qq = q + u * G;
-                const bool onL = qq < nL, onS = qq < nS;
-                const float sib = onL ? srw[qq] : 0.f;
-                const float osl = onL ? __ldcg(osr + qq) : -INFINITY;
-                const float ofl = onL ? __ldcg(ofr + qq) : -INFINITY;
-                const float lft = onS ? lcol[qq] : 0.f;
-                const float oss = onS ? __ldcg(osc + qq) : -INFINITY;
-                const float ofs = onS ? __ldcg(ofc + qq) : -INFINITY;
-                xl[2 * u] = R.r[0] + osl + sib;
-                xl[2 * u + 1] = R.r[4] + ofl + sib;
-                xs[2 * u] = R.r[0] + oss + lft;
-                xs[2 * u + 1] = R.r[4] + ofs + lft;
-            }
-            lse_add8(c.mL, c.sL, xl);
-            lse_add8(c.mS, c.sS, xs);
+        int n;
+        const float *o1, *o2, *in;
+        float extra = -INFINITY;
+        if (side == 0) {
+            const bool has = j + 1 <= L - 1;
+            n = has ? min(i + Wb, L - 1) - j : 0;
+            o1 = t.OSrow + (size_t)i * RS + d + 1;
+            o2 = t.OFrow + (size_t)i * RS + d + 1;
+            in = t.Srow + (size_t)min(j + 1, L - 1) * RS;
+            if (lane == 0 && has && L - 1 > i + Wb) extra = R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1];
+        } else {
+            const bool has = i >= 1;
+            n = has ? i - max(0, j - Wb) : 0;
+            o1 = t.OScol + (size_t)j * RS + d + 1;
+            o2 = t.OFcol + (size_t)j * RS + d + 1;
+            in = t.Lcol + (size_t)max(i - 1, 0) * RS;
+            // the last column's parents beyond the band, summed before the launch
+            if (lane == 0 && has && j == L - 1) extra = t.OSlast[i];
         }
-        if (lane == 0 && hasL && L - 1 > i + Wb) lse_add(c.mL, c.sL, R.r[0] + __ldcg(t.Osuf + i) + t.Ssuf[j + 1]);
-        // the last column's parents beyond the band, summed before the launch
-        if (lane == 0 && hasS && j == L - 1) lse_add(c.mS, c.sS, t.OSlast[i]);
-        // lanes 0 and 1: either may finish the cell (out_rows_finish)
-        if (lane < 2 && hasS && j <= L - 2 && d + 2 <= Wb) c.pp = t.pb[(size_t)(i - 1) * RS + d + 2];
+        int q = Q + lane;
+        if (G == 32)  // warp-uniform: one sum per warp
+            for (; q + 7 * 32 < n; q += 8 * 32) outside_full8<32>(c.m, c.s, o1, o2, in, q, R);
+        for (; q < n; q += 8 * G) {
+            float x0[8], x1[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int qq = q + u * G;
+                const bool on = qq < n;
+                const float v = on ? in[qq] : 0.f;
+                const float a = on ? __ldcg(o1 + qq) : -INFINITY;
+                const float b = on ? __ldcg(o2 + qq) : -INFINITY;
+                float* x = (u < 4) ? x0 : x1;
+                x[2 * (u & 3)] = R.r[0] + a + v;
+                x[2 * (u & 3) + 1] = R.r[4] + b + v;
+            }
+            lse_add8(c.m, c.s, x0);
+            lse_add8(c.m, c.s, x1);
+        }
+        lse_add(c.m, c.s, extra);
     }
-    group_reduce_rt(c.mL, c.sL, G);
-    group_reduce_rt(c.mS, c.sS, G);
+    group_reduce_rt(c.m, c.s, G);
     return c;
 }
 
 template <int Q>
-__device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, bool valid, int lane, OutPartial c,
+__device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, SumPartial cl, SumPartial cs,
                                                  const Rules& R)
 {
-    if (!(valid && lane == 0)) return;
     const int L = t.L, Wb = t.Wb, RS = t.RS;
     const int j = i + d;
     const bool hasL = j + 1 <= L - 1, hasS = i >= 1;
@@ -1240,25 +1270,29 @@ __device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, bo
         oss[q] = onS ? __ldcg(t.OScol + ocol + q) : -INFINITY;
         ofs[q] = onS ? __ldcg(t.OFcol + ocol + q) : -INFINITY;
     }
+    const bool enc = hasS && j <= L - 2 && d + 2 <= Wb;
+    const size_t pr = (size_t)max(i - 1, 0) * RS + d + 2;
+    const float pp = enc ? t.pb[pr] : -INFINITY;
+    const float fa = enc ? __ldcg(t.OSrow + pr) : -INFINITY;
+    const float fb = enc ? __ldcg(t.OFrow + pr) : -INFINITY;
+    const float fc = enc ? __ldcg(t.OLrow + pr) : -INFINITY;
     float oF = -INFINITY;
-    if (c.pp != -INFINITY) {
-        const size_t pr = (size_t)(i - 1) * RS + d + 2;
-        const float a = __ldcg(t.OSrow + pr), b = __ldcg(t.OFrow + pr), e = __ldcg(t.OLrow + pr);
+    if (pp != -INFINITY) {
         float m = -INFINITY, s = 0.f;
-        lse_add(m, s, R.r[2] + c.pp + a);
-        lse_add(m, s, R.r[3] + c.pp + b);
-        lse_add(m, s, R.r[6] + c.pp + e);
+        lse_add(m, s, R.r[2] + pp + fa);
+        lse_add(m, s, R.r[3] + pp + fb);
+        lse_add(m, s, R.r[6] + pp + fc);
         oF = lse_val(m, s);
     }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-        lse_add(c.mL, c.sL, R.r[0] + osl[q] + sib[q]);
-        lse_add(c.mL, c.sL, R.r[4] + ofl[q] + sib[q]);
-        lse_add(c.mS, c.sS, R.r[0] + oss[q] + lft[q]);
-        lse_add(c.mS, c.sS, R.r[4] + ofs[q] + lft[q]);
+        lse_add(cl.m, cl.s, R.r[0] + osl[q] + sib[q]);
+        lse_add(cl.m, cl.s, R.r[4] + ofl[q] + sib[q]);
+        lse_add(cs.m, cs.s, R.r[0] + oss[q] + lft[q]);
+        lse_add(cs.m, cs.s, R.r[4] + ofs[q] + lft[q]);
     }
-    const float oL = lse_val(c.mL, c.sL);
-    float oS = lse_val(c.mS, c.sS);
+    const float oL = lse_val(cl.m, cl.s);
+    float oS = lse_val(cs.m, cs.s);
     if (i == 0 && j == L - 1) oS = 0.f;
     t.OSrow[(size_t)i * RS + d] = oS;
     t.OScol[(size_t)j * RS + d] = oS;
@@ -1268,51 +1302,47 @@ __device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, bo
     if (j == L - 1) t.Osuf[i] = oS;
 }
 
-// The outside cells of one diagonal with rows [start, end), by all warps of
-// the CTA: partial sums of the first two rows of every group, then (after the
-// caller's wait) their finishing parts and any further rows whole.  Row
-// start + r goes to group (first + r) mod (groups per CTA), so that the
-// second diagonal of a pair starts on the groups the first one leaves idle.
-struct OutRows {
-    OutPartial c[2];
-};
-
+// The sums of one diagonal's rows [start, start + nrows) before the wait:
+// task tau = 2r + side (row r, one of its two sums) goes to lane group
+// (first + tau) mod (groups per CTA), two tasks per group, each group's
+// result to slot[tau].  The second diagonal of a pair starts on the groups
+// the first one leaves idle.
 template <int Q>
-__device__ __forceinline__ OutRows out_rows_partial(const Band& t, int d, int start, int end, int first,
-                                                    const Rules& R)
+__device__ __forceinline__ void out_sums_partial(const Band& t, int d, int start, int nrows, int first,
+                                                 float2* slot, const Rules& R)
 {
-    OutRows p;
     const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
     const int lane = threadIdx.x & (G - 1), g = (threadIdx.x / G + gpb - first % gpb) % gpb;
+    const int ntask = 2 * min(nrows, gpb);
 #pragma unroll
     for (int it = 0; it < 2; it++) {
-        const int i = start + g + it * gpb;
-        p.c[it] = outside_partial_t<Q>(t, i, d, i < end, lane, G, R);
+        const int tau = g + it * gpb;
+        const bool valid = tau < ntask;
+        const SumPartial c = outside_sum_t<Q>(t, start + (tau >> 1), d, tau & 1, valid, lane, G, R);
+        if (valid && lane == 0) slot[tau] = make_float2(c.m, c.s);
     }
-    return p;
 }
 
+// After the wait: one thread per row finishes the rows whose sums are in the
+// slots; rows beyond the groups of the CTA are computed whole, both sums by
+// one group and the cell finished by its lane 0.
 template <int Q>
-__device__ __forceinline__ void out_rows_finish(const Band& t, int d, int start, int end, int first,
-                                                const OutRows& p, const Rules& R)
+__device__ __forceinline__ void out_sums_finish(const Band& t, int d, int start, int nrows, const float2* slot,
+                                                const Rules& R)
 {
     const int G = group_width(2 * (t.Wb - d) + 2), gpb = blockDim.x / G;
-    const int lane = threadIdx.x & (G - 1), g = (threadIdx.x / G + gpb - first % gpb) % gpb;
-    if (G >= 2) {
-        // lanes 0 and 1 of a group finish its two cells side by side
-        const int it = lane & 1;
-        const int i = start + g + it * gpb;
-        outside_finish_t<Q>(t, i, d, lane < 2 && i < end, 0, it ? p.c[1] : p.c[0], R);
-    } else {
-#pragma unroll
-        for (int it = 0; it < 2; it++) {
-            const int i = start + g + it * gpb;
-            outside_finish_t<Q>(t, i, d, i < end, lane, p.c[it], R);
-        }
+    const int np = min(nrows, gpb);
+    for (int r = threadIdx.x; r < np; r += blockDim.x) {
+        const float2 a = slot[2 * r], b = slot[2 * r + 1];
+        outside_finish_t<Q>(t, start + r, d, SumPartial{a.x, a.y}, SumPartial{b.x, b.y}, R);
     }
-    for (int base = start + 2 * gpb; base < end; base += gpb) {
-        const int i = base + g;
-        outside_finish_t<Q>(t, i, d, i < end, lane, outside_partial_t<Q>(t, i, d, i < end, lane, G, R), R);
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+    for (int base = np; base < nrows; base += gpb) {
+        const int r = base + g;
+        const bool valid = r < nrows;
+        const SumPartial cl = outside_sum_t<Q>(t, start + r, d, 0, valid, lane, G, R);
+        const SumPartial cs = outside_sum_t<Q>(t, start + r, d, 1, valid, lane, G, R);
+        if (valid && lane == 0) outside_finish_t<Q>(t, start + r, d, cl, cs, R);
     }
 }
 
@@ -1350,11 +1380,12 @@ __global__ void outside_lastcol_kernel(Band t, Rules R)
 // CTAs)).  For the pair (e, e-1) it computes diagonal e for its rows plus row
 // b*R - 1 (which the previous CTA also computes, to the same bits) and then,
 // after a CTA barrier, diagonal e-1, whose cells read diagonal e only at rows
-// i and i-1.  The partial sums of both diagonals read spans >= e+3 and are
-// computed between the CTA's arrival at the barrier that completes e+1 and its
-// wait there.
+// i and i-1.  The sums of both diagonals read spans >= e+3 and are computed
+// between the CTA's arrival at the barrier that completes e+1 and its wait
+// there; the finishing parts follow the wait.
 __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, Rules R)
 {
+    __shared__ float2 slotA[2 * kWaveMaxThreads], slotB[2 * kWaveMaxThreads];
     unsigned int gen = 0;
     const int L = t.L, Wb = t.Wb;
     const int rows = (L + gridDim.x - 1) / gridDim.x;
@@ -1362,19 +1393,17 @@ __global__ void __launch_bounds__(kWaveMaxThreads) outside_wave_kernel(Band t, R
     grid_arrive(t.sync);  // the suffix column was written by the previous launch
     for (int eA = Wb; eA >= 0; eA -= 2) {
         const int eB = eA - 1;
-        const int sA = max(r0 - 1, 0), endA = min(r0 + rows, L - eA);
-        const int endB = (eB >= 0) ? min(r0 + rows, L - eB) : r0;
-        const int firstB = max(endA - sA, 0);  // diagonal e-1 after diagonal e's rows
-        const OutRows pa = out_rows_partial<2>(t, eA, sA, endA, 0, R);
-        OutRows pb;
-        if (eB >= 0) pb = out_rows_partial<3>(t, eB, r0, endB, firstB, R);
+        const int sA = max(r0 - 1, 0), nA = min(r0 + rows, L - eA) - sA;
+        const int nB = (eB >= 0) ? min(r0 + rows, L - eB) - r0 : 0;
+        out_sums_partial<2>(t, eA, sA, nA, 0, slotA, R);
+        if (eB >= 0) out_sums_partial<3>(t, eB, r0, nB, 2 * max(nA, 0), slotB, R);
         if (!grid_wait(t.sync, gen)) return;
-        out_rows_finish<2>(t, eA, sA, endA, 0, pa, R);
+        out_sums_finish<2>(t, eA, sA, nA, slotA, R);
         if (eB >= 0) {
             __syncthreads();  // diagonal e of rows r0-1 .. before diagonal e-1 reads it
-            out_rows_finish<3>(t, eB, r0, endB, firstB, pb, R);
+            out_sums_finish<3>(t, eB, r0, nB, slotB, R);
         }
-        grid_arrive(t.sync);
+        grid_arrive(t.sync);  // begins with a CTA barrier: the slots are free again
     }
 }
 
@@ -1413,23 +1442,26 @@ int wave_grid(messi_ctx* ctx, const void* kernel, int L, int threads)
 static int ctas_for_rows(int L, int warps) { return (warps > 1) ? (L + warps - 2) / (warps - 1) : L; }
 
 // Launch a persistent wavefront kernel (cooperative: every CTA resident).
-// paired: the CTA owns ceil(L / grid) rows of every diagonal plus one.  The
-// CTA grows (up to 1,024 threads, unless its size is set) to the smallest
-// size at which each half of it holds those rows one per warp with at most
-// one CTA per SM, so that the pipelined halves kernel runs (GB300, band of
-// 500: 23-29% faster for 1,200-2,000 columns than 256- or 512-thread CTAs of
-// the plain kernel); the grid then grows (up to one CTA per SM) until the
-// rows fit one per warp of a half, or else of the whole CTA.
+// share > 0 (paired kernels): the CTA owns ceil(L / grid) rows of every
+// diagonal plus one, and a row wants `share` warps per diagonal pair (the
+// inside pass: one per diagonal, 2; the outside pass: one per parent sum of
+// each diagonal, 4).  The CTA grows (up to 1,024 threads, unless its size is
+// set) to the smallest size at which warps / share of its warps hold those
+// rows one per warp with at most one CTA per SM (inside: the pipelined halves
+// kernel then runs; GB300, band of 500: 23-29% faster for 1,200-2,000
+// columns than 256- or 512-thread CTAs of the plain kernel); the grid then
+// grows (up to one CTA per SM) until the rows fit, or else fit one per warp
+// of the whole CTA.
 static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
-                       double band_cells, const char* what, bool paired = false, const void* halves_kernel = nullptr)
+                       double band_cells, const char* what, int share = 0, const void* halves_kernel = nullptr)
 {
     int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "barrier reset");
     int grid = wave_grid(ctx, kernel, L, threads);  // also sets ctx->num_sms
-    if (paired && ctx->wave_ctas <= 0) {
+    if (share > 0 && ctx->wave_ctas <= 0) {
         for (int t2 = threads; t2 <= (ctx->wave_threads ? threads : kWaveMaxThreads); t2 *= 2)
-            if (ctas_for_rows(L, t2 / 64) <= ctx->num_sms) {
+            if (ctas_for_rows(L, t2 / 32 / share) <= ctx->num_sms) {
                 if (t2 != threads) {
                     threads = t2;
                     grid = wave_grid(ctx, kernel, L, threads);
@@ -1437,7 +1469,7 @@ static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned
                 break;
             }
         const int warps = threads / 32;
-        const int half = ctas_for_rows(L, warps / 2);
+        const int half = ctas_for_rows(L, warps / share);
         const int want = (half <= ctx->num_sms) ? half : ctas_for_rows(L, warps);
         grid = std::max(grid, std::min(want, ctx->num_sms));
         // the halves shape (rows + 1 <= warps / 2 for ceil(L / grid) rows)
@@ -1485,7 +1517,7 @@ int run_inside(messi_ctx* ctx, const Band& t, double B)
     void* args[] = {&tt, &R, &Bv};
     prof_begin(ctx, 1, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
     int rc = launch_wave(ctx, (const void*)inside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
-                         "inside_wave_kernel", true, (const void*)inside_wave_pipe_kernel);
+                         "inside_wave_kernel", 2, (const void*)inside_wave_pipe_kernel);
     if (rc) return rc;
     prof_end(ctx);
     if (t.L - 1 > t.Wb) {
@@ -1847,10 +1879,10 @@ int run_outside(messi_ctx* ctx, const Band& t, double B)
     Band tt = t;
     void* args[] = {&tt, &R};
     prof_begin(ctx, 3, (double)t.L * (t.Wb + 1) - 0.5 * t.Wb * (t.Wb + 1.0));
-    // paired: a CTA's two diagonals of a pair (2 x rows + 1 cells) in one
-    // pass of its warps where the CTA can grow to hold them
+    // paired: the two sums of each cell of a CTA's diagonal pair (2 x (2 x
+    // rows + 1) sums) in one pass of its warps where the CTA can grow to hold them
     int rc = launch_wave(ctx, (const void*)outside_wave_kernel, args, t.sync, t.L, (double)t.L * (t.Wb + 1),
-                         "outside_wave_kernel", true);
+                         "outside_wave_kernel", 4);
     if (rc) return rc;
     prof_end(ctx);
     return queue_status_readback(ctx, t);
