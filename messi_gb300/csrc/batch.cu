@@ -501,16 +501,22 @@ int messi_batch_likelihood(messi_ctx* ctx, messi_batch* b, const messi_model* mo
     }
     const int G = (int)reps.size();
     std::vector<Categories> cats(G);
-    std::string err;
     // lambda = 1 categories are factorised when every model group leaves out
-    // the same ones (the merged launches share one category list)
+    // the same ones (the merged launches share one category list); the
+    // models' eigensystems are built on the host threads, one model per
+    // thread (256 models of 36 categories are 9,216 16-state eigensystems)
+    std::vector<int> rcs(G);
+    std::vector<std::string> errs(G);
     for (int pass = 0; pass < 2; pass++) {
         const bool factorise = (pass == 0);
-        bool same = true;
+#pragma omp parallel for schedule(dynamic, 1) if (G >= 4)
         for (int g = 0; g < G; g++) {
             const int a = reps[g];
-            if ((rc = build_categories(&models[a], b->ds[a]->numnodes, &cats[g], &err, true, factorise)))
-                return fail(ctx, rc, err);
+            rcs[g] = build_categories(&models[a], b->ds[a]->numnodes, &cats[g], &errs[g], true, factorise, G < 4);
+        }
+        bool same = true;
+        for (int g = 0; g < G; g++) {
+            if (rcs[g]) return fail(ctx, rcs[g], errs[g]);
             same = same && cats[g].lamF == cats[0].lamF;
         }
         if (same) break;

@@ -143,7 +143,7 @@ static double safe_log(double x) { return x > 0.0 ? std::log(x) : -INFINITY; }
 // log-likelihood.  The reference's CPU path takes the same shortcut
 // (src/FARCE.jl:1891-1901).
 int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs,
-                     bool factorise)
+                     bool factorise, bool threads)
 {
     if (!m || m->nsite < 1 || m->nlambda < 1 || !m->siteRates || !m->siteWeights || !m->lambdaGC ||
         !m->lambdaAT || !m->lambdaGT || !m->lambdaWeights || !m->branchlengths) {
@@ -202,7 +202,7 @@ int build_categories(const messi_model* m, int numnodes, Categories* out, std::s
     c.lam.assign(c.C, 0);
     // the 16-state eigensystems are independent: one per host thread
     std::vector<int> bad(c.C, 0);
-#pragma omp parallel for schedule(dynamic, 1) if (pairs && c.C >= 4)
+#pragma omp parallel for schedule(dynamic, 1) if (threads && pairs && c.C >= 4)
     for (int k = 0; k < c.C; k++) {
         const int s1 = k / (ns * nk), s2 = (k / nk) % ns, l = kept[k % nk];
         c.logw[k] = safe_log(m->siteWeights[s1]) + safe_log(m->siteWeights[s2]) + safe_log(m->lambdaWeights[l]);

@@ -291,9 +291,11 @@ int prof_begin(messi_ctx* ctx, int kernel, double units);
 void prof_end(messi_ctx* ctx);
 
 // ---- host model (host_model.cpp) ----
-// pairs = false skips the 16-state eigensystems (unpaired-only calls).
+// pairs = false skips the 16-state eigensystems (unpaired-only calls);
+// threads = false keeps the eigensystems on the calling thread (callers that
+// build many models in parallel themselves).
 int build_categories(const messi_model* m, int numnodes, Categories* out, std::string* err, bool pairs = true,
-                     bool factorise = false);
+                     bool factorise = false, bool threads = true);
 void host_gtr(const double* q, const double* piv, double* Q);
 void host_musefreqs(const double* pi4, double lGC, double lAT, double lGT, double* out16);
 void host_muse(double lGC, double lAT, double lGT, const double* q, const double* pi4, double sr1, double sr2,

@@ -749,7 +749,9 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
             lse_add8(c.m, c.s, x);
         }
     }
-    group_reduce_rt(c.m, c.s, G);
+    // the shuffles only where some lane group of the warp has a cell (the
+    // callers pass every lane of the warp; an empty slot's result is unused)
+    if (__any_sync(0xffffffffu, valid)) group_reduce_rt(c.m, c.s, G);
     return c;
 }
 
@@ -810,7 +812,9 @@ __device__ __forceinline__ CellPartial partial_complete(const Band& t, int i, in
             lse_add8(c.m, c.s, x);
         }
     }
-    group_reduce_rt(c.m, c.s, G);
+    // the shuffles only where some lane group of the warp has a cell (the
+    // callers pass every lane of the warp; an empty slot's result is unused)
+    if (__any_sync(0xffffffffu, valid)) group_reduce_rt(c.m, c.s, G);
     return c;
 }
 
@@ -1243,7 +1247,9 @@ __device__ __forceinline__ SumPartial outside_sum_t(const Band& t, int i, int d,
         }
         lse_add(c.m, c.s, extra);
     }
-    group_reduce_rt(c.m, c.s, G);
+    // the shuffles only where some lane group of the warp has a cell (the
+    // callers pass every lane of the warp; an empty slot's result is unused)
+    if (__any_sync(0xffffffffu, valid)) group_reduce_rt(c.m, c.s, G);
     return c;
 }
 
