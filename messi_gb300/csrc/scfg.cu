@@ -375,35 +375,6 @@ __device__ __forceinline__ void suffix_push_terms(float& m, float& s, const floa
     }
 }
 
-// suffix_push_terms for two cells of a thread (kbase1, kbase2; the second
-// only when `two`): both cells' 64 loads are issued before either sum, so a
-// thread's share of a block's far pushes costs one memory round trip.  Each
-// cell's terms are summed in the order of suffix_push_terms.
-__device__ __forceinline__ void suffix_push_terms2(float& m1, float& s1, float& m2, float& s2, bool two,
-                                                   const float* __restrict__ tab, int RS, int jbase, int dj,
-                                                   int kbase1, int kbase2, int dk, const float* vals, int nb, int Wb)
-{
-    float x1[32], x2[32];
-#pragma unroll
-    for (int u = 0; u < 32; u++) {
-        const int k1 = kbase1 + dk * u, k2 = kbase2 + dk * u;
-        const float* row = tab + (size_t)(jbase + dj * u) * RS;
-        const float v = vals[u];
-        x1[u] = (u < nb && k1 >= 0 && k1 <= Wb) ? __ldg(row + k1) + v : -INFINITY;
-        x2[u] = (two && u < nb && k2 >= 0 && k2 <= Wb) ? __ldg(row + k2) + v : -INFINITY;
-    }
-#pragma unroll
-    for (int u = 0; u < 32; u += 8) {
-        const float y[8] = {x1[u], x1[u + 1], x1[u + 2], x1[u + 3], x1[u + 4], x1[u + 5], x1[u + 6], x1[u + 7]};
-        lse_add8(m1, s1, y);
-    }
-#pragma unroll
-    for (int u = 0; u < 32; u += 8) {
-        const float y[8] = {x2[u], x2[u + 1], x2[u + 2], x2[u + 3], x2[u + 4], x2[u + 5], x2[u + 6], x2[u + 7]};
-        lse_add8(m2, s2, y);
-    }
-}
-
 __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, float* as, int win)
 {
     const int L = t.L, Wb = t.Wb, RS = t.RS;
@@ -535,27 +506,12 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                 }
             }
         } else if (w >= 2) {
-            // two cells per thread and step (c and c - stride)
-            const int stride = (int)blockDim.x - 64, cmin = max(0, lo - 1 - Wb);
-            for (int c = nlo - 1 - (threadIdx.x - 64); c >= cmin; c -= 2 * stride) {
-                const int c2 = c - stride;
-                const bool two = c2 >= cmin;
-                const bool fresh1 = (c < c_first) && (c + Wb + 1 <= i0);
-                const bool fresh2 = (c2 < c_first) && (c2 + Wb + 1 <= i0);
-                float m1 = fresh1 ? -INFINITY : am[c % win], s1 = fresh1 ? 0.f : as[c % win];
-                float m2 = -INFINITY, s2 = 0.f;
-                if (two && !fresh2) {
-                    m2 = am[c2 % win];
-                    s2 = as[c2 % win];
-                }
-                suffix_push_terms2(m1, s1, m2, s2, two, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, i0 - 1 - c2, -1, vals,
-                                   nb, Wb);
-                am[c % win] = m1;
-                as[c % win] = s1;
-                if (two) {
-                    am[c2 % win] = m2;
-                    as[c2 % win] = s2;
-                }
+            for (int c = nlo - 1 - (threadIdx.x - 64); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 64) {
+                const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
+                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
+                suffix_push_terms(m, s, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, -1, vals, nb, Wb);
+                am[c % win] = m;
+                as[c % win] = s;
             }
         }
         tb ^= 1;
@@ -1844,27 +1800,12 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 }
             }
         } else if (w >= 2) {
-            // two cells per thread and step (c and c + stride)
-            const int stride = (int)blockDim.x - 64, cmax = min(T - 1, hi + 1 + Wb);
-            for (int c = nhi + 1 + (threadIdx.x - 64); c <= cmax; c += 2 * stride) {
-                const int c2 = c + stride;
-                const bool two = c2 <= cmax;
-                const bool fresh1 = i0 <= max(0, c - 1 - Wb);
-                const bool fresh2 = i0 <= max(0, c2 - 1 - Wb);
-                float m1 = fresh1 ? -INFINITY : am[c % win], s1 = fresh1 ? 0.f : as[c % win];
-                float m2 = -INFINITY, s2 = 0.f;
-                if (two && !fresh2) {
-                    m2 = am[c2 % win];
-                    s2 = as[c2 % win];
-                }
-                suffix_push_terms2(m1, s1, m2, s2, two, t.Lrow, RS, i0, 1, c - 1 - i0, c2 - 1 - i0, -1, vals, nb,
-                                   Wb);
-                am[c % win] = m1;
-                as[c % win] = s1;
-                if (two) {
-                    am[c2 % win] = m2;
-                    as[c2 % win] = s2;
-                }
+            for (int c = nhi + 1 + (threadIdx.x - 64); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 64) {
+                const bool fresh = i0 <= max(0, c - 1 - Wb);
+                float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
+                suffix_push_terms(m, s, t.Lrow, RS, i0, 1, c - 1 - i0, -1, vals, nb, Wb);
+                am[c % win] = m;
+                as[c % win] = s;
             }
         }
         tb ^= 1;
