@@ -375,6 +375,61 @@ __device__ __forceinline__ void suffix_push_terms(float& m, float& s, const floa
     }
 }
 
+// In-block triangle of a suffix recurrence, by one warp: lane q owns cell q
+// of the block (nb cells) and enters with the log-sum-exp (m, s) of its
+// terms from outside the block; once cell l is final it adds
+// tri[q][q-l-1] + r1 + value_l to every later lane q (recv: the lane takes
+// in-block terms).  Returns every lane's final (m, s).
+// Linear form first: values relative to the block's largest accumulator in
+// FP32, E[l] = exp(tri + r1) computed up front, so a step of the serial chain
+// is one broadcast and one multiply-add (the log form's step, two
+// exponentials and their max, took ~290 cycles).  Where a value leaves
+// [1e-30, 1e30] of the reference (FP32 would lose digits or overflow) the
+// block is redone in the log-sum-exp form.
+__device__ __forceinline__ void suffix_triangle(float& m, float& s, const float (&tri)[32][33], int nb, bool recv,
+                                                int Wb, float r1, int lane)
+{
+    float mx = m;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    const float ref = (mx == -INFINITY) ? 0.f : mx;
+    float A = (m == -INFINITY) ? 0.f : s * __expf(m - ref);
+    float E[32];
+#pragma unroll
+    for (int l = 0; l < 32; l++) {
+        const int k = lane - l - 1;
+        E[l] = (recv && l < lane && k <= Wb) ? __expf(tri[lane][max(k, 0)] + r1) : 0.f;
+    }
+    bool any = (m != -INFINITY);
+#pragma unroll
+    for (int l = 0; l < 32; l++) {
+        if (l < nb) {
+            const float V = __shfl_sync(0xffffffffu, A, l);
+            A = fmaf(E[l], V, A);
+            any = any || (E[l] > 0.f && V > 0.f);
+        }
+    }
+    const bool bad = (lane < nb) && (!(A <= 1e30f) || (any && A < 1e-30f));
+    if (!__any_sync(0xffffffffu, bad)) {
+        if (A > 0.f) {
+            m = ref;
+            s = A;
+        } else {
+            m = -INFINITY;
+            s = 0.f;
+        }
+        return;
+    }
+#pragma unroll
+    for (int l = 0; l < 32; l++) {
+        if (l < nb) {
+            const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
+            const int k = lane - l - 1;
+            if (recv && lane > l && k <= Wb) lse_add_scaled(m, s, tri[lane][k] + r1 + ml, sl);
+        }
+    }
+}
+
 __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, float* as, int win)
 {
     const int L = t.L, Wb = t.Wb, RS = t.RS;
@@ -387,6 +442,10 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     // finished block values, double-buffered: the far pushes of one block may
     // still read them while warp 0 solves the next block
     __shared__ float vals2[2][32];
+    // xs[u][q]: the L value joining next-block cell lo-1-q to this block's
+    // cell i0-u (warp 0's push after the triangle), staged a block ahead by
+    // warp 1 and read into registers at the top of the block
+    __shared__ float xs2[2][32][33];
     int parity = 0, tb = 0;
     for (int c = threadIdx.x; c < win; c += blockDim.x) {
         am[c] = -INFINITY;
@@ -422,9 +481,16 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     // block's in-block terms (first line of Lrow rows lo-32 .. lo-1)
     prefetch_rows_l2(t.Lcol, RS, L, lo - 33, i0 - 1, RS / 32, threadIdx.x, blockDim.x);
     prefetch_rows_l2(t.Lrow, RS, L, lo - 32, lo - 1, 1, threadIdx.x, blockDim.x);
-    if (w == 1)
+    if (w == 1) {
         for (int q = 0; q < 32; q++)
             tri2[0][q][lane] = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
+        const int nb0 = i0 - lo + 1, nlo0 = max(0, lo - 32), c = lo - 1 - lane;
+        for (int u = 0; u < 32; u++) {
+            const int k = i0 - 1 - c - u;
+            xs2[0][u][lane] = (lo > 0 && c >= nlo0 && u < nb0 && k <= Wb) ? __ldg(t.Lcol + (size_t)(i0 - 1 - u) * RS + k)
+                                                                          : -INFINITY;
+        }
+    }
     __syncthreads();
     float cm = -INFINITY, cs = 0.f;  // warp 0: accumulator of cell i0 - lane
     if (w == 0 && i0 - lane >= lo) {
@@ -438,44 +504,36 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         parity ^= 1;
         float x[32];  // warp 0: L values joining its next-block cell to this block's cells
         if (w == 0) {
-            // issue the next push's loads first: they do not need this block's
-            // values, and they arrive while the triangle runs
-            const int c = lo - 1 - lane;
-#pragma unroll
-            for (int u = 0; u < 32; u++) {
-                const int k = i0 - 1 - c - u;
-                x[u] = (lo > 0 && c >= nlo && u < nb && k <= Wb) ? __ldg(t.Lcol + (size_t)(i0 - 1 - u) * RS + k)
-                                                                 : -INFINITY;
-            }
-            // column-oriented substitution: lane q owns cell i0 - q; once cell
-            // l is final its (m, s) is broadcast and every later cell adds
-            // L(cell, i0 - l - 1) + r1 + m_l weighted by s_l (no log on the
-            // serial path)
-            float (&tri)[32][33] = tri2[tb];
+            // column-oriented substitution: lane q owns cell i0 - q
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
-#pragma unroll
-            for (int l = 0; l < 32; l++) {
-                if (l < nb) {
-                    const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
-                    const int k = lane - l - 1;
-                    if (lane > l && lane < nb && k <= Wb) lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
-                }
-            }
-            // lane q's (m, s) is final from step q on: the block's values are
-            // formed and stored by all lanes at once, off the serial path
+            suffix_triangle(m, s, tri2[tb], nb, lane < nb, Wb, R.r[0], lane);
+            // the block's values, formed and stored by all lanes at once
             if (lane < nb) {
                 const float sv = R.r[0] + lse_val(m, s);
                 t.Ssuf[i0 - lane] = sv;
                 vals[lane] = sv;
             }
+            // the push operands, before the barrier: warp 1 refills this
+            // buffer in the next block
+#pragma unroll
+            for (int u = 0; u < 32; u++) x[u] = xs2[tb][u][lane];
         } else if (w == 1 && lo > 0) {
-            // all 32 loads first, then the stores: one memory round trip
-            float v[32];
+            // the next block's in-block terms and push operands: all 64 loads
+            // first, then the stores (one memory round trip)
+            const int i0n = lo - 1, nbn = lo - nlo, nlon = max(0, nlo - 32), c = nlo - 1 - lane;
+            float v[32], y[32];
 #pragma unroll
-            for (int q = 0; q < 32; q++)
+            for (int q = 0; q < 32; q++) {
                 v[q] = (lo - 1 - q >= nlo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane) : -INFINITY;
+                const int k = i0n - 1 - c - q;
+                y[q] = (nlo > 0 && c >= nlon && q < nbn && k <= Wb) ? __ldg(t.Lcol + (size_t)(i0n - 1 - q) * RS + k)
+                                                                   : -INFINITY;
+            }
 #pragma unroll
-            for (int q = 0; q < 32; q++) tri2[tb ^ 1][q][lane] = v[q];
+            for (int q = 0; q < 32; q++) {
+                tri2[tb ^ 1][q][lane] = v[q];
+                xs2[tb ^ 1][q][lane] = y[q];
+            }
         } else if (w >= 2) {
             // the block after the next one: its pushes read Lcol rows
             // lo-65 .. lo-34, its in-block terms Lrow rows lo-64 .. lo-33
@@ -1703,6 +1761,9 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
     // tri[q][k] = Lcol[i0 + q - 1][k] for the block's cells i0 + q, double-buffered
     __shared__ float tri2[2][32][33];
     __shared__ float vals2[2][32];
+    // xs[u][q]: the L value joining next-block cell hi+1+q to this block's
+    // cell i0+u (warp 0's push after the triangle), staged a block ahead by warp 1
+    __shared__ float xs2[2][32][33];
     int parity = 0, tb = 0;
     for (int c = threadIdx.x; c < win; c += blockDim.x) {
         am[c] = -INFINITY;
@@ -1713,12 +1774,20 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
     // block's in-block terms (first line of Lcol rows hi .. hi+31)
     prefetch_rows_l2(t.Lrow, RS, t.L, i0, hi + 32, RS / 32, threadIdx.x, blockDim.x);
     prefetch_rows_l2(t.Lcol, RS, t.L, hi, hi + 31, 1, threadIdx.x, blockDim.x);
-    if (w == 1)
+    if (w == 1) {
         for (int q = 0; q < 32; q++) {
             const int c = i0 + q;
             tri2[0][q][lane] =
                 (c <= hi && c >= 1 && lane <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + lane) : -INFINITY;
         }
+        const int nb0 = hi - i0 + 1, nhi0 = min(T - 1, hi + 32), c = hi + 1 + lane;
+        for (int u = 0; u < 32; u++) {
+            const int k = c - 1 - i0 - u;
+            xs2[0][u][lane] = (hi < T - 1 && c <= nhi0 && u < nb0 && k >= 0 && k <= Wb)
+                                  ? __ldg(t.Lrow + (size_t)(i0 + u) * RS + k)
+                                  : -INFINITY;
+        }
+    }
     __syncthreads();
     float cm = -INFINITY, cs = 0.f;
     for (;;) {
@@ -1728,47 +1797,43 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
         parity ^= 1;
         float x[32];  // warp 0: L values joining its next-block cell to this block's cells
         if (w == 0) {
-            const int c = hi + 1 + lane;
-#pragma unroll
-            for (int u = 0; u < 32; u++) {
-                const int k = c - 1 - i0 - u;
-                x[u] = (hi < T - 1 && c <= nhi && u < nb && k >= 0 && k <= Wb)
-                           ? __ldg(t.Lrow + (size_t)(i0 + u) * RS + k)
-                           : -INFINITY;
-            }
             // column-oriented substitution (lane q owns cell i0 + q); Osuf[0]
             // = 0 is (m, s) = (-r1, 1), so every value is r1 + m + log s
-            float (&tri)[32][33] = tri2[tb];
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
             if (i0 + lane == 0) {
                 m = -R.r[0];
                 s = 1.f;
             }
-#pragma unroll
-            for (int l = 0; l < 32; l++) {
-                if (l < nb) {
-                    const float ml = __shfl_sync(0xffffffffu, m, l), sl = __shfl_sync(0xffffffffu, s, l);
-                    const int k = lane - l - 1;
-                    if (lane > l && lane < nb && k <= Wb && i0 + lane >= 1)
-                        lse_add_scaled(m, s, tri[lane][k] + R.r[0] + ml, sl);
-                }
-            }
-            // lane q's (m, s) is final from step q on (values stored by all lanes)
+            suffix_triangle(m, s, tri2[tb], nb, lane < nb && i0 + lane >= 1, Wb, R.r[0], lane);
+            // the block's values, stored by all lanes at once
             if (lane < nb) {
                 const float sv = (i0 + lane == 0) ? 0.f : R.r[0] + lse_val(m, s);
                 t.Osuf[i0 + lane] = sv;
                 vals[lane] = sv;
             }
+            // the push operands, before the barrier: warp 1 refills this
+            // buffer in the next block
+#pragma unroll
+            for (int u = 0; u < 32; u++) x[u] = xs2[tb][u][lane];
         } else if (w == 1 && hi < T - 1) {
-            // all 32 loads first, then the stores: one memory round trip
-            float v[32];
+            // the next block's in-block terms and push operands: all 64 loads
+            // first, then the stores (one memory round trip)
+            const int i0n = hi + 1, nbn = nhi - hi, nhin = min(T - 1, nhi + 32), c = nhi + 1 + lane;
+            float v[32], y[32];
 #pragma unroll
             for (int q = 0; q < 32; q++) {
                 const int cq = hi + 1 + q;
                 v[q] = (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
+                const int k = c - 1 - i0n - q;
+                y[q] = (nhi < T - 1 && c <= nhin && q < nbn && k >= 0 && k <= Wb)
+                           ? __ldg(t.Lrow + (size_t)(i0n + q) * RS + k)
+                           : -INFINITY;
             }
 #pragma unroll
-            for (int q = 0; q < 32; q++) tri2[tb ^ 1][q][lane] = v[q];
+            for (int q = 0; q < 32; q++) {
+                tri2[tb ^ 1][q][lane] = v[q];
+                xs2[tb ^ 1][q][lane] = y[q];
+            }
         } else if (w >= 2) {
             // the block after the next one: its pushes read Lrow rows
             // hi+33 .. hi+64, its in-block terms Lcol rows hi+32 .. hi+63
