@@ -353,6 +353,23 @@ __device__ __forceinline__ void prefetch_rows_l2(const float* tab, int RS, int L
     }
 }
 
+// A read-only global load under a predicate (`dflt` where it is false),
+// written as one predicated instruction so that a run of them stays a run of
+// independent loads in flight (a conditional expression may become a branch
+// around each load, and the loads one after another).  `p` is never read
+// when `pred` is false.
+__device__ __forceinline__ float ldg_if(const float* p, bool pred, float dflt)
+{
+    float v;
+    asm("{\n\t.reg .pred q;\n\t"
+        "setp.ne.b32 q, %2, 0;\n\t"
+        "mov.f32 %0, %3;\n\t"
+        "@q ld.global.nc.f32 %0, [%1];\n\t}"
+        : "=f"(v)
+        : "l"(__cvta_generic_to_global(p)), "r"((int)pred), "f"(dflt));
+    return v;
+}
+
 // Adds to (m, s) the terms col[u] + vals[u] for the block's values u < nb,
 // where col[u] = tab[(jbase + dj*u) * RS + kbase + dk*u] (the L cell that
 // joins this thread's cell to value u; skipped when its band offset is
@@ -366,8 +383,11 @@ __device__ __forceinline__ void suffix_push_terms(float& m, float& s, const floa
 #pragma unroll
     for (int u = 0; u < 32; u++) {
         const int k = kbase + dk * u;
-        x[u] = (u < nb && k >= 0 && k <= Wb) ? __ldg(tab + (size_t)(jbase + dj * u) * RS + k) + vals[u] : -INFINITY;
+        const bool on = u < nb && k >= 0 && k <= Wb;
+        x[u] = ldg_if(tab + (on ? (size_t)(jbase + dj * u) * RS + k : 0), on, -INFINITY);
     }
+#pragma unroll
+    for (int u = 0; u < 32; u++) x[u] += vals[u];
 #pragma unroll
     for (int u = 0; u < 32; u += 8) {
         const float y[8] = {x[u], x[u + 1], x[u + 2], x[u + 3], x[u + 4], x[u + 5], x[u + 6], x[u + 7]};
@@ -394,11 +414,16 @@ __device__ __forceinline__ void suffix_triangle(float& m, float& s, const float 
     for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
     const float ref = (mx == -INFINITY) ? 0.f : mx;
     float A = (m == -INFINITY) ? 0.f : s * __expf(m - ref);
+    // every shared load first (clamped index, no branch), then the
+    // exponentials, then the selects
     float E[32];
+#pragma unroll
+    for (int l = 0; l < 32; l++) E[l] = tri[lane][max(lane - l - 1, 0)];
 #pragma unroll
     for (int l = 0; l < 32; l++) {
         const int k = lane - l - 1;
-        E[l] = (recv && l < lane && k <= Wb) ? __expf(tri[lane][max(k, 0)] + r1) : 0.f;
+        const float e = __expf(E[l] + r1);
+        E[l] = (recv && l < lane && k <= Wb) ? e : 0.f;
     }
     bool any = (m != -INFINITY);
 #pragma unroll
@@ -524,10 +549,11 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
             float v[32], y[32];
 #pragma unroll
             for (int q = 0; q < 32; q++) {
-                v[q] = (lo - 1 - q >= nlo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(lo - 1 - q) * RS + lane) : -INFINITY;
+                const bool onv = lo - 1 - q >= nlo && lane <= Wb;
+                v[q] = ldg_if(t.Lrow + (onv ? (size_t)(lo - 1 - q) * RS + lane : 0), onv, -INFINITY);
                 const int k = i0n - 1 - c - q;
-                y[q] = (nlo > 0 && c >= nlon && q < nbn && k <= Wb) ? __ldg(t.Lcol + (size_t)(i0n - 1 - q) * RS + k)
-                                                                   : -INFINITY;
+                const bool ony = nlo > 0 && c >= nlon && q < nbn && k <= Wb;
+                y[q] = ldg_if(t.Lcol + (ony ? (size_t)(i0n - 1 - q) * RS + k : 0), ony, -INFINITY);
             }
 #pragma unroll
             for (int q = 0; q < 32; q++) {
@@ -1823,11 +1849,11 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
 #pragma unroll
             for (int q = 0; q < 32; q++) {
                 const int cq = hi + 1 + q;
-                v[q] = (cq <= nhi && lane <= Wb) ? __ldg(t.Lcol + (size_t)(cq - 1) * RS + lane) : -INFINITY;
+                const bool onv = cq <= nhi && lane <= Wb;
+                v[q] = ldg_if(t.Lcol + (onv ? (size_t)(cq - 1) * RS + lane : 0), onv, -INFINITY);
                 const int k = c - 1 - i0n - q;
-                y[q] = (nhi < T - 1 && c <= nhin && q < nbn && k >= 0 && k <= Wb)
-                           ? __ldg(t.Lrow + (size_t)(i0n + q) * RS + k)
-                           : -INFINITY;
+                const bool ony = nhi < T - 1 && c <= nhin && q < nbn && k >= 0 && k <= Wb;
+                y[q] = ldg_if(t.Lrow + (ony ? (size_t)(i0n + q) * RS + k : 0), ony, -INFINITY);
             }
 #pragma unroll
             for (int q = 0; q < 32; q++) {
