@@ -401,29 +401,29 @@ __device__ __forceinline__ void suffix_push_terms(float& m, float& s, const floa
 // tri[q][q-l-1] + r1 + value_l to every later lane q (recv: the lane takes
 // in-block terms).  Returns every lane's final (m, s).
 // Linear form first: values relative to the block's largest accumulator in
-// FP32, E[l] = exp(tri + r1) computed up front, so a step of the serial chain
-// is one broadcast and one multiply-add (the log form's step, two
-// exponentials and their max, took ~290 cycles).  Where a value leaves
-// [1e-30, 1e30] of the reference (FP32 would lose digits or overflow) the
-// block is redone in the log-sum-exp form.
-__device__ __forceinline__ void suffix_triangle(float& m, float& s, const float (&tri)[32][33], int nb, bool recv,
-                                                int Wb, float r1, int lane)
+// FP32, the factors E = exp(tri + r1) staged beside tri by the staging warp,
+// so a step of the serial chain is one broadcast and one multiply-add (the
+// log form's step, two exponentials and their max, took ~290 cycles).  Where
+// a value leaves [1e-30, 1e30] of the reference (FP32 would lose digits or
+// overflow) the block is redone in the log-sum-exp form.
+__device__ __forceinline__ void suffix_triangle(float& m, float& s, const float (&tri)[32][33],
+                                                const float (&etri)[32][33], int nb, bool recv, int Wb, float r1,
+                                                int lane)
 {
     float mx = m;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
     const float ref = (mx == -INFINITY) ? 0.f : mx;
     float A = (m == -INFINITY) ? 0.f : s * __expf(m - ref);
-    // every shared load first (clamped index, no branch), then the
-    // exponentials, then the selects
+    // the factors exp(tri + r1), staged with tri (unconditional shared
+    // loads at a clamped index, then the selects)
     float E[32];
 #pragma unroll
-    for (int l = 0; l < 32; l++) E[l] = tri[lane][max(lane - l - 1, 0)];
+    for (int l = 0; l < 32; l++) E[l] = etri[lane][max(lane - l - 1, 0)];
 #pragma unroll
     for (int l = 0; l < 32; l++) {
         const int k = lane - l - 1;
-        const float e = __expf(E[l] + r1);
-        E[l] = (recv && l < lane && k <= Wb) ? e : 0.f;
+        E[l] = (recv && l < lane && k <= Wb) ? E[l] : 0.f;
     }
     bool any = (m != -INFINITY);
 #pragma unroll
@@ -464,6 +464,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     // tri[q][k] = Lrow[i0 - q][k]: the in-block terms of the block's cells,
     // double-buffered (warp 1 stages the next block's while warp 0 solves)
     __shared__ float tri2[2][32][33];
+    __shared__ float etri2[2][32][33];  // exp(tri + r1), staged with tri
     // finished block values, double-buffered: the far pushes of one block may
     // still read them while warp 0 solves the next block
     __shared__ float vals2[2][32];
@@ -507,8 +508,11 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
     prefetch_rows_l2(t.Lcol, RS, L, lo - 33, i0 - 1, RS / 32, threadIdx.x, blockDim.x);
     prefetch_rows_l2(t.Lrow, RS, L, lo - 32, lo - 1, 1, threadIdx.x, blockDim.x);
     if (w == 1) {
-        for (int q = 0; q < 32; q++)
-            tri2[0][q][lane] = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
+        for (int q = 0; q < 32; q++) {
+            const float v = (i0 - q >= lo && lane <= Wb) ? __ldg(t.Lrow + (size_t)(i0 - q) * RS + lane) : -INFINITY;
+            tri2[0][q][lane] = v;
+            etri2[0][q][lane] = __expf(v + R.r[0]);
+        }
         const int nb0 = i0 - lo + 1, nlo0 = max(0, lo - 32), c = lo - 1 - lane;
         for (int u = 0; u < 32; u++) {
             const int k = i0 - 1 - c - u;
@@ -531,7 +535,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
         if (w == 0) {
             // column-oriented substitution: lane q owns cell i0 - q
             float m = (lane < nb) ? cm : -INFINITY, s = (lane < nb) ? cs : 0.f;
-            suffix_triangle(m, s, tri2[tb], nb, lane < nb, Wb, R.r[0], lane);
+            suffix_triangle(m, s, tri2[tb], etri2[tb], nb, lane < nb, Wb, R.r[0], lane);
             // the block's values, formed and stored by all lanes at once
             if (lane < nb) {
                 const float sv = R.r[0] + lse_val(m, s);
@@ -558,6 +562,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
 #pragma unroll
             for (int q = 0; q < 32; q++) {
                 tri2[tb ^ 1][q][lane] = v[q];
+                etri2[tb ^ 1][q][lane] = __expf(v[q] + R.r[0]);
                 xs2[tb ^ 1][q][lane] = y[q];
             }
         } else if (w >= 2) {
@@ -1786,6 +1791,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // tri[q][k] = Lcol[i0 + q - 1][k] for the block's cells i0 + q, double-buffered
     __shared__ float tri2[2][32][33];
+    __shared__ float etri2[2][32][33];  // exp(tri + r1), staged with tri
     __shared__ float vals2[2][32];
     // xs[u][q]: the L value joining next-block cell hi+1+q to this block's
     // cell i0+u (warp 0's push after the triangle), staged a block ahead by warp 1
@@ -1803,8 +1809,9 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
     if (w == 1) {
         for (int q = 0; q < 32; q++) {
             const int c = i0 + q;
-            tri2[0][q][lane] =
-                (c <= hi && c >= 1 && lane <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + lane) : -INFINITY;
+            const float v = (c <= hi && c >= 1 && lane <= Wb) ? __ldg(t.Lcol + (size_t)(c - 1) * RS + lane) : -INFINITY;
+            tri2[0][q][lane] = v;
+            etri2[0][q][lane] = __expf(v + R.r[0]);
         }
         const int nb0 = hi - i0 + 1, nhi0 = min(T - 1, hi + 32), c = hi + 1 + lane;
         for (int u = 0; u < 32; u++) {
@@ -1830,7 +1837,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                 m = -R.r[0];
                 s = 1.f;
             }
-            suffix_triangle(m, s, tri2[tb], nb, lane < nb && i0 + lane >= 1, Wb, R.r[0], lane);
+            suffix_triangle(m, s, tri2[tb], etri2[tb], nb, lane < nb && i0 + lane >= 1, Wb, R.r[0], lane);
             // the block's values, stored by all lanes at once
             if (lane < nb) {
                 const float sv = (i0 + lane == 0) ? 0.f : R.r[0] + lse_val(m, s);
@@ -1858,6 +1865,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
 #pragma unroll
             for (int q = 0; q < 32; q++) {
                 tri2[tb ^ 1][q][lane] = v[q];
+                etri2[tb ^ 1][q][lane] = __expf(v[q] + R.r[0]);
                 xs2[tb ^ 1][q][lane] = y[q];
             }
         } else if (w >= 2) {
