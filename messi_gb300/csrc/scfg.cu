@@ -425,14 +425,22 @@ __device__ __forceinline__ void suffix_triangle(float& m, float& s, const float 
         const int k = lane - l - 1;
         E[l] = (recv && l < lane && k <= Wb) ? E[l] : 0.f;
     }
+    // the serial chain: lane l's A is final at step l (full blocks without
+    // the per-step bound check)
+    if (nb == 32) {
+#pragma unroll
+        for (int l = 0; l < 32; l++) A = fmaf(E[l], __shfl_sync(0xffffffffu, A, l), A);
+    } else {
+#pragma unroll
+        for (int l = 0; l < 32; l++)
+            if (l < nb) A = fmaf(E[l], __shfl_sync(0xffffffffu, A, l), A);
+    }
+    // whether the lane has any term (a zero A is then an underflow), off the chain
     bool any = (m != -INFINITY);
 #pragma unroll
     for (int l = 0; l < 32; l++) {
-        if (l < nb) {
-            const float V = __shfl_sync(0xffffffffu, A, l);
-            A = fmaf(E[l], V, A);
-            any = any || (E[l] > 0.f && V > 0.f);
-        }
+        const float V = __shfl_sync(0xffffffffu, A, l);
+        any = any || (l < nb && E[l] > 0.f && V > 0.f);
     }
     const bool bad = (lane < nb) && (!(A <= 1e30f) || (any && A < 1e-30f));
     if (!__any_sync(0xffffffffu, bad)) {
