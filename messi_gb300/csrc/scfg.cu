@@ -370,6 +370,20 @@ __device__ __forceinline__ float ldg_if(const float* p, bool pred, float dflt)
     return v;
 }
 
+// ldg_if through L2 only (ld.global.cg): for the wavefronts' tables, which
+// other CTAs write during the launch.
+__device__ __forceinline__ float ldcg_if(const float* p, bool pred, float dflt)
+{
+    float v;
+    asm("{\n\t.reg .pred q;\n\t"
+        "setp.ne.b32 q, %2, 0;\n\t"
+        "mov.f32 %0, %3;\n\t"
+        "@q ld.global.cg.f32 %0, [%1];\n\t}"
+        : "=f"(v)
+        : "l"(__cvta_generic_to_global(p)), "r"((int)pred), "f"(dflt));
+    return v;
+}
+
 // Adds to (m, s) the terms col[u] + vals[u] for the block's values u < nb,
 // where col[u] = tab[(jbase + dj*u) * RS + kbase + dk*u] (the L cell that
 // joins this thread's cell to value u; skipped when its band offset is
@@ -796,6 +810,36 @@ __device__ __forceinline__ void split_full16(float& m, float& s, const float* lr
     lse_add8(m, s, x1);
 }
 
+// The last rem points (1..16) of a lane at G = 32, in one or two blocks of
+// eight (TWO), summed in order: predicated loads at constant offsets from two
+// base addresses, the absent points -inf.  Most of a lane's points on bands
+// up to 800 wide fall here (at most 25 per lane).
+template <bool TWO>
+__device__ __forceinline__ void split_tail32(float& m, float& s, const float* lrow, const float* scol, int k,
+                                             int rem)
+{
+    constexpr int NQ = TWO ? 16 : 8;
+    const float* pa = lrow + k;
+    const float* pb = scol - k;
+    float a[NQ], b[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        const bool on = q < rem;
+        a[q] = ldcg_if(pa + q * 32, on, -INFINITY);
+        b[q] = ldcg_if(pb - q * 32, on, -INFINITY);
+    }
+    float x0[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x0[q] = a[q] + b[q];
+    lse_add8(m, s, x0);
+    if (TWO) {
+        float x1[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) x1[q] = a[(8 + q) % NQ] + b[(8 + q) % NQ];
+        lse_add8(m, s, x1);
+    }
+}
+
 template <int NLO, int NHI, bool WIDE>
 __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int d, bool valid, int lane, int G)
 {
@@ -814,36 +858,50 @@ __device__ __forceinline__ CellPartial cell_partial_t(const Band& t, int i, int 
         // flight for kernels without the registers.  Points past the end are
         // -inf, which lse_add8 skips exactly, so both forms give the same bits.
         int k = NLO + lane;
-        if (WIDE && G == 32)  // warp-uniform: one cell per warp
-            for (; k + 15 * 32 < kend; k += 16 * 32) split_full16<32>(c.m, c.s, lrow, scol, k);
-        if (WIDE) {
-            for (; k + 8 * G < kend; k += 16 * G) {
-                float a[16], b[16];
-#pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    const int kq = k + q * G;
-                    const bool on = kq < kend;
-                    a[q] = on ? __ldcg(lrow + kq) : -INFINITY;
-                    b[q] = on ? __ldcg(scol - kq) : -INFINITY;
+        if (G == 32) {  // warp-uniform: one cell per warp, constant strides
+            int rem;
+            if (WIDE) {
+                for (; k + 15 * 32 < kend; k += 16 * 32) split_full16<32>(c.m, c.s, lrow, scol, k);
+                rem = (kend - k + 31) / 32;  // points left (<= 0: none)
+                if (rem > 8) {
+                    split_tail32<true>(c.m, c.s, lrow, scol, k, rem);
+                    rem = 0;
                 }
-                float x0[8], x1[8];
+            } else {
+                rem = (kend - k + 31) / 32;
+            }
+            for (; rem > 0; rem -= 8, k += 8 * 32) split_tail32<false>(c.m, c.s, lrow, scol, k, rem);
+        } else {
+            if (WIDE) {
+                for (; k + 8 * G < kend; k += 16 * G) {
+                    float a[16], b[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int kq = k + q * G;
+                        const bool on = kq < kend;
+                        a[q] = ldcg_if(lrow + kq, on, -INFINITY);
+                        b[q] = ldcg_if(scol - kq, on, -INFINITY);
+                    }
+                    float x0[8], x1[8];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        x0[q] = a[q] + b[q];
+                        x1[q] = a[8 + q] + b[8 + q];
+                    }
+                    lse_add8(c.m, c.s, x0);
+                    lse_add8(c.m, c.s, x1);
+                }
+            }
+            for (; k < kend; k += 8 * G) {
+                float x[8];
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
-                    x0[q] = a[q] + b[q];
-                    x1[q] = a[8 + q] + b[8 + q];
+                    const int kq = k + q * G;
+                    const bool on = kq < kend;
+                    x[q] = ldcg_if(lrow + kq, on, -INFINITY) + ldcg_if(scol - kq, on, -INFINITY);
                 }
-                lse_add8(c.m, c.s, x0);
-                lse_add8(c.m, c.s, x1);
+                lse_add8(c.m, c.s, x);
             }
-        }
-        for (; k < kend; k += 8 * G) {
-            float x[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int kq = k + q * G;
-                x[q] = (kq < kend) ? __ldcg(lrow + kq) + __ldcg(scol - kq) : -INFINITY;
-            }
-            lse_add8(c.m, c.s, x);
         }
     }
     // the shuffles only where some lane group of the warp has a cell (the
@@ -872,12 +930,23 @@ __device__ __forceinline__ void partial_issue(const Band& t, int i, int d, bool 
     const int kend = d - NHI;
     const float* lrow = t.Lrow + (size_t)i * RS;
     const float* scol = t.Scol + (size_t)(i + d) * RS + (d - 1);
+    if (G == 32) {  // constant strides from two base addresses
+        const float* pa = lrow + NLO + lane;
+        const float* pb = scol - NLO - lane;
 #pragma unroll
-    for (int q = 0; q < 16; q++) {
-        const int kq = NLO + lane + q * G;
-        const bool on = valid && kq < kend;
-        pp.a[q] = on ? __ldcg(lrow + kq) : -INFINITY;
-        pp.b[q] = on ? __ldcg(scol - kq) : -INFINITY;
+        for (int q = 0; q < 16; q++) {
+            const bool on = valid && NLO + lane + q * 32 < kend;
+            pp.a[q] = ldcg_if(pa + q * 32, on, -INFINITY);
+            pp.b[q] = ldcg_if(pb - q * 32, on, -INFINITY);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int kq = NLO + lane + q * G;
+            const bool on = valid && kq < kend;
+            pp.a[q] = ldcg_if(lrow + kq, on, -INFINITY);
+            pp.b[q] = ldcg_if(scol - kq, on, -INFINITY);
+        }
     }
 }
 
