@@ -1393,8 +1393,29 @@ __device__ __forceinline__ SumPartial outside_sum_t(const Band& t, int i, int d,
             if (lane == 0 && has && j == L - 1) extra = t.OSlast[i];
         }
         int q = Q + lane;
-        if (G == 32)  // warp-uniform: one sum per warp
+        if (G == 32) {  // warp-uniform: one sum per warp, constant strides
             for (; q + 7 * 32 < n; q += 8 * 32) outside_full8<32>(c.m, c.s, o1, o2, in, q, R);
+            const int rem = (n - q + 31) / 32;  // points left (0..7)
+            if (rem > 0) {
+                const float* p1 = o1 + q;
+                const float* p2 = o2 + q;
+                const float* p3 = in + q;
+                float x0[8], x1[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const bool on = u < rem;
+                    const float v = ldg_if(p3 + u * 32, on, 0.f);
+                    const float a = ldcg_if(p1 + u * 32, on, -INFINITY);
+                    const float b = ldcg_if(p2 + u * 32, on, -INFINITY);
+                    float* x = (u < 4) ? x0 : x1;
+                    x[2 * (u & 3)] = R.r[0] + a + v;
+                    x[2 * (u & 3) + 1] = R.r[4] + b + v;
+                }
+                lse_add8(c.m, c.s, x0);
+                lse_add8(c.m, c.s, x1);
+            }
+            q = n;
+        }
         for (; q < n; q += 8 * G) {
             float x0[8], x1[8];
 #pragma unroll
