@@ -1034,8 +1034,12 @@ __device__ __forceinline__ void cell_write_t(const Band& t, int i, int d, CellPa
 {
     const int RS = t.RS;
     const int j = i + d;
+    // the outer split points as one block (one max, independent exponentials:
+    // this is the serial part of a cell after the barrier)
+    float x[8];
 #pragma unroll
-    for (int q = 0; q < NLO + NHI; q++) lse_add(c.m, c.s, o.l[q] + o.s[q]);
+    for (int q = 0; q < 8; q++) x[q] = (q < NLO + NHI) ? o.l[q % (NLO + NHI)] + o.s[q % (NLO + NHI)] : -INFINITY;
+    lse_add8(c.m, c.s, x);
     const float tmp = lse_val(c.m, c.s);
     const float v = c.pbv + o.fin;
     const float S = lse2f(R.r[0] + tmp, R.r[2] + v);
@@ -1472,18 +1476,22 @@ __device__ __forceinline__ void outside_finish_t(const Band& t, int i, int d, Su
     float oF = -INFINITY;
     if (pp != -INFINITY) {
         float m = -INFINITY, s = 0.f;
-        lse_add(m, s, R.r[2] + pp + fa);
-        lse_add(m, s, R.r[3] + pp + fb);
-        lse_add(m, s, R.r[6] + pp + fc);
+        lse_add4(m, s, R.r[2] + pp + fa, R.r[3] + pp + fb, R.r[6] + pp + fc, -INFINITY);
         oF = lse_val(m, s);
     }
+    // the near parents of each sum as one block (one max, independent exponentials)
+    float xl[8], xs[8];
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-        lse_add(cl.m, cl.s, R.r[0] + osl[q] + sib[q]);
-        lse_add(cl.m, cl.s, R.r[4] + ofl[q] + sib[q]);
-        lse_add(cs.m, cs.s, R.r[0] + oss[q] + lft[q]);
-        lse_add(cs.m, cs.s, R.r[4] + ofs[q] + lft[q]);
+    for (int q = 0; q < 4; q++) {
+        const bool on = q < Q;
+        const int qq = on ? q : 0;
+        xl[2 * q] = on ? R.r[0] + osl[qq] + sib[qq] : -INFINITY;
+        xl[2 * q + 1] = on ? R.r[4] + ofl[qq] + sib[qq] : -INFINITY;
+        xs[2 * q] = on ? R.r[0] + oss[qq] + lft[qq] : -INFINITY;
+        xs[2 * q + 1] = on ? R.r[4] + ofs[qq] + lft[qq] : -INFINITY;
     }
+    lse_add8(cl.m, cl.s, xl);
+    lse_add8(cs.m, cs.s, xs);
     const float oL = lse_val(cl.m, cl.s);
     float oS = lse_val(cs.m, cs.s);
     if (i == 0 && j == L - 1) oS = 0.f;
