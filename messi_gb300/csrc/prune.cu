@@ -287,56 +287,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// Bulk copies of child rows into a warp's stage, completed on an mbarrier:
-// the copy engine moves the rows, so the L1 data pipe (the pruning kernel's
-// busiest unit with per-lane cp.async gathers) carries only the reads.
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
-
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void bulk_copy_row(void* dst, const float* src, unsigned long long* bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     smem_u32(dst)),
-                 "l"(__cvta_generic_to_global(src)), "r"(64), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// Bounded wait for the phase with the given parity: false after kMbarSpins
-// polls (each try_wait suspends for a bounded, hardware-defined time).
-constexpr int kMbarSpins = 1 << 20;
-
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity)
-{
-    const unsigned a = smem_u32(bar);
-    for (int i = 0; i < kMbarSpins; i++) {
-        unsigned ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
 // Exact power-of-two rescale of a row max m > 0: m * 2^-ex in [0.5, 1).
 __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
 {
@@ -361,10 +311,8 @@ __device__ __forceinline__ void pow2_scale(float m, int& ex, float& sc)
 
 // Per-warp staging of one category: 8 float4 per lane (child rows) + 2 exponents.
 struct WarpStage {
-    float rows[2][32][16];  // left and right child rows of the warp's 32 pairs (pair-major, 64 B each)
+    float4 x[8][32];
     int e[2][32];
-    unsigned long long bar;  // completes when the stage's 64 row copies have landed
-    unsigned long long pad;
 };
 
 template <bool ROOT, int STAGES, int MINB>
@@ -382,35 +330,32 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
     const int base = tile.y + warp * 32;  // first pair of this warp
     if (base >= n) return;                // whole warp idle (warp-uniform)
     WarpStage* stage = reinterpret_cast<WarpStage*>(smem_raw) + (size_t)warp * STAGES;
-    if (lane == 0)
-        for (int s0 = 0; s0 < STAGES; s0++) mbar_init(&stage[s0].bar, 1);
-    fence_mbar_init();
-    __syncwarp();
-    // child rows of pair base + lane (copied by this lane) and of pair
-    // g + 8t (whose scalars this lane keeps), clamped to a valid row past the end
-    const int cu = min(base + lane, n - 1);
-    const int cl = __ldg(nd.li + cu), cr = __ldg(nd.ri + cu);
-    const int myu = base + g + 8 * t;
+    // child rows of pairs g + 8k (clamped to a valid row past the end)
+    int li[4], ri[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int u = base + g + 8 * k;
+        const int uc = (u < n) ? u : (n - 1);
+        li[k] = __ldg(nd.li + uc);
+        ri[k] = __ldg(nd.ri + uc);
+    }
+    const int myu = base + g + 8 * t;  // pair whose scalars this lane keeps
     const bool myvalid = myu < n;
-    const int mu = min(myu, n - 1);
-    const int myl = __ldg(nd.li + mu), myr = __ldg(nd.ri + mu);
+    const int myl = li[0] * (t == 0) + li[1] * (t == 1) + li[2] * (t == 2) + li[3] * (t == 3);
+    const int myr = ri[0] * (t == 0) + ri[1] * (t == 1) + ri[2] * (t == 2) + ri[3] * (t == 3);
     const float* lf = nd.lf;
     const float* rf = nd.rf;
     const int* le = nd.le;
     const int* re = nd.re;
     const long long lcs = nd.lcs, rcs = nd.rcs;
-    bool stalled = false;
-    // issue the copies of category cc into its stage: every lane's reads of
-    // the stage's previous rows are done (the warp barrier), lane 0 announces
-    // the 4 KB, each lane copies its pair's two rows; the exponents by cp.async
-    // (each lane copies what it later reads)
+    // issue the copies of category cc into its stage (each lane copies what it later reads)
     auto issue = [&](int cc) {
         WarpStage& st = stage[cc % STAGES];
-        __syncwarp();
-        fence_proxy_async_smem();
-        if (lane == 0) mbar_arrive_expect_tx(&st.bar, 2 * 32 * 64);
-        bulk_copy_row(&st.rows[0][lane][0], lf + ((size_t)cc * lcs + cl) * 16, &st.bar);
-        bulk_copy_row(&st.rows[1][lane][0], rf + ((size_t)cc * rcs + cr) * 16, &st.bar);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            cp_async16(&st.x[k][lane], lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
+            cp_async16(&st.x[4 + k][lane], rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
+        }
         if (le) cp_async4(&st.e[0][lane], le + (size_t)cc * lcs + myl);
         if (re) cp_async4(&st.e[1][lane], re + (size_t)cc * rcs + myr);
     };
@@ -431,16 +376,13 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
         if (cc + STAGES - 1 < nc) issue(cc + STAGES - 1);
         cp_async_commit();
         cp_async_wait<STAGES - 1>();
-        WarpStage& st = stage[cc % STAGES];
-        if (!mbar_wait(&st.bar, (unsigned)(cc / STAGES) & 1u)) stalled = true;
-        const float bad = stalled ? __int_as_float(0x7fc00000) : 1.f;  // a stalled copy poisons the results
+        const WarpStage& st = stage[cc % STAGES];
         // x = m_left * m_right: states 4t..4t+3 of pairs g + 8k
         float4 X[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const float4 a = reinterpret_cast<const float4*>(&st.rows[0][g + 8 * k][0])[t];
-            const float4 b = reinterpret_cast<const float4*>(&st.rows[1][g + 8 * k][0])[t];
-            X[k] = make_float4(a.x * b.x * bad, a.y * b.y, a.z * b.z, a.w * b.w);
+            const float4 a = st.x[k][lane], b = st.x[4 + k][lane];
+            X[k] = make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
         }
         const int e = (le ? st.e[0][lane] : 0) + (re ? st.e[1][lane] : 0);
         if (ROOT) {
@@ -522,14 +464,6 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
                 const int ex = exk[0] * (t == 0) + exk[1] * (t == 1) + exk[2] * (t == 2) + exk[3] * (t == 3);
                 nd.oe[(size_t)cc * nd.ocs + myu] = e + ex;
             }
-        }
-    }
-    if (stalled) {
-        // a copy that did not land in time: wait (bounded) for the stages'
-        // last copies before the CTA's shared memory is released
-        for (int s0 = 0; s0 < STAGES && s0 < nc; s0++) {
-            const int last = s0 + ((nc - 1 - s0) / STAGES) * STAGES;
-            mbar_wait(&stage[s0].bar, (unsigned)(last / STAGES) & 1u);
         }
     }
     cp_async_wait<0>();
