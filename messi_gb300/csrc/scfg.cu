@@ -409,12 +409,6 @@ __device__ __forceinline__ void suffix_push_terms(float& m, float& s, const floa
     }
 }
 
-// Named CTA barrier 1 (barrier 0 is __syncthreads): the far-push warps wait
-// there for warp 0's push into the next block, so that warp 0's loads are not
-// queued behind theirs (warp 0's push is on the recurrence's serial path).
-__device__ __forceinline__ void bar_arrive1(int nthreads) { asm volatile("bar.arrive 1, %0;\n" ::"r"(nthreads) : "memory"); }
-__device__ __forceinline__ void bar_sync1(int nthreads) { asm volatile("bar.sync 1, %0;\n" ::"r"(nthreads) : "memory"); }
-
 // In-block triangle of a suffix recurrence, by one warp: lane q owns cell q
 // of the block (nb cells) and enters with the log-sum-exp (m, s) of its
 // terms from outside the block; once cell l is final it adds
@@ -622,9 +616,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
                     lse_add8(cm, cs, y);
                 }
             }
-            bar_arrive1((int)blockDim.x - 32);
         } else if (w >= 2) {
-            bar_sync1((int)blockDim.x - 32);
             for (int c = nlo - 1 - (threadIdx.x - 64); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 64) {
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
@@ -2012,9 +2004,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
                     lse_add8(cm, cs, y);
                 }
             }
-            bar_arrive1((int)blockDim.x - 32);
         } else if (w >= 2) {
-            bar_sync1((int)blockDim.x - 32);
             for (int c = nhi + 1 + (threadIdx.x - 64); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 64) {
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
