@@ -440,6 +440,15 @@ def run_ours(args):
     # ---- e2e: the reference-facing call chain with host buffers
     ne2e = min(args.steps, 5)
     t_e2e = []
+    # warm-up: the pairs-only and inside-only entry points are workloads of
+    # their own for the launch-shape autotuner, whose first calls time
+    # candidate shapes
+    for k in range(max(args.warmup, 5)):
+        prm = params[k % len(params)]
+        u = api.computeunpairedlikelihoods(ds, prm, ctx=ctx)
+        mat, _ = api.felsensteincuda(ds, prm, None, W, ctx=ctx)
+        api.maskgapped(mat, ds.gapfrequency, 1.0, -np.inf)
+        api.computeinsideKH99(u, mat, ctx=ctx)
     for k in range(ne2e):
         prm = params[args.warmup + k]
         torch.cuda.synchronize()
