@@ -72,21 +72,23 @@ __device__ __forceinline__ void lse_add4(float& m, float& s, float x0, float x1,
 }
 
 // Eight terms at once (sixteen independent loads in flight per lane).
+// Without branches: the rescale of (m, s) always runs (exp(0) = 1 leaves s
+// exactly as it is when the block brings no larger term, and a block of
+// -inf terms adds exact zeros), so lanes of a warp never diverge here.
 __device__ __forceinline__ void lse_add8(float& m, float& s, const float (&x)[8])
 {
     float mx = x[0];
 #pragma unroll
     for (int q = 1; q < 8; q++) mx = fmaxf(mx, x[q]);
-    if (mx == -INFINITY) return;
-    if (mx > m) {
-        s *= __expf(m - mx);
-        m = mx;
-    }
+    const float nm = fmaxf(m, mx);
+    const float base = (nm == -INFINITY) ? 0.f : nm;
+    s *= __expf(m - base);
+    m = nm;
     float a = 0.f, b = 0.f;
 #pragma unroll
     for (int q = 0; q < 8; q += 2) {
-        a += __expf(x[q] - m);
-        b += __expf(x[q + 1] - m);
+        a += __expf(x[q] - base);
+        b += __expf(x[q + 1] - base);
     }
     s += a + b;
 }
