@@ -387,20 +387,23 @@ __device__ __forceinline__ float ldcg_if(const float* p, bool pred, float dflt)
 }
 
 // Adds to (m, s) the terms col[u] + vals[u] for the block's values u < nb,
-// where col[u] = tab[(jbase + dj*u) * RS + kbase + dk*u] (the L cell that
-// joins this thread's cell to value u; skipped when its band offset is
-// outside 0..Wb): the 32 loads are issued together, then summed in blocks of
-// eight.
+// where col[u] = tab[(jbase + dj*u) * RS + kbase - u] (the L cell that joins
+// this thread's cell to value u; skipped when its band offset kbase - u is
+// outside 0..Wb): the valid u are one range, computed once, and the
+// addresses one base plus u times a stride, so a load costs two compares and
+// an address step; the 32 loads are issued together, then summed in blocks
+// of eight.
 __device__ __forceinline__ void suffix_push_terms(float& m, float& s, const float* __restrict__ tab, int RS,
-                                                  int jbase, int dj, int kbase, int dk, const float* vals, int nb,
-                                                  int Wb)
+                                                  int jbase, int dj, int kbase, const float* vals, int nb, int Wb)
 {
+    const int ulo = max(0, kbase - Wb), uhi = min(nb - 1, kbase);
+    const long long step = (long long)dj * RS - 1;
+    const float* base = tab + ((ulo <= uhi) ? (long long)jbase * RS + kbase : 0);
     float x[32];
 #pragma unroll
     for (int u = 0; u < 32; u++) {
-        const int k = kbase + dk * u;
-        const bool on = u < nb && k >= 0 && k <= Wb;
-        x[u] = ldg_if(tab + (on ? (size_t)(jbase + dj * u) * RS + k : 0), on, -INFINITY);
+        const bool on = u >= ulo && u <= uhi;
+        x[u] = ldg_if(base + (on ? u * step : 0), on, -INFINITY);
     }
 #pragma unroll
     for (int u = 0; u < 32; u++) x[u] += vals[u];
@@ -622,7 +625,7 @@ __device__ void inside_suffix_body(const Band& t, const Rules& R, float* am, flo
             for (int c = nlo - 1 - (threadIdx.x - 64); c >= max(0, lo - 1 - Wb); c -= (int)blockDim.x - 64) {
                 const bool fresh = (c < c_first) && (c + Wb + 1 <= i0);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
-                suffix_push_terms(m, s, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, -1, vals, nb, Wb);
+                suffix_push_terms(m, s, t.Lcol, RS, i0 - 1, -1, i0 - 1 - c, vals, nb, Wb);
                 am[c % win] = m;
                 as[c % win] = s;
             }
@@ -2024,7 +2027,7 @@ __device__ void outside_suffix_body(const Band& t, const Rules& R, float* am, fl
             for (int c = nhi + 1 + (threadIdx.x - 64); c <= min(T - 1, hi + 1 + Wb); c += (int)blockDim.x - 64) {
                 const bool fresh = i0 <= max(0, c - 1 - Wb);
                 float m = fresh ? -INFINITY : am[c % win], s = fresh ? 0.f : as[c % win];
-                suffix_push_terms(m, s, t.Lrow, RS, i0, 1, c - 1 - i0, -1, vals, nb, Wb);
+                suffix_push_terms(m, s, t.Lrow, RS, i0, 1, c - 1 - i0, vals, nb, Wb);
                 am[c % win] = m;
                 as[c % win] = s;
             }
