@@ -63,30 +63,36 @@ __global__ void to_double_kernel(const float* __restrict__ in, double* __restric
 // pair[i*L + k], the reference kernel's indexing (the matrix is symmetric).
 //
 // Cell (i, j = i+d): the best split over k = i+1 .. j-1 of
-// alpha*pair(i,k) + e(i+1,k-1) + e(k+1,j) reads cells of spans <= d-2 only,
-// as does e2 = alpha*pair(i,j) + e(i+1,j-1); only e1 = single(i) + e(i+1,j)
-// reads diagonal d-1.  decode_cell_split computes the split maximum (lowest k
-// among equal values, the reference's order) and e2; decode_cell_finish adds
-// e1 and writes the cell.  The wavefront computes the split part of its first
-// cells between its arrival at the barrier of diagonal d-1 and its wait.
+// alpha*pair(i,k) + e(i+1,k-1) + e(k+1,j), e2 = alpha*pair(i,j) + e(i+1,j-1)
+// and e1 = single(i) + e(i+1,j).  Split point k reads spans k-i-2 and j-k-1.
+// Diagonals go two per grid barrier, (dA, dB) = (2p-1, 2p): decode_split_t
+// takes the split points k = i+KLO .. j-KHI, whose spans are <= 2p-4 and so
+// complete before the wait on the barrier that completes 2p-2 (dA: KLO = 2,
+// KHI = 1; dB: KLO = 3, KHI = 2), as a lane-group (value, k) arg-max;
+// decode_finish_t adds the outer split points in ascending k, e2 and e1 and
+// writes the cell.  The maximum is exact and ties go to the smallest k (the
+// reference's loop order) however the points are split, so the bits are the
+// reference kernel's.
 struct DecodePart {
-    float bv, e2;
+    float bv;
     int bk;
 };
 
-__device__ __forceinline__ DecodePart decode_cell_split(const float* __restrict__ pair, const float* erow,
-                                                        const float* ecol, int L, float alpha, int i, int d,
-                                                        bool valid, int lane, int G)
+template <int KLO, int KHI>
+__device__ __forceinline__ DecodePart decode_split_t(const float* __restrict__ pair, const float* erow,
+                                                     const float* ecol, int L, float alpha, int i, int d,
+                                                     bool valid, int lane, int G)
 {
-    DecodePart p{-1e10f, -INFINITY, 0};  // the reference's initial maximum and index
+    DecodePart p{-1e10f, 0};  // the reference's initial maximum and index
     const int j = i + d;
     if (valid) {
         const float* prow = pair + (size_t)i * L;
         const float* er = erow + (size_t)(i + 1) * L;  // e(i+1, k-1)
         const float* ec = ecol + (size_t)j * L;        // e(k+1, j)
-        int k = i + 1 + lane;
+        const int kend = j - KHI;
+        int k = i + KLO + lane;
         // four splits per step, loads issued together, compared in ascending k
-        for (; k + 3 * G <= j - 1; k += 4 * G) {
+        for (; k + 3 * G <= kend; k += 4 * G) {
             float v[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -100,35 +106,44 @@ __device__ __forceinline__ DecodePart decode_cell_split(const float* __restrict_
                     p.bk = k + q * G;
                 }
         }
-        for (; k <= j - 1; k += G) {
+        for (; k <= kend; k += G) {
             const float v = __fmaf_rn(alpha, __ldg(prow + k), __ldcg(er + k - 1)) + __ldcg(ec + k + 1);
             if (v > p.bv) {
                 p.bv = v;
                 p.bk = k;
             }
         }
-        if (lane == 0)
-            p.e2 = __fmaf_rn(alpha, __ldg(pair + (size_t)i * L + j), __ldcg(erow + (size_t)(i + 1) * L + j - 1));
     }
-    for (int off = G >> 1; off > 0; off >>= 1) {
-        const float v2 = __shfl_xor_sync(0xffffffffu, p.bv, off);
-        const int k2 = __shfl_xor_sync(0xffffffffu, p.bk, off);
-        amax_merge(p.bv, p.bk, v2, k2);
-    }
+    if (__any_sync(0xffffffffu, valid))
+        for (int off = G >> 1; off > 0; off >>= 1) {
+            const float v2 = __shfl_xor_sync(0xffffffffu, p.bv, off);
+            const int k2 = __shfl_xor_sync(0xffffffffu, p.bk, off);
+            amax_merge(p.bv, p.bk, v2, k2);
+        }
     return p;
 }
 
-__device__ __forceinline__ void decode_cell_finish(const float* __restrict__ single, float* erow, float* ecol,
-                                                   int* scol, int L, int i, int d, bool valid, int lane,
-                                                   const DecodePart& p)
+template <int KLO, int KHI>
+__device__ __forceinline__ void decode_finish_t(const float* __restrict__ single, const float* __restrict__ pair,
+                                                float* erow, float* ecol, int* scol, int L, float alpha, int i,
+                                                int d, bool valid, DecodePart p)
 {
-    if (!(valid && lane == 0)) return;
+    if (!valid) return;
     const int j = i + d;
-    const float e1 = __ldg(single + i) + __ldcg(erow + (size_t)(i + 1) * L + j);
+    const float* prow = pair + (size_t)i * L;
+    const float* er = erow + (size_t)(i + 1) * L;
+    const float* ec = ecol + (size_t)j * L;
+    // the outer split points, ascending k (ties to the smaller k)
+    for (int k = i + 1; k <= min(i + KLO - 1, j - 1); k++)
+        amax_merge(p.bv, p.bk, __fmaf_rn(alpha, __ldg(prow + k), __ldcg(er + k - 1)) + __ldcg(ec + k + 1), k);
+    for (int k = max(i + KLO, j - KHI + 1); k <= j - 1; k++)
+        amax_merge(p.bv, p.bk, __fmaf_rn(alpha, __ldg(prow + k), __ldcg(er + k - 1)) + __ldcg(ec + k + 1), k);
+    const float e2 = __fmaf_rn(alpha, __ldg(prow + j), __ldcg(er + j - 1));
+    const float e1 = __ldg(single + i) + __ldcg(er + j);
     float mv = e1;
     int sv = -1;
-    if (p.e2 > mv) {
-        mv = p.e2;
+    if (e2 > mv) {
+        mv = e2;
         sv = -2;
     }
     if (p.bv > mv) {
@@ -140,6 +155,61 @@ __device__ __forceinline__ void decode_cell_finish(const float* __restrict__ sin
     scol[(size_t)j * L + i] = sv;
 }
 
+// The cells of one diagonal with rows [r0, end), by all warps of the CTA:
+// split parts of the first two rows of every lane group before the wait,
+// their finishing parts (lanes 0 and 1 of a group side by side) and any
+// further rows whole after it.
+struct DecodeRows {
+    DecodePart c[2];
+};
+
+template <int KLO, int KHI>
+__device__ __forceinline__ DecodeRows decode_rows_split(const float* __restrict__ pair, const float* erow,
+                                                        const float* ecol, int L, float alpha, int d, int r0,
+                                                        int end)
+{
+    DecodeRows p;
+    const int G = group_width(d - 1), gpb = blockDim.x / G;
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const int i = r0 + g + it * gpb;
+        p.c[it] = decode_split_t<KLO, KHI>(pair, erow, ecol, L, alpha, i, d, i < end, lane, G);
+    }
+    return p;
+}
+
+template <int KLO, int KHI>
+__device__ __forceinline__ void decode_rows_finish(const float* __restrict__ single, const float* __restrict__ pair,
+                                                   float* erow, float* ecol, int* scol, int L, float alpha, int d,
+                                                   int r0, int end, const DecodeRows& p)
+{
+    const int G = group_width(d - 1), gpb = blockDim.x / G;
+    const int lane = threadIdx.x & (G - 1), g = threadIdx.x / G;
+    if (G >= 2) {
+        const int it = lane & 1;
+        const int i = r0 + g + it * gpb;
+        decode_finish_t<KLO, KHI>(single, pair, erow, ecol, scol, L, alpha, i, d, lane < 2 && i < end,
+                                  it ? p.c[1] : p.c[0]);
+    } else {
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+            const int i = r0 + g + it * gpb;
+            decode_finish_t<KLO, KHI>(single, pair, erow, ecol, scol, L, alpha, i, d, i < end, p.c[it]);
+        }
+    }
+    for (int base = r0 + 2 * gpb; base < end; base += gpb) {
+        const int i = base + g;
+        const DecodePart c = decode_split_t<KLO, KHI>(pair, erow, ecol, L, alpha, i, d, i < end, lane, G);
+        decode_finish_t<KLO, KHI>(single, pair, erow, ecol, scol, L, alpha, i, d, i < end && lane == 0, c);
+    }
+}
+
+// All diagonals, two per grid barrier.  CTA b owns rows [b*R, (b+1)*R) of
+// every diagonal (R = ceil(L / CTAs)); for the pair (dA, dB) it computes dA
+// for its rows plus row (b+1)*R (which the next CTA also computes, to the
+// same bits) and then, after a CTA barrier, dB, whose e1 reads dA at row
+// i+1, its own.
 __global__ void __launch_bounds__(kWaveMaxThreads) decode_wave_kernel(const float* __restrict__ single,
                                                           const float* __restrict__ pair, int L, float alpha,
                                                           float* __restrict__ erow, float* __restrict__ ecol,
@@ -147,22 +217,18 @@ __global__ void __launch_bounds__(kWaveMaxThreads) decode_wave_kernel(const floa
 {
     unsigned int gen = 0;
     grid_arrive(sync);  // spans 0 and -1 are the zero-filled tables
-    for (int d = 1; d < L; d++) {
-        const int G = group_width(d - 1);
-        const int gpb = blockDim.x / G;
-        const int total = gridDim.x * gpb;
-        const int lane = threadIdx.x & (G - 1);
-        const int gid0 = blockIdx.x * gpb + threadIdx.x / G;
-        const int ncell = L - d;
-        const DecodePart p0 = decode_cell_split(pair, erow, ecol, L, alpha, gid0, d, gid0 < ncell, lane, G);
+    const int rows = (L + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * rows;
+    for (int dA = 1; dA < L; dA += 2) {
+        const int dB = dA + 1;
+        const int endA = min(r0 + rows + 1, L - dA);
+        const int endB = (dB < L) ? min(r0 + rows, L - dB) : r0;
+        const DecodeRows pa = decode_rows_split<2, 1>(pair, erow, ecol, L, alpha, dA, r0, endA);
+        const DecodeRows pb = decode_rows_split<3, 2>(pair, erow, ecol, L, alpha, dB, r0, endB);
         if (!grid_wait(sync, gen)) return;
-        decode_cell_finish(single, erow, ecol, scol, L, gid0, d, gid0 < ncell, lane, p0);
-        for (int base = total; base < ncell; base += total) {
-            const int i = base + gid0;
-            const bool valid = i < ncell;
-            const DecodePart p = decode_cell_split(pair, erow, ecol, L, alpha, i, d, valid, lane, G);
-            decode_cell_finish(single, erow, ecol, scol, L, i, d, valid, lane, p);
-        }
+        decode_rows_finish<2, 1>(single, pair, erow, ecol, scol, L, alpha, dA, r0, endA, pa);
+        __syncthreads();  // diagonal dA of this CTA's rows before dB reads it
+        decode_rows_finish<3, 2>(single, pair, erow, ecol, scol, L, alpha, dB, r0, endB, pb);
         grid_arrive(sync);
     }
 }
@@ -409,12 +475,11 @@ int run_posterior_decoding(messi_ctx* ctx, int L, const double* d_single, const 
         const float a = (float)alpha;
         int Lv = L;
         void* args[] = {(void*)&f_single, (void*)&f_pair, &Lv, (void*)&a, &erow, &ecol, &d_scol, &d_sync};
-        const int threads = wave_threads(ctx, 0.5 * (double)L * L);
-        const int grid = wave_grid(ctx, (const void*)decode_wave_kernel, L, threads);
-        e = cudaLaunchCooperativeKernel((const void*)decode_wave_kernel, dim3(grid), dim3(threads), args, 0,
-                                        ctx->stream);
-        ctx->launches++;
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "decode_wave_kernel");
+        // paired shape: a CTA's two diagonals of a pair (2 x rows + 1 cells)
+        // in one pass of its warps where the CTA can grow to hold them
+        const int rc = launch_wave(ctx, (const void*)decode_wave_kernel, args, d_sync, L, 0.5 * (double)L * L,
+                                   "decode_wave_kernel", 2);
+        if (rc) return rc;
     }
     if (d_paired) {
         decode_traceback_kernel<<<1, 32, 0, ctx->stream>>>(d_scol, L, d_paired, d_stack);

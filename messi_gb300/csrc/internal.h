@@ -433,5 +433,10 @@ void tune_end(messi_ctx* ctx, const void* key, int C);
 void tune_forget(messi_ctx* ctx, const void* key);
 // Queue a copy of the wavefront barrier status into ctx->status_host.
 int queue_status_readback(messi_ctx* ctx, const Band& t);
+// Cooperative launch of a persistent wavefront kernel (scfg.cu): resets the
+// barrier words, picks the CTA size and grid; share > 0 for kernels that own
+// rows of diagonal pairs (warps per row and pair).
+int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L, double band_cells,
+                const char* what, int share = 0, const void* halves_kernel = nullptr);
 
 }  // namespace messi

@@ -1672,8 +1672,8 @@ static int ctas_for_rows(int L, int warps) { return (warps > 1) ? (L + warps - 2
 // columns than 256- or 512-thread CTAs of the plain kernel); the grid then
 // grows (up to one CTA per SM) until the rows fit, or else fit one per warp
 // of the whole CTA.
-static int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L,
-                       double band_cells, const char* what, int share = 0, const void* halves_kernel = nullptr)
+int launch_wave(messi_ctx* ctx, const void* kernel, void** args, unsigned int* sync, int L, double band_cells,
+                const char* what, int share, const void* halves_kernel)
 {
     int threads = wave_threads(ctx, band_cells);
     cudaError_t e = cudaMemsetAsync(sync, 0, kSyncWords * sizeof(unsigned int), ctx->stream);
