@@ -77,9 +77,8 @@ __device__ __forceinline__ void lse_add4(float& m, float& s, float x0, float x1,
 // -inf terms adds exact zeros), so lanes of a warp never diverge here.
 __device__ __forceinline__ void lse_add8(float& m, float& s, const float (&x)[8])
 {
-    float mx = x[0];
-#pragma unroll
-    for (int q = 1; q < 8; q++) mx = fmaxf(mx, x[q]);
+    // the maximum as a tree (three dependent steps instead of seven; exact)
+    const float mx = fmaxf(fmaxf(fmaxf(x[0], x[1]), fmaxf(x[2], x[3])), fmaxf(fmaxf(x[4], x[5]), fmaxf(x[6], x[7])));
     const float nm = fmaxf(m, mx);
     const float base = (nm == -INFINITY) ? 0.f : nm;
     s *= __expf(m - base);
