@@ -62,6 +62,27 @@ def test_posterior_decoding_equals_reference_kernel(api, L):
     np.testing.assert_array_equal(s_o, s_ref)
 
 
+@pytest.mark.parametrize("env", [{"MESSI_WAVE_CTAS": "7"}, {"MESSI_WAVE_CTAS": "1"}, {"MESSI_WAVE_THREADS": "1024"}])
+def test_posterior_decoding_same_bits_on_any_grid(api, env, monkeypatch):
+    """The decoding wavefront takes two diagonals per grid barrier, each CTA
+    owning a run of rows (and one more on the pair's first diagonal): with 7
+    CTAs or one (rows beyond two per lane group computed whole) or 1,024-
+    thread CTAs, e and s equal the oracle's to the bit."""
+    L, W = 150, 149
+    u, p = _scores(L, W, seed=11)
+    single, pair = _posteriors(u, p)
+    e_ref, s_ref = co.posterior_decoding(single, pair, 2.0)
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    ctx = api.Context(0)
+    try:
+        e, s = api.computeposteriordecodingcuda(single, pair, 2.0, ctx=ctx)
+    finally:
+        ctx.close()
+    np.testing.assert_array_equal(e, e_ref.astype(np.float64))
+    np.testing.assert_array_equal(s, s_ref)
+
+
 def _check_structure(row, W):
     L = len(row)
     stack = []
