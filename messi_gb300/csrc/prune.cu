@@ -156,10 +156,23 @@ __global__ void __launch_bounds__(256) leaf_msg_kernel(const float* __restrict__
     if (r >= R) return;
     (void)C;
     const float* p = P + ((size_t)(c0 + cc) * numnodes + __ldg(rownode + r)) * 256 + a * 16;
-    const float* x = rows + r * 16;
+    const float4* x4 = reinterpret_cast<const float4*>(rows + r * 16);
+    float x[16];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float4 v = __ldg(x4 + q);
+        x[4 * q] = v.x;
+        x[4 * q + 1] = v.y;
+        x[4 * q + 2] = v.z;
+        x[4 * q + 3] = v.w;
+    }
+    // an observed base pair is one nonzero state: its zero terms are skipped
+    // (adding +0.0 would leave the sum as it is), the same branch for the 16
+    // threads of the row
     double s = 0.0;
 #pragma unroll
-    for (int d = 0; d < 16; d++) s += (double)__ldg(p + d) * (double)__ldg(x + d);
+    for (int d = 0; d < 16; d++)
+        if (x[d] != 0.f) s += (double)__ldg(p + d) * (double)x[d];
     out[((size_t)cc * R + r) * 16 + a] = (float)s;
 }
 
