@@ -104,6 +104,14 @@ const char* messi_ctx_last_error(messi_ctx* ctx);
  * mechanism works); the call itself returns MESSI_OK and leaves the context
  * usable. */
 int messi_selftest_bounded_wait(messi_ctx* ctx, int32_t* status);
+/* The host eigensystem behind P = exp(Qt) (no counterpart in the reference,
+ * which diagonalises Q in Julia, src/FARCE.jl:410-433): Q (n x n row-major,
+ * n <= 16) reversible with respect to pi > 0; on return w[n] are the
+ * eigenvalues and U[n * n] (row-major, column p = eigenvector p) the
+ * orthonormal eigenvectors of D^1/2 Q D^-1/2, D = diag(pi).  Host only: needs
+ * no context and no GPU.  MESSI_EINVAL for n outside 1..16, a pi entry that is
+ * not positive, a non-finite entry or no convergence. */
+int messi_host_reversible_eig(int32_t n, const double* Q, const double* pi, double* w, double* U);
 
 /* Per-kernel timing (instrumentation; no counterpart in the reference).
  * enable != 0 records a CUDA event pair around each launch of the timed

@@ -564,6 +564,12 @@ int messi_selftest_bounded_wait(messi_ctx* ctx, int32_t* status)
     return MESSI_OK;
 }
 
+int messi_host_reversible_eig(int32_t n, const double* Q, const double* pi, double* w, double* U)
+{
+    if (n < 1 || n > 16 || !Q || !pi || !w || !U) return MESSI_EINVAL;
+    return host_reversible_eig(n, Q, pi, w, U);
+}
+
 int messi_ctx_launch_shapes(messi_ctx* ctx, int32_t* prune_shape, int32_t* wave_threads, int32_t* tuned)
 {
     if (!ctx) return MESSI_EINVAL;
