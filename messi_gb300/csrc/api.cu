@@ -478,7 +478,7 @@ int messi_ctx_create(int device, messi_ctx** out)
         const char* ps = std::getenv("MESSI_PRUNE_SHAPE");
         if (ps) {
             const int v = std::atoi(ps);
-            ctx->prune_shape = (v >= 0 && v <= 2) ? v : 0;
+            ctx->prune_shape = (v >= 0 && v <= 3) ? v : 0;
             ctx->fixed_prune = true;
         }
         const char* at = std::getenv("MESSI_AUTOTUNE");

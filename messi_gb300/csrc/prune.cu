@@ -494,6 +494,294 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------
+// tcgen05 form of the interior node update (launch shape 3, chosen only on
+// request: MESSI_PRUNE_SHAPE=3).  The CTA's 128 unique pairs of one node are
+// the M = 128 rows of one tcgen05.mma (kind::tf32, N = 16 states, K = 8):
+//   * the child rows are gathered with cp.async as in prune_msg_kernel, into
+//     a [side][state quad][pair] stage, so that thread p reads pair p's rows
+//     with conflict-free 16-byte loads;
+//   * thread p forms x = m_left * m_right, splits it into TF32 hi and lo and
+//     writes both to its own TMEM lane (tcgen05.st): the A operand comes from
+//     tensor memory, not through shared memory;
+//   * the node's branch matrix P (B operand, N x K, K-major) is split into hi
+//     and lo by the CTA and written to shared memory in the canonical
+//     no-swizzle layout: core matrices of 8 rows x 16 bytes, the two 8-row
+//     groups of N 128 bytes apart (SBO), the two 4-wide K groups of one MMA
+//     256 bytes apart (LBO);
+//   * one thread issues, per K half, lo*hi, hi*lo, hi*hi into that half's
+//     own accumulator (TMEM columns 32..47 and 48..63), the same split and
+//     order as prune_msg_kernel (K half 0 = states {0,1,4,5,8,9,12,13}), and
+//     commits them to an mbarrier;
+//   * thread p reads its pair's 2 x 16 accumulators back (tcgen05.ld), adds
+//     the halves and half an ulp as prune_msg_kernel does, rescales by a power
+//     of two and stores the row.
+// TMEM: 64 columns per CTA (A hi 0..15, A lo 16..31, D 32..63); at most 6
+// CTAs of this kernel fit on an SM by shared memory (36 KB each), 384 columns.  A wait on
+// the mbarrier that gives up (bounded) writes NaN rows, so the likelihood
+// that uses them is NaN, and the CTA still frees its TMEM before it returns.
+// ---------------------------------------------------------------------------
+namespace tc {
+constexpr int kStages = 2;
+constexpr unsigned kCols = 64;
+constexpr unsigned kColAhi = 0, kColAlo = 16, kColD = 32;
+
+struct Stage {
+    float4 x[2][4][kTile];  // [side][state quad q: states 4q..4q+3][pair]
+    int e[2][kTile];
+};
+
+struct Smem {
+    Stage st[kStages];
+    float bhi[256];  // P hi, canonical K-major layout (boff below)
+    float blo[256];
+    unsigned long long mbar;
+    unsigned tmem_base;
+    int fail;
+};
+
+// Contraction index of column c (0..7) of K half ks: d = 4(c/2) + 2ks + c%2.
+__host__ __device__ constexpr int kidx(int ks, int c) { return 4 * (c >> 1) + 2 * ks + (c & 1); }
+
+// Float offset of P[i][d] in the B buffer: K half ks = (d/2)%2 at 128 floats,
+// column c = 2(d/4) + d%2 of that half; core matrix (row group i/8, K group
+// c/4) at (c/4)*64 + (i/8)*32 floats, row i%8 at 4 floats, element c%4.
+__host__ __device__ constexpr int boff(int i, int d)
+{
+    return ((d >> 1) & 1) * 128 + (((2 * (d >> 2) + (d & 1)) >> 2) * 64) + (i >> 3) * 32 + (i & 7) * 4 +
+           ((2 * (d >> 2) + (d & 1)) & 3);
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, no swizzle: start, LBO, SBO in 16-byte
+// units; bit 46 = descriptor version 1.
+__device__ __forceinline__ unsigned long long bdesc(unsigned addr)
+{
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)(256u >> 4) << 16) |
+           ((unsigned long long)(128u >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::tf32: D F32 (bits 4-5 = 1), A and B TF32
+// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+constexpr unsigned kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_ts(unsigned d, unsigned a, unsigned long long b, unsigned acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d),
+        "r"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+
+__device__ __forceinline__ void st16(unsigned taddr, const uint32_t (&v)[16])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
+            taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]));
+}
+
+__device__ __forceinline__ void ld32(unsigned taddr, uint32_t (&v)[32])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// Bounded wait for phase `parity` of the mbarrier; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned parity)
+{
+    for (int it = 0; it < (1 << 16); it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+}  // namespace tc
+
+__global__ void __launch_bounds__(kTile, 4) prune_tc_kernel(const NodeDev* __restrict__ nodes,
+                                                           const int2* __restrict__ tiles,
+                                                           const float* __restrict__ P, int numnodes, int c0, int nc)
+{
+    extern __shared__ float4 smem_raw[];
+    tc::Smem& S = *reinterpret_cast<tc::Smem*>(smem_raw);
+    const int2 tile = tiles[blockIdx.x];
+    const NodeDev& nd = nodes[tile.x];
+    const int n = nd.n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const unsigned mbar = tc::smem_u32(&S.mbar);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         tc::smem_u32(&S.tmem_base)),
+                     "r"(tc::kCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        S.fail = 0;
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const unsigned tbase = S.tmem_base;
+    const unsigned tlane = tbase + ((unsigned)(32 * warp) << 16);  // this warp's 32 TMEM lanes
+
+    // gathers: lane (g, t) copies state quad t of pairs g + 8k of its warp
+    const int wbase = 32 * warp;
+    int li[4], ri[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int u = tile.y + wbase + g + 8 * k;
+        const int uc = (u < n) ? u : (n - 1);
+        li[k] = __ldg(nd.li + uc);
+        ri[k] = __ldg(nd.ri + uc);
+    }
+    const int myl = li[0] * (t == 0) + li[1] * (t == 1) + li[2] * (t == 2) + li[3] * (t == 3);
+    const int myr = ri[0] * (t == 0) + ri[1] * (t == 1) + ri[2] * (t == 2) + ri[3] * (t == 3);
+    const float* lf = nd.lf;
+    const float* rf = nd.rf;
+    const int* le = nd.le;
+    const int* re = nd.re;
+    const long long lcs = nd.lcs, rcs = nd.rcs;
+    auto issue = [&](int cc) {
+        tc::Stage& st = S.st[cc % tc::kStages];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int pl = wbase + g + 8 * k;
+            cp_async16(&st.x[0][t][pl], lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
+            cp_async16(&st.x[1][t][pl], rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
+        }
+        if (le) cp_async4(&st.e[0][wbase + g + 8 * t], le + (size_t)cc * lcs + myl);
+        if (re) cp_async4(&st.e[1][wbase + g + 8 * t], re + (size_t)cc * rcs + myr);
+    };
+#pragma unroll
+    for (int s0 = 0; s0 < tc::kStages - 1; s0++) {
+        if (s0 < nc) issue(s0);
+        cp_async_commit();
+    }
+    const int myu = tile.y + tid;  // the pair this thread finishes
+    const bool myvalid = myu < n;
+    // this thread's two entries of P: row i, states d and d + 1
+    const int pi_ = (2 * tid) >> 4, pd = (2 * tid) & 15;
+    for (int cc = 0; cc < nc; cc++) {
+        if (cc + tc::kStages - 1 < nc) issue(cc + tc::kStages - 1);
+        cp_async_commit();
+        cp_async_wait<tc::kStages - 1>();
+        __syncwarp();
+        const tc::Stage& st = S.st[cc % tc::kStages];
+        float x[16];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float4 a = st.x[0][q][tid], b = st.x[1][q][tid];
+            x[4 * q] = a.x * b.x;
+            x[4 * q + 1] = a.y * b.y;
+            x[4 * q + 2] = a.z * b.z;
+            x[4 * q + 3] = a.w * b.w;
+        }
+        const int e = (le ? st.e[0][tid] : 0) + (re ? st.e[1][tid] : 0);
+        {
+            uint32_t hi[16], lo[16];
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++)
+#pragma unroll
+                for (int c = 0; c < 8; c++) split_a(x[tc::kidx(ks, c)], hi[8 * ks + c], lo[8 * ks + c]);
+            tc::st16(tlane + tc::kColAhi, hi);
+            tc::st16(tlane + tc::kColAlo, lo);
+        }
+        {
+            const float* pv = P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256;
+            const float2 pp = __ldg(reinterpret_cast<const float2*>(pv + 2 * tid));
+            uint32_t h0, l0, h1, l1;
+            split_a(pp.x, h0, l0);
+            split_a(pp.y, h1, l1);
+            const int o = tc::boff(pi_, pd);
+            *reinterpret_cast<float2*>(S.bhi + o) = make_float2(__uint_as_float(h0), __uint_as_float(h1));
+            *reinterpret_cast<float2*>(S.blo + o) = make_float2(__uint_as_float(l0), __uint_as_float(l1));
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        tc::fence_before();
+        __syncthreads();
+        if (*(volatile int*)&S.fail) break;  // a previous wait gave up (uniform: read after the barrier)
+        if (tid == 0) {
+            tc::fence_after();
+            const unsigned bh = tc::smem_u32(S.bhi), bl = tc::smem_u32(S.blo);
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++) {
+                const unsigned d = tbase + tc::kColD + 16 * ks;
+                const unsigned long long dh = tc::bdesc(bh + 512 * ks), dl = tc::bdesc(bl + 512 * ks);
+                tc::mma_ts(d, tbase + tc::kColAlo + 8 * ks, dh, 0u);
+                tc::mma_ts(d, tbase + tc::kColAhi + 8 * ks, dl, 1u);
+                tc::mma_ts(d, tbase + tc::kColAhi + 8 * ks, dh, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                         : "memory");
+        }
+        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(mbar, (unsigned)(cc & 1)));
+        tc::fence_after();
+        float V[16];
+        if (ok) {
+            uint32_t D[32];
+            tc::ld32(tlane + tc::kColD, D);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            // D[c] / D[16 + c]: K halves 0 and 1 of state c
+#pragma unroll
+            for (int c = 0; c < 16; c++) V[c] = add_half_ulp(__uint_as_float(D[c]) + __uint_as_float(D[16 + c]));
+        } else {
+#pragma unroll
+            for (int c = 0; c < 16; c++) V[c] = __int_as_float(0x7fc00000);
+            if (lane == 0) *(volatile int*)&S.fail = 1;
+        }
+        tc::fence_before();
+        float m = V[0];
+#pragma unroll
+        for (int c = 1; c < 16; c++) m = fmaxf(m, V[c]);
+        int ex;
+        float sc;
+        pow2_scale(m, ex, sc);
+        if (myvalid) {
+            float4* o = reinterpret_cast<float4*>(nd.of + ((size_t)cc * nd.ocs + myu) * 16);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                o[q] = make_float4(V[4 * q] * sc, V[4 * q + 1] * sc, V[4 * q + 2] * sc, V[4 * q + 3] * sc);
+            nd.oe[(size_t)cc * nd.ocs + myu] = e + ex;
+        }
+    }
+    cp_async_wait<0>();
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(tc::kCols));
+    }
+}
+
+static int launch_prune_tc(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, const float* d_P,
+                           int numnodes, int c0, int nc)
+{
+    prune_tc_kernel<<<nt, kTile, sizeof(tc::Smem), ctx->stream>>>(d_nodes, d_tiles, d_P, numnodes, c0, nc);
+    LAUNCH_CHECK(ctx, "prune_tc_kernel");
+    return MESSI_OK;
+}
+
 template <int STAGES, int MINB>
 static int launch_prune_shape(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_tiles, int nt, bool root,
                               const float* d_P, int numnodes, int c0, int nc, int C, const float* d_pi16,
@@ -525,7 +813,9 @@ int launch_prune_tiles(messi_ctx* ctx, const NodeDev* d_nodes, const int2* d_til
                        const double* d_logw, const int* d_lam, bool per_lambda)
 {
     if (nt <= 0) return MESSI_OK;
-    // shapes: 0 = 2 stages x 4 CTAs/SM, 1 = 3 stages x 3 CTAs, 2 = 2 stages x 3 CTAs
+    // shapes: 0 = 2 stages x 4 CTAs/SM, 1 = 3 stages x 3 CTAs, 2 = 2 stages x 3 CTAs (the autotuner's
+    // candidates); 3 = interior levels in the tcgen05 form, the roots as shape 0 (on request only)
+    if (ctx->prune_shape == 3 && !root) return launch_prune_tc(ctx, d_nodes, d_tiles, nt, d_P, numnodes, c0, nc);
     switch (ctx->prune_shape) {
         case 1: return launch_prune_shape<3, 3>(ctx, d_nodes, d_tiles, nt, root, d_P, numnodes, c0, nc, C, d_pi16,
                                                 d_logw, d_lam, per_lambda);
