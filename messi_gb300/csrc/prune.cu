@@ -499,8 +499,9 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
 // request: MESSI_PRUNE_SHAPE=3).  The CTA's 128 unique pairs of one node are
 // the M = 128 rows of one tcgen05.mma (kind::tf32, N = 16 states, K = 8):
 //   * the child rows are gathered with cp.async as in prune_msg_kernel, into
-//     a [side][state quad][pair] stage, so that thread p reads pair p's rows
-//     with conflict-free 16-byte loads;
+//     a stage of whole rows with XOR-ordered quads (Stage), so that both the
+//     gathers and thread p's reads of pair p's rows are free of bank
+//     conflicts;
 //   * thread p forms x = m_left * m_right, splits it into TF32 hi and lo and
 //     writes both to its own TMEM lane (tcgen05.st): the A operand comes from
 //     tensor memory, not through shared memory;
@@ -526,10 +527,16 @@ constexpr int kStages = 2;
 constexpr unsigned kCols = 64;
 constexpr unsigned kColAhi = 0, kColAlo = 16, kColD = 32;
 
+// A stage holds each pair's two child rows whole (64 bytes each: the four
+// 16-byte copies of one row land side by side, as the gather delivers them),
+// with the quads of row p in XOR order q ^ ((p / 2) % 4), so that thread p's
+// load of quad q from 32 consecutive rows touches every bank once per
+// 128 bytes.
 struct Stage {
-    float4 x[2][4][kTile];  // [side][state quad q: states 4q..4q+3][pair]
+    float4 x[2][kTile][4];  // [side][pair][quad position]
     int e[2][kTile];
 };
+__device__ __forceinline__ int qpos(int p, int q) { return q ^ ((p >> 1) & 3); }
 
 struct Smem {
     Stage st[kStages];
@@ -614,7 +621,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned parity)
 }
 }  // namespace tc
 
-__global__ void __launch_bounds__(kTile, 4) prune_tc_kernel(const NodeDev* __restrict__ nodes,
+__global__ void __launch_bounds__(kTile, 6) prune_tc_kernel(const NodeDev* __restrict__ nodes,
                                                            const int2* __restrict__ tiles,
                                                            const float* __restrict__ P, int numnodes, int c0, int nc)
 {
@@ -666,8 +673,8 @@ __global__ void __launch_bounds__(kTile, 4) prune_tc_kernel(const NodeDev* __res
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int pl = wbase + g + 8 * k;
-            cp_async16(&st.x[0][t][pl], lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
-            cp_async16(&st.x[1][t][pl], rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
+            cp_async16(&st.x[0][pl][tc::qpos(pl, t)], lf + ((size_t)cc * lcs + li[k]) * 16 + 4 * t);
+            cp_async16(&st.x[1][pl][tc::qpos(pl, t)], rf + ((size_t)cc * rcs + ri[k]) * 16 + 4 * t);
         }
         if (le) cp_async4(&st.e[0][wbase + g + 8 * t], le + (size_t)cc * lcs + myl);
         if (re) cp_async4(&st.e[1][wbase + g + 8 * t], re + (size_t)cc * rcs + myr);
@@ -690,7 +697,7 @@ __global__ void __launch_bounds__(kTile, 4) prune_tc_kernel(const NodeDev* __res
         float x[16];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const float4 a = st.x[0][q][tid], b = st.x[1][q][tid];
+            const float4 a = st.x[0][tid][tc::qpos(tid, q)], b = st.x[1][tid][tc::qpos(tid, q)];
             x[4 * q] = a.x * b.x;
             x[4 * q + 1] = a.y * b.y;
             x[4 * q + 2] = a.z * b.z;
@@ -758,10 +765,15 @@ __global__ void __launch_bounds__(kTile, 4) prune_tc_kernel(const NodeDev* __res
         float sc;
         pow2_scale(m, ex, sc);
         if (myvalid) {
-            float4* o = reinterpret_cast<float4*>(nd.of + ((size_t)cc * nd.ocs + myu) * 16);
+            // the row as two 32-byte stores: whole sectors
+            float* o = nd.of + ((size_t)cc * nd.ocs + myu) * 16;
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                o[q] = make_float4(V[4 * q] * sc, V[4 * q + 1] * sc, V[4 * q + 2] * sc, V[4 * q + 3] * sc);
+            for (int h = 0; h < 2; h++)
+                asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"l"(o + 8 * h),
+                             "f"(V[8 * h] * sc), "f"(V[8 * h + 1] * sc), "f"(V[8 * h + 2] * sc),
+                             "f"(V[8 * h + 3] * sc), "f"(V[8 * h + 4] * sc), "f"(V[8 * h + 5] * sc),
+                             "f"(V[8 * h + 6] * sc), "f"(V[8 * h + 7] * sc)
+                             : "memory");
             nd.oe[(size_t)cc * nd.ocs + myu] = e + ex;
         }
     }
