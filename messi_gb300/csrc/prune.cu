@@ -516,7 +516,9 @@ __global__ void __launch_bounds__(kTile, MINB) prune_msg_kernel(
 //     commits them to an mbarrier;
 //   * thread p reads its pair's 2 x 16 accumulators back (tcgen05.ld), adds
 //     the halves and half an ulp as prune_msg_kernel does, rescales by a power
-//     of two and stores the row.
+//     of two and stores the row -- one category late: the MMAs of category c
+//     run while the CTA waits for and multiplies the rows of category c + 1,
+//     and P is loaded one category ahead.
 // TMEM: 64 columns per CTA (A hi 0..15, A lo 16..31, D 32..63); at most 6
 // CTAs of this kernel fit on an SM by shared memory (36 KB each), 384 columns.  A wait on
 // the mbarrier that gives up (bounded) writes NaN rows, so the likelihood
@@ -686,63 +688,20 @@ __global__ void __launch_bounds__(kTile, 6) prune_tc_kernel(const NodeDev* __res
     }
     const int myu = tile.y + tid;  // the pair this thread finishes
     const bool myvalid = myu < n;
-    // this thread's two entries of P: row i, states d and d + 1
-    const int pi_ = (2 * tid) >> 4, pd = (2 * tid) & 15;
-    for (int cc = 0; cc < nc; cc++) {
-        if (cc + tc::kStages - 1 < nc) issue(cc + tc::kStages - 1);
-        cp_async_commit();
-        cp_async_wait<tc::kStages - 1>();
-        __syncwarp();
-        const tc::Stage& st = S.st[cc % tc::kStages];
-        float x[16];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const float4 a = st.x[0][tid][tc::qpos(tid, q)], b = st.x[1][tid][tc::qpos(tid, q)];
-            x[4 * q] = a.x * b.x;
-            x[4 * q + 1] = a.y * b.y;
-            x[4 * q + 2] = a.z * b.z;
-            x[4 * q + 3] = a.w * b.w;
-        }
-        const int e = (le ? st.e[0][tid] : 0) + (re ? st.e[1][tid] : 0);
-        {
-            uint32_t hi[16], lo[16];
-#pragma unroll
-            for (int ks = 0; ks < 2; ks++)
-#pragma unroll
-                for (int c = 0; c < 8; c++) split_a(x[tc::kidx(ks, c)], hi[8 * ks + c], lo[8 * ks + c]);
-            tc::st16(tlane + tc::kColAhi, hi);
-            tc::st16(tlane + tc::kColAlo, lo);
-        }
-        {
-            const float* pv = P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256;
-            const float2 pp = __ldg(reinterpret_cast<const float2*>(pv + 2 * tid));
-            uint32_t h0, l0, h1, l1;
-            split_a(pp.x, h0, l0);
-            split_a(pp.y, h1, l1);
-            const int o = tc::boff(pi_, pd);
-            *reinterpret_cast<float2*>(S.bhi + o) = make_float2(__uint_as_float(h0), __uint_as_float(h1));
-            *reinterpret_cast<float2*>(S.blo + o) = make_float2(__uint_as_float(l0), __uint_as_float(l1));
-        }
-        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        tc::fence_before();
-        __syncthreads();
-        if (*(volatile int*)&S.fail) break;  // a previous wait gave up (uniform: read after the barrier)
-        if (tid == 0) {
-            tc::fence_after();
-            const unsigned bh = tc::smem_u32(S.bhi), bl = tc::smem_u32(S.blo);
-#pragma unroll
-            for (int ks = 0; ks < 2; ks++) {
-                const unsigned d = tbase + tc::kColD + 16 * ks;
-                const unsigned long long dh = tc::bdesc(bh + 512 * ks), dl = tc::bdesc(bl + 512 * ks);
-                tc::mma_ts(d, tbase + tc::kColAlo + 8 * ks, dh, 0u);
-                tc::mma_ts(d, tbase + tc::kColAhi + 8 * ks, dl, 1u);
-                tc::mma_ts(d, tbase + tc::kColAhi + 8 * ks, dh, 1u);
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
-                         : "memory");
-        }
-        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(mbar, (unsigned)(cc & 1)));
+    // this thread's two B entries, in layout order (floats 2 tid and 2 tid + 1
+    // of the buffer, the inverse of boff, so the stores are conflict-free): row
+    // pi_ of P, states pd and pd + 1
+    const int bo = 2 * tid, brem = bo & 127;
+    const int pi_ = (((brem >> 5) & 1) << 3) | ((brem >> 2) & 7);
+    const int pd = tc::kidx(bo >> 7, ((brem >> 6) << 2) | (brem & 3));
+    auto pload = [&](int cc) {
+        return __ldg(reinterpret_cast<const float2*>(P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256 + pi_ * 16 +
+                                                     pd));
+    };
+    // category cf's accumulators back from TMEM (its MMAs ran while the next
+    // category's rows were read), rescaled and stored with exponent ef
+    auto finish = [&](int cf, int ef) {
+        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(mbar, (unsigned)(cf & 1)));
         tc::fence_after();
         float V[16];
         if (ok) {
@@ -766,7 +725,7 @@ __global__ void __launch_bounds__(kTile, 6) prune_tc_kernel(const NodeDev* __res
         pow2_scale(m, ex, sc);
         if (myvalid) {
             // the row as two 32-byte stores: whole sectors
-            float* o = nd.of + ((size_t)cc * nd.ocs + myu) * 16;
+            float* o = nd.of + ((size_t)cf * nd.ocs + myu) * 16;
 #pragma unroll
             for (int h = 0; h < 2; h++)
                 asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"l"(o + 8 * h),
@@ -774,9 +733,70 @@ __global__ void __launch_bounds__(kTile, 6) prune_tc_kernel(const NodeDev* __res
                              "f"(V[8 * h + 3] * sc), "f"(V[8 * h + 4] * sc), "f"(V[8 * h + 5] * sc),
                              "f"(V[8 * h + 6] * sc), "f"(V[8 * h + 7] * sc)
                              : "memory");
-            nd.oe[(size_t)cc * nd.ocs + myu] = e + ex;
+            nd.oe[(size_t)cf * nd.ocs + myu] = ef + ex;
         }
+    };
+    float2 ppn = (nc > 0) ? pload(0) : make_float2(0.f, 0.f);
+    int eprev = 0;
+    for (int cc = 0; cc < nc; cc++) {
+        if (cc + tc::kStages - 1 < nc) issue(cc + tc::kStages - 1);
+        cp_async_commit();
+        cp_async_wait<tc::kStages - 1>();
+        __syncwarp();
+        const float2 pp = ppn;
+        if (cc + 1 < nc) ppn = pload(cc + 1);
+        const tc::Stage& st = S.st[cc % tc::kStages];
+        float x[16];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float4 a = st.x[0][tid][tc::qpos(tid, q)], b = st.x[1][tid][tc::qpos(tid, q)];
+            x[4 * q] = a.x * b.x;
+            x[4 * q + 1] = a.y * b.y;
+            x[4 * q + 2] = a.z * b.z;
+            x[4 * q + 3] = a.w * b.w;
+        }
+        const int e = (le ? st.e[0][tid] : 0) + (re ? st.e[1][tid] : 0);
+        // the previous category's MMAs are done with A, B and D after this
+        if (cc > 0) finish(cc - 1, eprev);
+        {
+            uint32_t hi[16], lo[16];
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++)
+#pragma unroll
+                for (int c = 0; c < 8; c++) split_a(x[tc::kidx(ks, c)], hi[8 * ks + c], lo[8 * ks + c]);
+            tc::st16(tlane + tc::kColAhi, hi);
+            tc::st16(tlane + tc::kColAlo, lo);
+        }
+        {
+            uint32_t h0, l0, h1, l1;
+            split_a(pp.x, h0, l0);
+            split_a(pp.y, h1, l1);
+            *reinterpret_cast<float2*>(S.bhi + bo) = make_float2(__uint_as_float(h0), __uint_as_float(h1));
+            *reinterpret_cast<float2*>(S.blo + bo) = make_float2(__uint_as_float(l0), __uint_as_float(l1));
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        tc::fence_before();
+        __syncthreads();
+        if (*(volatile int*)&S.fail) break;  // a wait gave up (uniform: read after the barrier)
+        if (tid == 0) {
+            tc::fence_after();
+            const unsigned bh = tc::smem_u32(S.bhi), bl = tc::smem_u32(S.blo);
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++) {
+                const unsigned d = tbase + tc::kColD + 16 * ks;
+                const unsigned long long dh = tc::bdesc(bh + 512 * ks), dl = tc::bdesc(bl + 512 * ks);
+                tc::mma_ts(d, tbase + tc::kColAlo + 8 * ks, dh, 0u);
+                tc::mma_ts(d, tbase + tc::kColAhi + 8 * ks, dl, 1u);
+                tc::mma_ts(d, tbase + tc::kColAhi + 8 * ks, dh, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                         : "memory");
+        }
+        eprev = e;
     }
+    // S.fail is uniform here: last written before the final loop barrier
+    if (nc > 0 && !*(volatile int*)&S.fail) finish(nc - 1, eprev);
     cp_async_wait<0>();
     tc::fence_before();
     __syncthreads();
