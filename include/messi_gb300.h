@@ -88,7 +88,8 @@ int messi_ctx_last_launches(messi_ctx* ctx, int64_t* launches);
 int messi_ctx_graph_replays(messi_ctx* ctx, int64_t* replays);
 /* Launch shapes of the last likelihood evaluation (no counterpart in the
  * reference): the pruning pipeline shape (0 = 2 stages x 4 CTAs per SM,
- * 1 = 3 x 3, 2 = 2 x 3) and the wavefront CTA size (0 = chosen by band size),
+ * 1 = 3 x 3, 2 = 2 x 3; 3 = the interior levels in the tcgen05 form, chosen
+ * only by MESSI_PRUNE_SHAPE=3) and the wavefront CTA size (0 = chosen by band size),
  * and how many workloads have finished autotuning.  The first four
  * evaluations of a dataset (or batch) at a category count try candidate
  * shapes, timed with CUDA events, and later ones use the fastest
