@@ -561,6 +561,26 @@ __host__ __device__ constexpr int boff(int i, int d)
            ((2 * (d >> 2) + (d & 1)) & 3);
 }
 
+// Row and state of P held at float o (even) of the B buffer: the inverse of
+// boff, so that a thread storing floats o and o + 1 reads P[row][d..d+1].
+__host__ __device__ constexpr int brow(int o) { return (((o & 127) >> 5 & 1) << 3) | (((o & 127) >> 2) & 7); }
+__host__ __device__ constexpr int bstate(int o) { return kidx(o >> 7, (((o & 127) >> 6) << 2) | (o & 3)); }
+
+constexpr bool b_layout_ok()
+{
+    bool seen[256] = {};
+    for (int i = 0; i < 16; i++)
+        for (int d = 0; d < 16; d++) {
+            const int o = boff(i, d);
+            if (o < 0 || o >= 256 || seen[o]) return false;
+            seen[o] = true;
+        }
+    for (int o = 0; o < 256; o += 2)
+        if ((bstate(o) & 1) || boff(brow(o), bstate(o)) != o || boff(brow(o), bstate(o) + 1) != o + 1) return false;
+    return true;
+}
+static_assert(b_layout_ok(), "B operand layout: boff must be a bijection and brow/bstate its inverse");
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 // Shared-memory matrix descriptor, no swizzle: start, LBO, SBO in 16-byte
@@ -691,9 +711,8 @@ __global__ void __launch_bounds__(kTile, 6) prune_tc_kernel(const NodeDev* __res
     // this thread's two B entries, in layout order (floats 2 tid and 2 tid + 1
     // of the buffer, the inverse of boff, so the stores are conflict-free): row
     // pi_ of P, states pd and pd + 1
-    const int bo = 2 * tid, brem = bo & 127;
-    const int pi_ = (((brem >> 5) & 1) << 3) | ((brem >> 2) & 7);
-    const int pd = tc::kidx(bo >> 7, ((brem >> 6) << 2) | (brem & 3));
+    const int bo = 2 * tid;
+    const int pi_ = tc::brow(bo), pd = tc::bstate(bo);
     auto pload = [&](int cc) {
         return __ldg(reinterpret_cast<const float2*>(P + ((size_t)(c0 + cc) * numnodes + nd.self) * 256 + pi_ * 16 +
                                                      pd));
