@@ -23,7 +23,10 @@
 //     as an int), which computes the same likelihood as the reference's
 //     divide-by-max (felsenstein.cu:193-198);
 //   * the root variant folds sumfinal and the category log-sum-exp into the
-//     same pass (FP64 log-likelihood reduction).
+//     same pass (FP64 log-likelihood reduction);
+//   * prune_tc_kernel: the interior update as tcgen05.mma (A in tensor
+//     memory, P in shared memory, accumulators in tensor memory), the same
+//     bits as prune_msg_kernel; chosen only on request (launch shape 3).
 // unpaired_site_kernel + unpaired_mix_kernel restate
 // computeunpairedlikelihoodscat (src/FARCE.jl:742-773) in FP64 with the CPU
 // rescaling rule.
