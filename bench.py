@@ -544,10 +544,13 @@ def run_mcmc(args):
     (mp, sp), (ml, sl) = means["plain"], means["learned"]
     z = np.abs(mp - ml) / np.sqrt(sp ** 2 + sl ** 2)
     ratio = out["learned"]["median_ess_per_s"] / out["plain"]["median_ess_per_s"]
+    per_param = (np.array(out["learned"]["ess_per_s"]) / np.array(out["plain"]["ess_per_s"])).tolist()
     line = {"metric": "MCMC ESS/s learned vs plain proposal", "value": ratio, "unit": "x (median over parameters)",
             "higher_is_better": True, "n_gpus": 1, "iterations": n, "burnin": burn, "data": "synthetic",
             "config": {"workload": WORKLOAD_TEXT[args.workload] + ", 45 categories", "parameters": list(mcmc.FREE)},
             "plain": out["plain"], "learned": out["learned"],
+            "per_parameter_ratio": per_param, "min_per_parameter_ratio": float(min(per_param)),
+            "worst_parameter_ratio": out["learned"]["min_ess_per_s"] / out["plain"]["min_ess_per_s"],
             "posterior_mean_agreement_z": z.tolist(), "max_z": float(z.max()),
             "within_2_mcse": bool(np.all(z <= 2.0 * math.sqrt(2.0)))}
     print(json.dumps(line), flush=True)
